@@ -1,0 +1,375 @@
+"""Benchmark of the explicit snow-MPM step on GB300.
+
+Default workload (the plain large single scene): two snowballs colliding
+head-on at +-5 m/s, 1,048,576 particles (8 per cell), 256^3 grid, h = 1/256,
+dt = 2e-5, FAST mode (FP32, error <= 1e-5 vs the FP64 oracle per step).
+
+A step is one ExplicitTimeUpdate::update(dt) over the whole scene. The L2
+cache (129 MB) is flushed by writing a 256 MB buffer before each timed step;
+each step is timed with CUDA events on the library's stream.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0). --impl reference times the reference's own
+compute shaders compiled as C++ (oracle/_ref) on the host cores, or the
+oracle restatement when those are not built.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s batched vs per-scene at ≤1e-5 rel err; p50/p99 job latency"
+UNIT = "particle-steps/s"
+L2_FLUSH_BYTES = 256 << 20
+
+# Algorithmic bytes (FP32 SoA state): per particle-step P2G reads 72 B
+# (x, m, v, V0, F_E, J_p) and G2P + advance reads 64 B and writes 64 B;
+# per active grid node P2G writes 16 B, the grid update moves 40 B, G2P
+# reads 24 B.
+BYTES_P2G = (72, 16)
+BYTES_GRID = (0, 40)
+BYTES_G2P = (128, 24)
+
+
+def rank_info():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def kernels_per_step(n_colliders, sort_step, key_bits):
+    plain = (1 if n_colliders else 0) + 1 + 1 + 2 + 3  # rigid, begin, compact, 2 prefix, p2g, grid, g2p
+    if not sort_step:
+        return plain
+    passes = (key_bits + 7) // 8
+    return plain + 1 + passes * 5 + 3  # keys, (hist + 3 scan + scatter) per pass, permute, heads, items
+
+
+def bench_ours(args, local_rank):
+    import torch
+
+    from snow_gb300 import api, native as N, scenes
+
+    torch.cuda.set_device(local_rank)
+    t0 = time.time()
+    s = scenes.cfg2_two_snowballs(n=args.particles, grid_edge=args.grid)
+    gen_s = time.time() - t0
+    ctx = api.Context(local_rank)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    sim = api.SimScene(ctx, s, mode=N.MODE_FAST)
+    sim.upload().init()
+    n = s.n
+    dt = s.dt
+    # active grid nodes (nodes with mass) after one step, for the roofline
+    sim.step(dt, 1)
+    ctx.synchronize()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local_rank}")
+    for _ in range(args.warmup):
+        sim.step(dt, 1)
+    ctx.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with ClockSampler(local_rank) as clocks:
+        torch.cuda.synchronize()
+        for i in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                starts[i].record(stream)
+            sim.step(dt, 1)
+            with torch.cuda.stream(stream):
+                ends[i].record(stream)
+        torch.cuda.synchronize()
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    total_ms = sum(step_ms)
+    st = sim.stats()
+    if st["nonfinite"]:
+        raise RuntimeError("non-finite particle state in the timed run")
+
+    # per-kernel device time (eager launches with events around each phase)
+    ctx.set_profiling(True)
+    sim.phase_times(reset=True)
+    prof_steps = max(8, min(args.steps, 32))
+    sim.step(dt, prof_steps)
+    ph = sim.phase_times(reset=True)
+    ctx.set_profiling(False)
+
+    # active nodes: count from a dense download right after a P2G dispatch
+    sim.dispatch(N.K_RIGID_ADVANCE, dt)
+    sim.dispatch(N.K_P2G, dt)
+    g = sim.grid()
+    A = int(np.count_nonzero(g["mass"] > 0))
+    sim.dispatch(N.K_G_FORCE, dt)
+    sim.dispatch(N.K_G2P, dt)
+    del g
+
+    per = {k: ph[k] / max(ph["steps"], 1) for k in ("sort_ms", "p2g_ms", "grid_ms", "g2p_ms")}
+    peak, peak_kind = measured_peak_hbm()
+    dominant = max(("p2g_ms", "g2p_ms", "grid_ms"), key=lambda k: per[k])
+    b = {"p2g_ms": BYTES_P2G, "g2p_ms": BYTES_G2P, "grid_ms": BYTES_GRID}[dominant]
+    alg_bytes = b[0] * n + b[1] * A
+    achieved = alg_bytes / (per[dominant] * 1e-3) / 1e9
+
+    # end to end through the C ABI: upload from host arrays, init, per step
+    # one step + a device->host read of the step's bulk statistics, download.
+    e2e_steps = args.steps
+    t1 = time.perf_counter()
+    sim2 = api.SimScene(ctx, s, mode=N.MODE_FAST)
+    sim2.upload().init()
+    for _ in range(e2e_steps):
+        sim2.step(dt, 1)
+        sim2.stats()
+    out = sim2.download()
+    e2e_s = time.perf_counter() - t1
+    h2d = n * (12 + 12 + 4)
+    d2h_stats = 8 * 20
+    d2h_final = n * (12 + 12 + 36 + 4 + 4)
+    sim2.close()
+    del out
+
+    sort_every = sim.params.sort_interval or 8
+    key_bits = math.ceil(math.log2(((args.grid + 3) // 4) ** 3 * 64))
+    launches = 0
+    for i in range(args.steps):
+        launches += kernels_per_step(len(s.colliders), False, key_bits)
+    launches += (args.steps // sort_every) * (kernels_per_step(len(s.colliders), True, key_bits) -
+                                               kernels_per_step(len(s.colliders), False, key_bits))
+    res = dict(total_ms=total_ms, step_ms=step_ms, n=n, A=A, per=per, dominant=dominant, alg_bytes=alg_bytes,
+               achieved=achieved, peak=peak, peak_kind=peak_kind, clocks=clocks.summary(), e2e_s=e2e_s,
+               e2e_steps=e2e_steps, h2d=h2d, d2h=d2h_stats + d2h_final / e2e_steps, launches=launches,
+               gen_s=gen_s, stats=st, scene=s)
+    ctx.close()
+    return res
+
+
+def cpu_baseline_port(scene, steps=2):
+    """The oracle restatement in the shaders' FP32 arithmetic (FAITHFUL32) on
+    all host cores, on the same scene: `steps` full steps after init."""
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    o = O.OracleSim(scene, mode=O.FAITHFUL32, threads=threads).upload_std140(*scene.std140()).init()
+    t = time.perf_counter()
+    o.step(n=steps)
+    el = time.perf_counter() - t
+    return dict(value=scene.n * steps / el, unit=UNIT, cores=threads, kind="port",
+                sample=f"{steps} full steps of the same {scene.n}-particle scene, FP32 int32-fixed-point "
+                       f"restatement of the shaders, OpenMP over {threads} threads")
+
+
+def bench_reference(args):
+    """The reference's compute shaders compiled as C++ on the host cores.
+    Each timed step advances a particle sample of the workload's scene; the
+    full-scene rate is extrapolated from the measured per-step grid sweep
+    (a step with no particles) and the per-particle cost."""
+    from oracle import oracle as O
+    from snow_gb300 import scenes
+
+    threads = os.cpu_count() or 1
+    s = scenes.cfg2_two_snowballs(n=args.particles, grid_edge=args.grid)
+    rng = np.random.default_rng(7)
+    k = max(1, min(s.n, args.ref_sample))
+    idx = np.sort(rng.choice(s.n, size=k, replace=False))
+    sample = scenes.Scene(**{f: getattr(s, f) for f in ("grid_pos", "grid_dim", "grid_spacing", "young", "poisson",
+                                                        "hardening", "crit_compression", "crit_stretch", "alpha",
+                                                        "gravity", "dt", "colliders")})
+    sample.x, sample.v, sample.m = s.x[idx], s.v[idx], s.m[idx]
+    kind = "reference" if O.ref_lib() is not None else "port"
+    if kind == "reference":
+        sim = O.RefSim(sample, threads=threads).upload_std140(*sample.std140()).init()
+        stepper = lambda: sim.update()
+        empty = scenes.Scene(**{f: getattr(sample, f) for f in ("grid_pos", "grid_dim", "grid_spacing", "young",
+                                                                 "poisson", "hardening", "crit_compression",
+                                                                 "crit_stretch", "alpha", "gravity", "dt",
+                                                                 "colliders")})
+        empty.x, empty.v, empty.m = sample.x[:1], sample.v[:1], sample.m[:1]
+        esim = O.RefSim(empty, threads=threads).upload_std140(*empty.std140()).init()
+        estep = lambda: esim.update()
+    else:
+        sim = O.OracleSim(sample, mode=O.FAITHFUL32, threads=threads).upload_std140(*sample.std140()).init()
+        stepper = lambda: sim.step()
+        empty = None
+        estep = None
+    for _ in range(args.warmup):
+        stepper()
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        stepper()
+        times.append(time.perf_counter() - t)
+    t_sample = statistics.median(times)
+    t_grid = 0.0
+    if estep is not None:
+        et = []
+        for _ in range(3):
+            t = time.perf_counter()
+            estep()
+            et.append(time.perf_counter() - t)
+        t_grid = min(et)
+    per_particle = max(t_sample - t_grid, 1e-12) / k
+    t_full = t_grid + per_particle * s.n
+    value = s.n / t_full
+    sample_desc = (f"{k} of {s.n} particles of the workload scene per step ({args.steps} timed steps, "
+                   f"median {t_sample:.3f} s); full-scene rate extrapolated as N / (T_grid + N * t_particle) "
+                   f"with T_grid = {t_grid:.3f} s measured on a 1-particle step")
+    return dict(value=value, unit=UNIT, cores=threads, kind=kind, sample=sample_desc, t_sample=t_sample)
+
+
+def workload_config(args):
+    return {"workload": f"two snowballs colliding head-on at +-5 m/s, {args.particles} particles (8 per cell), "
+                        f"{args.grid}^3 grid, h=1/{args.grid}, dt=2e-5, FAST mode",
+            "particles": args.particles, "grid": f"{args.grid}^3", "dt": 2e-5, "mode": "fast (FP32)",
+            "l2": "flushed (256 MB write) before every timed step", "parallelism": "replicas"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=64)
+    ap.add_argument("--warmup", type=int, default=8)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--particles", type=int, default=1 << 20)
+    ap.add_argument("--grid", type=int, default=256)
+    ap.add_argument("--ref-sample", type=int, default=32768)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world, local_rank = rank_info()
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        r = bench_reference(args)
+        line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * args.particles / r["value"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32+i32", "data": "synthetic",
+                "config": workload_config(args), "impl": "reference",
+                "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": r["cores"], "kind": r["kind"],
+                                 "sample": r["sample"]},
+                "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    res = bench_ours(args, local_rank)
+    total_ms = res["total_ms"]
+    if dist is not None:
+        import torch
+        t = torch.tensor([total_ms], device=f"cuda:{local_rank}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+        dist.barrier()
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return 0
+    n = res["n"]
+    value = world * n * args.steps / (total_ms * 1e-3)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered lattice)",
+        "config": workload_config(args),
+        "roofline": {"bound": "hbm", "kernel": res["dominant"].replace("_ms", ""), "achieved": res["achieved"],
+                     "peak": res["peak"], "unit": "GB/s", "frac": res["achieved"] / res["peak"],
+                     "peak_source": res["peak_kind"], "traffic": None,
+                     "algorithmic_bytes_per_launch": res["alg_bytes"], "active_nodes": res["A"]},
+        "phase_ms": {k.replace("_ms", ""): v for k, v in res["per"].items()},
+        "clocks": res["clocks"],
+        "e2e": {"value": n * res["e2e_steps"] / res["e2e_s"], "unit": UNIT,
+                "h2d_bytes_per_step": res["h2d"] / res["e2e_steps"], "d2h_bytes_per_step": res["d2h"],
+                "note": "upload + init + per-step (step + stats read) + download through the C ABI"},
+        "gpu_launches": res["launches"],
+        "step_ms_p50": statistics.median(res["step_ms"]), "step_ms_max": max(res["step_ms"]),
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_port(res["scene"], steps=2)
+    print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,212 @@
+/*
+ * snow_mpm.h -- C ABI of the GB300-native explicit snow-MPM step.
+ *
+ * The library replaces the explicit time-integration stage of MeyerFabian/snow:
+ *
+ *   reference                                          this ABI
+ *   ---------------------------------------------------------------------------
+ *   TimeUpdate(PhysicalScene&&) + init() + update(dt)   snow_scene_create / _upload /
+ *     (src/snow/simulation/timeUpdate.hpp:10-18)          snow_scene_init / snow_scene_step
+ *   ExplicitTimeUpdate::init                            snow_scene_init
+ *     (src/snow/simulation/timeUpdate/explicittimeupdate.cpp:4-34)
+ *   ExplicitTimeUpdate::update(double dt)               snow_scene_step(scene, dt, 1)
+ *     (explicittimeupdate.cpp:36-63)
+ *   Technique::dispatch_with_barrier per kernel         snow_dispatch(scene, SNOW_K_*, dt)
+ *     (src/snow/simulation/computingTechnique/*.cpp)
+ *   ParticleSystem::initSSBO std140 buffers             snow_scene_upload_std140 /
+ *     (src/snow/object/particlesystem.cpp:101-228)        snow_scene_download_std140
+ *   CollisionObjects::initSSBO cx/cv/cn                 snow_collider (48 bytes = cx, cv, cn)
+ *     (src/snow/object/collisionObjects.cpp:25-66)
+ *   defines.hpp constants                               snow_params_default
+ *     (src/snow/utils/defines.hpp:14-54)
+ *   launchSnow's six wall half-planes                   snow_default_walls
+ *     (src/snow/utils/launchHelper/explicit.cpp:9-67)
+ *
+ * Conventions: the caller owns every host array; the library owns device
+ * memory and runs on one CUDA stream per context. Calls return snow_status
+ * (0 = success, negative = error; snow_last_error gives the text). No C++
+ * exception crosses the ABI. A context is used by one host thread at a time.
+ * Matrices in the plain (non-std140) calls are N x 9 row-major floats:
+ * F[p][r][c] at 9p + 3r + c.
+ */
+#ifndef SNOW_MPM_H
+#define SNOW_MPM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum snow_status {
+  SNOW_OK = 0,
+  SNOW_EINVAL = -1,       /* invalid argument */
+  SNOW_ENOMEM = -2,       /* device allocation failed */
+  SNOW_EBUDGET = -3,      /* the context's HBM budget would be exceeded */
+  SNOW_ETIMEDOUT = -4,    /* a bounded wait expired */
+  SNOW_ENUMERIC = -5,     /* NaN / Inf particle state detected */
+  SNOW_ECUDA = -6,        /* CUDA runtime error */
+  SNOW_ESTATE = -7,       /* call out of order (step before init, ...) */
+  SNOW_EUNSUPPORTED = -8, /* not available in this scene's mode */
+  SNOW_ECAPACITY = -9     /* sparse grid block pool overflowed */
+} snow_status;
+
+typedef enum snow_mode {
+  /* The shaders' arithmetic: int32 fixed-point grid and particle
+   * accumulators (x1e8 / x1e6, truncating), V rounded to 1e-5 in the SVD,
+   * R / F_E / F_P rounded to 1e-9, dense grid, std140 device buffers. */
+  SNOW_MODE_REFERENCE = 0,
+  /* FP32 throughout with float accumulation, no quantisation, J_p tracked as
+   * a scalar, sparse blocked grid, shared-memory tiled P2G. */
+  SNOW_MODE_FAST = 1
+} snow_mode;
+
+/* Kernels of one explicit step, named after the reference's Techniques. */
+typedef enum snow_kernel {
+  SNOW_K_RIGID_ADVANCE = 0, /* rigidAdvance.glsl      */
+  SNOW_K_G_RESET = 1,       /* gReset.glsl            */
+  SNOW_K_P2G = 2,           /* p2gTransfer.glsl       */
+  SNOW_K_G_FORCE = 3,       /* gForceCompute.glsl     */
+  SNOW_K_G2P = 4,           /* g2pTransfer.glsl       */
+  SNOW_K_P_ADVANCE = 5,     /* particleAdvance.glsl   */
+  SNOW_K_G_MASS = 6,        /* gMassCompute.glsl      */
+  SNOW_K_P_VOLUME = 7       /* pVolumeCompute.glsl    */
+} snow_kernel;
+
+typedef struct snow_params {
+  float grid_pos[3];      /* GRID_POS_X/Y/Z                       */
+  int grid_dim[3];        /* GRID_DIM_X/Y/Z                       */
+  float grid_spacing;     /* GRID_SPACING                         */
+  float young;            /* YOUNG_MODULUS  (E0)                  */
+  float poisson;          /* POISSON        (nu)                  */
+  float hardening;        /* HARDENING      (xi)                  */
+  float crit_compression; /* CRIT_COMPRESSION (theta_c)           */
+  float crit_stretch;     /* CRIT_STRETCH     (theta_s)           */
+  float alpha;            /* PIC/FLIP blend, 0.95 in the shaders  */
+  float gravity[3];       /* (0, -9.81, 0) in gForceCompute.glsl  */
+  int mode;               /* snow_mode                            */
+  int sort_interval;      /* FAST: re-bin particles every k steps (0 = library default) */
+} snow_params;
+
+/* One collision object: the reference's cx = (pos, type), cv = (vel,
+ * radius), cn = (normal, friction) vec4 triple. type 0 = half-plane through
+ * pos with normal; type 1 = sphere of radius about pos. */
+typedef struct snow_collider {
+  float pos[3];
+  int32_t type;
+  float vel[3];
+  float radius;
+  float normal[3];
+  float friction;
+} snow_collider;
+
+/* Bulk statistics of one scene (for horizons where trajectories diverge). */
+typedef struct snow_stats {
+  double mass;              /* sum m_p                  */
+  double momentum[3];       /* sum m_p v_p              */
+  double kinetic_energy;    /* sum 0.5 m_p |v_p|^2      */
+  double center_of_mass[3];
+  double bbox_min[3], bbox_max[3];
+  double mean_jp;           /* mean det F_P             */
+  uint64_t nonfinite;       /* particles with a NaN / Inf field */
+  uint64_t n;
+} snow_stats;
+
+/* Device-timed phases of snow_scene_step when profiling is on (ms, summed
+ * over steps since the last reset). */
+typedef struct snow_phase_times {
+  double sort_ms, p2g_ms, grid_ms, g2p_ms, other_ms, total_ms;
+  uint64_t steps;
+} snow_phase_times;
+
+typedef struct snow_ctx snow_ctx;
+typedef struct snow_scene snow_scene;
+typedef struct snow_batch snow_batch;
+
+/* defines.hpp defaults; mode = SNOW_MODE_FAST. */
+void snow_params_default(snow_params* p);
+/* The six wall half-planes of explicit.cpp:9-67 for p's grid; returns 6. */
+int snow_default_walls(const snow_params* p, snow_collider out[6]);
+
+snow_status snow_ctx_create(int device, size_t hbm_budget_bytes, snow_ctx** out);
+/* Also destroys every scene and batch of the context still alive; their
+ * handles are invalid afterwards. */
+void snow_ctx_destroy(snow_ctx* ctx);
+const char* snow_last_error(const snow_ctx* ctx);
+size_t snow_ctx_bytes_in_use(const snow_ctx* ctx);
+snow_status snow_ctx_set_profiling(snow_ctx* ctx, int on);
+/* The cudaStream_t every call of this context launches on, for callers that
+ * order or time their own GPU work against it. */
+void* snow_ctx_stream(const snow_ctx* ctx);
+snow_status snow_ctx_synchronize(snow_ctx* ctx);
+
+/* A scene holds up to `capacity` particles (0 = take n from the first upload). */
+snow_status snow_scene_create(snow_ctx* ctx, const snow_params* p, const snow_collider* colliders,
+                              int n_colliders, size_t capacity, snow_scene** out);
+/* Also destroys the batches that hold this scene. */
+void snow_scene_destroy(snow_scene* s);
+/* Device bytes a scene with these parameters and n particles will hold. */
+size_t snow_scene_footprint(const snow_params* p, size_t n);
+
+/* x, v: N x 3; m: N; FE, FP: N x 9 row-major or NULL for identity. */
+snow_status snow_scene_upload(snow_scene* s, const float* x, const float* v, const float* m, const float* FE,
+                              const float* FP, size_t n);
+/* The reference's buffers as ParticleSystem::initSSBO fills them: pxm N x
+ * vec4 (x, m), pv N x ivec4 (v*1e8, density*1e6), pFE / pFP N x mat4
+ * (column-major). */
+snow_status snow_scene_upload_std140(snow_scene* s, const float* pxm, const int32_t* pv, const float* pFE,
+                                     const float* pFP, size_t n);
+/* Sets the initial particle volume V0 = m / rho0 (N floats) instead of
+ * letting snow_scene_init derive it from the first grid mass (pVolumeCompute).
+ * Call after an upload and before snow_scene_init; init then keeps it. Used to
+ * resume a scene from a saved state. */
+snow_status snow_scene_set_volume(snow_scene* s, const float* volume, size_t n);
+/* ExplicitTimeUpdate::init: grid reset, grid mass, particle density. */
+snow_status snow_scene_init(snow_scene* s);
+/* n_steps x ExplicitTimeUpdate::update(dt). Asynchronous: returns once the
+ * work is queued; errors found on the device surface at the next call that
+ * synchronises (download, stats, snow_ctx_synchronize). */
+snow_status snow_scene_step(snow_scene* s, double dt, int n_steps);
+/* One kernel of the step (per-kernel parity checks). In SNOW_MODE_FAST the
+ * gather and the particle update are one kernel: SNOW_K_G2P runs both and
+ * SNOW_K_P_ADVANCE does nothing; SNOW_K_G_RESET does nothing (the block pool
+ * is cleared as the grid update consumes it). */
+snow_status snow_dispatch(snow_scene* s, int kernel, double dt);
+
+/* Any pointer may be NULL. FP is only kept in SNOW_MODE_REFERENCE (FAST
+ * returns SNOW_EUNSUPPORTED if FP is requested); Jp = det F_P; volume =
+ * initial particle volume m / rho0. */
+snow_status snow_scene_download(snow_scene* s, float* x, float* v, float* FE, float* FP, float* Jp, float* volume);
+snow_status snow_scene_download_std140(snow_scene* s, float* pxm, int32_t* pv, float* pFE, float* pFP);
+/* Dense G = X*Y*Z grid arrays after P2G / the grid update: mass G, momentum
+ * G x 3, force G x 3, vstar G x 3 (post-collision velocity). */
+snow_status snow_scene_download_grid(snow_scene* s, float* mass, float* momentum, float* force, float* vstar);
+snow_status snow_scene_download_colliders(snow_scene* s, snow_collider* out);
+snow_status snow_scene_stats(snow_scene* s, snow_stats* out);
+size_t snow_scene_size(const snow_scene* s);
+
+/* Particle -> cell binning as used by the FAST path: per-particle block-major
+ * cell key (block (i>>2, j>>2, k>>2) numbered x fastest, times 64, plus
+ * (i&3) + 4(j&3) + 16(k&3), cell = trunc((x - grid_pos)/h) clamped to the
+ * grid) and the stable sort permutation (perm[k] = particle at rank k).
+ * Computed on the device from the current positions. */
+snow_status snow_scene_cell_keys(snow_scene* s, uint32_t* keys, uint32_t* perm);
+
+snow_status snow_scene_phase_times(snow_scene* s, snow_phase_times* out, int reset);
+
+/* Batched stepping of many independent scenes (all SNOW_MODE_FAST): one
+ * launch per phase covers every scene, the whole step is a CUDA graph. */
+snow_status snow_batch_create(snow_ctx* ctx, snow_scene* const* scenes, int n, snow_batch** out);
+void snow_batch_destroy(snow_batch* b);
+/* dt: one per scene (NULL = each scene's last dt or 1e-3). */
+snow_status snow_batch_step(snow_batch* b, const double* dt, int n_steps);
+/* Tunes tile/block/sort parameters on the batch by timing a few steps; the
+ * choice is kept in the batch (and reported in *choice_out if non-NULL). */
+snow_status snow_batch_autotune(snow_batch* b, const double* dt, int* choice_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SNOW_MPM_H */

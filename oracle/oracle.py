@@ -49,6 +49,7 @@ def lib():
         _lib.oracle_download_grid_fixed.argtypes = [C.c_void_p, ip, ip]
         _lib.oracle_download_accumulators.argtypes = [C.c_void_p, dp, dp]
         _lib.oracle_download_colliders.argtypes = [C.c_void_p, dp]
+        _lib.oracle_set_density.argtypes = [C.c_void_p, dp]
         _lib.oracle_svd.argtypes = [dp, dp, dp, dp, C.c_int, C.c_int, C.c_int]
         _lib.oracle_lame.argtypes = [C.c_float, C.c_float, C.c_float, C.c_float, fp, fp]
         _lib.oracle_cell_keys.argtypes = [fp, C.c_size_t, fp, ip, C.c_float, up, up, up]
@@ -171,6 +172,11 @@ class OracleSim:
 
     def init(self):
         self.L.oracle_init(self.h)
+        return self
+
+    def set_density(self, rho):
+        r = np.ascontiguousarray(rho, np.float64)
+        self.L.oracle_set_density(self.h, _p(r, C.c_double))
         return self
 
     def step(self, dt=None, n=1):

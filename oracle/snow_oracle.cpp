@@ -347,6 +347,7 @@ struct OracleBase {
   virtual void download_grid_fixed(int* gv, int* gf) const = 0;
   virtual void download_accumulators(double* vpic, double* dv) const = 0;
   virtual void download_colliders(double* pos) const = 0;
+  virtual void set_density(const double* rho) = 0;
 };
 
 enum {
@@ -894,6 +895,15 @@ struct Oracle : OracleBase {
     }
   }
 
+  void set_density(const double* rh) override {
+    for (size_t p = 0; p < N; p++) {
+      if (FIXED)
+        rhoi[p] = (int)(float(rh[p]) * 1e6f);
+      else
+        rho[p] = R(rh[p]);
+    }
+  }
+
   void download_colliders(double* out) const override {
     for (size_t i = 0; i < cpos.size(); i++)
       for (int k = 0; k < 3; k++) out[3 * i + k] = double(cpos[i][k]);
@@ -958,6 +968,7 @@ void oracle_download_grid_fixed(void* h, int* gv, int* gf) {
 void oracle_download_accumulators(void* h, double* vpic, double* dv) {
   static_cast<OracleBase*>(h)->download_accumulators(vpic, dv);
 }
+void oracle_set_density(void* h, const double* rho) { static_cast<OracleBase*>(h)->set_density(rho); }
 void oracle_download_colliders(void* h, double* pos) { static_cast<OracleBase*>(h)->download_colliders(pos); }
 
 // 3x3 SVD of row-major matrices (KAT / property tests): A = W S V^T.

@@ -1,0 +1,1212 @@
+// Host runtime behind include/snow_mpm.h: contexts, scenes, uploads and
+// downloads, the step sequence (captured in CUDA graphs), batches.
+//
+// The step follows ExplicitTimeUpdate::update
+// (src/snow/simulation/timeUpdate/explicittimeupdate.cpp:36-63):
+// rigid advance -> grid reset -> P2G -> grid update -> G2P -> particle advance.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <set>
+#include <string>
+#include <vector>
+
+#include "snow_internal.h"
+
+using namespace snow;
+
+struct snow_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  size_t budget = 0;
+  size_t used = 0;
+  std::string err;
+  bool profiling = false;
+  StatsAccum* d_stats = nullptr;
+  StatsAccum* h_stats = nullptr;  // pinned
+  int* h_counters = nullptr;      // pinned, kCounterStride ints
+  cudaEvent_t ev[8] = {};
+  // live children, destroyed with the context if the caller did not
+  std::set<snow_scene*> scenes;
+  std::set<snow_batch*> batches;
+};
+
+struct snow_scene {
+  snow_ctx* ctx = nullptr;
+  snow_params p{};
+  int mode = SNOW_MODE_FAST;
+  size_t cap = 0;
+  size_t n = 0;
+  bool uploaded = false;
+  bool initialized = false;
+  std::vector<snow_collider> coll_h;
+  snow_collider* coll_d = nullptr;
+  int ncoll = 0;
+  std::vector<std::pair<void*, size_t>> allocs;
+  size_t bytes = 0;
+  long long G = 0;
+  // reference mode
+  RefArgs ra{};
+  // fast mode
+  SceneDev sd{};
+  SceneDev* sd_dev = nullptr;
+  BinScratch bin{};
+  FastTuning tune{};
+  int key_bits = 0;
+  int* d_prefix = nullptr;  // [0,2) items, [2,4) active, [4,6) chunks, [6,8) blocks
+  int steps_since_sort = 1 << 30;
+  int version = 0;
+  bool volume_given = false;
+  // graphs of one step, keyed by (dt, with sort)
+  cudaGraphExec_t g_plain = nullptr, g_sort = nullptr;
+  float g_dt = NAN;
+  snow_phase_times times{};
+  float last_dt = 1e-3f;
+};
+
+struct snow_batch {
+  snow_ctx* ctx = nullptr;
+  std::vector<snow_scene*> scenes;
+  SceneDev* d_scenes = nullptr;
+  int* d_prefix = nullptr;  // items (n+1), active (n+1), chunks (n+1), blocks (n+1)
+  std::vector<int> versions;
+  long long total_chunks = 0, total_blocks = 0;
+  int step_count = 0;
+  std::map<int, cudaGraphExec_t> graphs;  // phase (step % sort_interval) -> graph
+  std::vector<float> g_dt;
+  int g_threads = 0;
+  size_t bytes = 0;
+  std::vector<std::pair<void*, size_t>> allocs;
+};
+
+// ---------------------------------------------------------------------------
+namespace {
+
+snow_status fail(snow_ctx* c, snow_status st, const std::string& msg) {
+  if (c) c->err = msg;
+  return st;
+}
+
+snow_status cuda_fail(snow_ctx* c, cudaError_t e, const char* what) {
+  cudaGetLastError();
+  char buf[256];
+  snprintf(buf, sizeof buf, "%s: %s", what, cudaGetErrorString(e));
+  return fail(c, SNOW_ECUDA, buf);
+}
+
+#define CK(x)                                            \
+  do {                                                   \
+    cudaError_t e_ = (x);                                \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #x); \
+  } while (0)
+
+snow_status dalloc(snow_ctx* ctx, std::vector<std::pair<void*, size_t>>& owner, size_t& owner_bytes, size_t bytes,
+                   void** out) {
+  *out = nullptr;
+  if (bytes == 0) return SNOW_OK;
+  bytes = (bytes + 255) & ~(size_t)255;
+  if (ctx->budget && ctx->used + bytes > ctx->budget)
+    return fail(ctx, SNOW_EBUDGET, "HBM budget exceeded");
+  const cudaError_t e = cudaMalloc(out, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *out = nullptr;
+    return fail(ctx, SNOW_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  ctx->used += bytes;
+  owner_bytes += bytes;
+  owner.emplace_back(*out, bytes);
+  return SNOW_OK;
+}
+
+void dfree_all(snow_ctx* ctx, std::vector<std::pair<void*, size_t>>& owner, size_t& owner_bytes) {
+  for (auto& a : owner) {
+    cudaFree(a.first);
+    ctx->used -= a.second;
+  }
+  owner.clear();
+  owner_bytes = 0;
+}
+
+void dfree_one(snow_ctx* ctx, snow_scene* s, void* p) {
+  for (size_t i = 0; i < s->allocs.size(); i++)
+    if (s->allocs[i].first == p) {
+      cudaFree(p);
+      ctx->used -= s->allocs[i].second;
+      s->bytes -= s->allocs[i].second;
+      s->allocs.erase(s->allocs.begin() + (long)i);
+      return;
+    }
+}
+
+template <class T>
+snow_status salloc(snow_scene* s, size_t count, T** out) {
+  return dalloc(s->ctx, s->allocs, s->bytes, count * sizeof(T), reinterpret_cast<void**>(out));
+}
+
+int ceil_log2(unsigned long long v) {
+  int b = 0;
+  while ((1ull << b) < v) b++;
+  return b;
+}
+
+void drop_graphs(snow_scene* s) {
+  if (s->g_plain) cudaGraphExecDestroy(s->g_plain);
+  if (s->g_sort) cudaGraphExecDestroy(s->g_sort);
+  s->g_plain = s->g_sort = nullptr;
+  s->g_dt = NAN;
+}
+
+bool valid_params(const snow_params* p) {
+  if (!p) return false;
+  for (int k = 0; k < 3; k++)
+    if (p->grid_dim[k] <= 0 || p->grid_dim[k] > 4096) return false;
+  if (!(p->grid_spacing > 0.0f)) return false;
+  if ((double)p->grid_dim[0] * p->grid_dim[1] * p->grid_dim[2] > 2.0e9) return false;
+  if (p->mode != SNOW_MODE_REFERENCE && p->mode != SNOW_MODE_FAST) return false;
+  return true;
+}
+
+void fill_sd_params(snow_scene* s) {
+  SceneDev& d = s->sd;
+  for (int k = 0; k < 3; k++) {
+    d.gpos[k] = s->p.grid_pos[k];
+    d.dim[k] = s->p.grid_dim[k];
+    d.bdim[k] = (s->p.grid_dim[k] + 3) / 4;
+    d.grav[k] = s->p.gravity[k];
+  }
+  d.h = s->p.grid_spacing;
+  d.nblocks = d.bdim[0] * d.bdim[1] * d.bdim[2];
+  d.young = s->p.young;
+  d.poisson = s->p.poisson;
+  d.hardening = s->p.hardening;
+  d.crit_lo = 1.0f - s->p.crit_compression;
+  d.crit_hi = 1.0f + s->p.crit_stretch;
+  d.alpha = s->p.alpha;
+  d.ncoll = s->ncoll;
+  d.coll = s->coll_d;
+}
+
+snow_status push_sd(snow_scene* s) {
+  snow_ctx* ctx = s->ctx;
+  CK(cudaMemcpyAsync(s->sd_dev, &s->sd, sizeof(SceneDev), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  s->version++;
+  drop_graphs(s);
+  return SNOW_OK;
+}
+
+// ---- fast-mode buffers ----------------------------------------------------
+snow_status fast_alloc_particles(snow_scene* s, size_t cap) {
+  SceneDev& d = s->sd;
+  snow_status st;
+  if ((st = salloc(s, cap, &d.xm)) || (st = salloc(s, cap, &d.vv)) || (st = salloc(s, cap, &d.fa)) ||
+      (st = salloc(s, cap, &d.fb)) || (st = salloc(s, cap, &d.fc)) || (st = salloc(s, cap, &d.pid)))
+    return st;
+  BinScratch& b = s->bin;
+  const size_t tiles = radix_tiles(cap);
+  const size_t hist = 256 * tiles;
+  const size_t partial = (hist + 4095) / 4096 + 1;
+  if ((st = salloc(s, cap, &b.keys[0])) || (st = salloc(s, cap, &b.keys[1])) || (st = salloc(s, cap, &b.vals[0])) ||
+      (st = salloc(s, cap, &b.vals[1])) || (st = salloc(s, hist, &b.hist)) || (st = salloc(s, partial, &b.scan_tmp)) ||
+      (st = salloc(s, cap, &b.tmp4[0])) || (st = salloc(s, cap, &b.tmp4[1])) || (st = salloc(s, cap, &b.tmp4[2])) ||
+      (st = salloc(s, cap, &b.tmp4[3])) || (st = salloc(s, cap, &b.tmp2)) || (st = salloc(s, cap, &b.tmp_pid)))
+    return st;
+  b.n_cap = cap;
+  const int items_max = s->tune.p2g_items_max;
+  d.item_cap = (int)(cap / items_max + std::min<size_t>(cap, (size_t)d.nblocks) + 1);
+  if ((st = salloc(s, (size_t)d.item_cap, &d.items))) return st;
+  return SNOW_OK;
+}
+
+snow_status fast_alloc_grid(snow_scene* s) {
+  SceneDev& d = s->sd;
+  snow_status st;
+  const size_t nb = (size_t)d.nblocks;
+  if ((st = salloc(s, nb, &d.blk_slot)) || (st = salloc(s, nb, &d.blk_flag)) ||
+      (st = salloc(s, nb, &s->bin.bstart)) || (st = salloc(s, nb, &s->bin.bend)) ||
+      (st = salloc(s, nb, &s->bin.home)) || (st = salloc(s, (size_t)kCounterStride, &d.counters)) ||
+      (st = salloc(s, (size_t)8, &s->d_prefix)) || (st = salloc(s, (size_t)1, &s->sd_dev)))
+    return st;
+  snow_ctx* ctx = s->ctx;
+  CK(cudaMemsetAsync(d.blk_flag, 0, nb * sizeof(int), ctx->stream));
+  CK(cudaMemsetAsync(d.blk_slot, 0xff, nb * sizeof(int), ctx->stream));
+  CK(cudaMemsetAsync(d.counters, 0, kCounterStride * sizeof(int), ctx->stream));
+  return SNOW_OK;
+}
+
+snow_status fast_alloc_pool(snow_scene* s, int cap_blocks) {
+  SceneDev& d = s->sd;
+  snow_ctx* ctx = s->ctx;
+  if (d.acc) dfree_one(ctx, s, d.acc);
+  if (d.gout) dfree_one(ctx, s, d.gout);
+  if (d.active) dfree_one(ctx, s, d.active);
+  d.acc = d.gout = nullptr;
+  d.active = nullptr;
+  snow_status st;
+  if ((st = salloc(s, (size_t)cap_blocks * kAccBlockFloats, &d.acc)) ||
+      (st = salloc(s, (size_t)cap_blocks * kOutBlockFloats, &d.gout)) || (st = salloc(s, (size_t)cap_blocks, &d.active)))
+    return st;
+  CK(cudaMemsetAsync(d.acc, 0, (size_t)cap_blocks * kAccBlockFloats * sizeof(float), ctx->stream));
+  d.pool_cap = cap_blocks;
+  return SNOW_OK;
+}
+
+// Host prefix arrays of a one-scene "batch": [items 0,1][active 2,3][chunks 4,5][blocks 6,7].
+snow_status fast_single_prefix(snow_scene* s) {
+  snow_ctx* ctx = s->ctx;
+  const int chunk = s->tune.g2p_threads;
+  int h[8] = {0, 0, 0, 0, 0, (int)((s->n + chunk - 1) / chunk), 0, s->sd.nblocks};
+  CK(cudaMemcpyAsync(s->d_prefix + 4, h + 4, 4 * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SNOW_OK;
+}
+
+int p2g_ctas(const snow_scene* s) { return num_sms() * (s->tune.p2g_threads >= 256 ? 4 : 8); }
+int grid_ctas() { return num_sms() * 8; }
+
+// Binning: keys, radix sort, permutation, work items.
+void fast_bin(snow_scene* s, cudaStream_t st) {
+  fast_sort_keys(s->sd, s->sd_dev, s->bin, s->key_bits, st);
+  fast_apply_bins(s->sd, s->sd_dev, s->bin, s->tune.p2g_items_max, st);
+}
+
+// The step's kernels for a one-scene batch (enqueue only).
+void fast_enqueue_p2g(snow_scene* s, bool bin, bool mass_only, cudaStream_t st) {
+  if (bin) fast_bin(s, st);
+  fast_begin_step(s->sd_dev, 1, st);
+  fast_compact(s->sd_dev, s->d_prefix + 6, 1, s->sd.nblocks, st);
+  fast_prefix(s->sd_dev, 1, CNT_ITEMS, s->d_prefix + 0, st);
+  fast_prefix(s->sd_dev, 1, CNT_ACTIVE, s->d_prefix + 2, st);
+  fast_p2g(s->sd_dev, s->d_prefix + 0, 1, p2g_ctas(s), mass_only, s->tune.p2g_threads, st);
+}
+void fast_enqueue_grid(snow_scene* s, cudaStream_t st) { fast_grid(s->sd_dev, s->d_prefix + 2, 1, grid_ctas(), false, st); }
+void fast_enqueue_g2p(snow_scene* s, cudaStream_t st) {
+  const int chunk = s->tune.g2p_threads;
+  fast_g2p_advance(s->sd_dev, s->d_prefix + 4, 1, (long long)((s->n + chunk - 1) / chunk), chunk, st);
+}
+void fast_enqueue_step(snow_scene* s, bool bin, cudaStream_t st) {
+  if (s->ncoll > 0) fast_rigid(s->sd_dev, 1, nullptr, st);
+  fast_enqueue_p2g(s, bin, false, st);
+  fast_enqueue_grid(s, st);
+  fast_enqueue_g2p(s, st);
+}
+
+snow_status set_dt(snow_scene* s, float dt) {
+  if (s->sd.dt != dt) {
+    s->sd.dt = dt;
+    return push_sd(s);
+  }
+  return SNOW_OK;
+}
+
+// Checks device-side error counters; grows the block pool when it runs full.
+snow_status fast_check(snow_scene* s) {
+  snow_ctx* ctx = s->ctx;
+  CK(cudaMemcpyAsync(ctx->h_counters, s->sd.counters, kCounterStride * sizeof(int), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  const int active = ctx->h_counters[CNT_ACTIVE];
+  const int overflow = ctx->h_counters[CNT_OVERFLOW];
+  const int nonfinite = ctx->h_counters[CNT_NONFINITE];
+  if (overflow > 0) return fail(ctx, SNOW_ECAPACITY, "grid block pool overflowed");
+  if (nonfinite > 0) return fail(ctx, SNOW_ENUMERIC, "non-finite particle state");
+  if (active > (s->sd.pool_cap * 3) / 4 && s->sd.pool_cap < s->sd.nblocks) {
+    const int want = std::min(s->sd.nblocks, std::max(2 * active, s->sd.pool_cap + 1024));
+    snow_status st = fast_alloc_pool(s, want);
+    if (st) return st;
+    return push_sd(s);
+  }
+  return SNOW_OK;
+}
+
+snow_status fast_init(snow_scene* s) {
+  snow_ctx* ctx = s->ctx;
+  cudaStream_t st = ctx->stream;
+  snow_status r;
+  s->sd.n = (int)s->n;
+  if ((r = fast_single_prefix(s))) return r;
+  if ((r = push_sd(s))) return r;
+  fast_bin(s, st);
+  // size the block pool from the blocks the particles touch now
+  const int chunk = s->tune.g2p_threads;
+  const long long chunks = (long long)((s->n + chunk - 1) / chunk);
+  fast_mark(s->sd_dev, s->d_prefix + 4, 1, chunks, st);
+  CK(cudaMemsetAsync(s->sd.counters + CNT_ACTIVE, 0, sizeof(int), st));
+  fast_count_flags(s->sd_dev, s->sd.nblocks, st);
+  CK(cudaMemcpyAsync(ctx->h_counters, s->sd.counters, kCounterStride * sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  const int touched = ctx->h_counters[CNT_ACTIVE];
+  const int cap = std::min(s->sd.nblocks, std::max(2 * touched + 1024, 4096));
+  if ((r = fast_alloc_pool(s, cap))) return r;
+  if ((r = push_sd(s))) return r;
+  // gMassCompute + pVolumeCompute (explicittimeupdate.cpp:29-33)
+  fast_enqueue_p2g(s, false, true, st);
+  if (!s->volume_given) fast_volume(s->sd_dev, s->d_prefix + 4, 1, chunks, st);
+  fast_grid(s->sd_dev, s->d_prefix + 2, 1, grid_ctas(), true, st);  // clear the pool
+  fast_mark(s->sd_dev, s->d_prefix + 4, 1, chunks, st);             // blocks of step 1
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(st));
+  s->steps_since_sort = 0;
+  return SNOW_OK;
+}
+
+RefArgs& ref_args(snow_scene* s) {
+  RefArgs& a = s->ra;
+  for (int k = 0; k < 3; k++) {
+    a.gpos[k] = s->p.grid_pos[k];
+    a.dim[k] = s->p.grid_dim[k];
+    a.grav[k] = s->p.gravity[k];
+  }
+  a.h = s->p.grid_spacing;
+  a.young = s->p.young;
+  a.poisson = s->p.poisson;
+  a.hardening = s->p.hardening;
+  a.crit_c = s->p.crit_compression;
+  a.crit_s = s->p.crit_stretch;
+  a.alpha = s->p.alpha;
+  a.ncoll = s->ncoll;
+  a.coll = s->coll_d;
+  a.n = (int)s->n;
+  a.G = s->G;
+  return a;
+}
+
+snow_status ref_alloc(snow_scene* s, size_t cap) {
+  RefArgs& a = s->ra;
+  snow_status st;
+  if ((st = salloc(s, cap, &a.pxm)) || (st = salloc(s, cap, &a.pv)) || (st = salloc(s, 4 * cap, &a.pfe)) ||
+      (st = salloc(s, 4 * cap, &a.pfp)) || (st = salloc(s, cap, &a.pvn)) || (st = salloc(s, cap, &a.pd0)) ||
+      (st = salloc(s, cap, &a.pd1)) || (st = salloc(s, cap, &a.pd2)))
+    return st;
+  if (!a.gv) {
+    if ((st = salloc(s, (size_t)s->G, &a.gv)) || (st = salloc(s, (size_t)s->G, &a.gf)) ||
+        (st = salloc(s, (size_t)s->G, &a.gvn)))
+      return st;
+  }
+  return SNOW_OK;
+}
+
+snow_status ensure_capacity(snow_scene* s, size_t n) {
+  if (n == 0) return fail(s->ctx, SNOW_EINVAL, "no particles");
+  if (n > 0x7fffffffull) return fail(s->ctx, SNOW_EINVAL, "too many particles");
+  if (s->cap == 0) {
+    s->cap = n;
+    return s->mode == SNOW_MODE_FAST ? fast_alloc_particles(s, n) : ref_alloc(s, n);
+  }
+  if (n > s->cap) return fail(s->ctx, SNOW_EINVAL, "more particles than the scene's capacity");
+  return SNOW_OK;
+}
+
+double det_rowmajor(const float* f) {
+  const double a = f[0], b = f[1], c = f[2], d = f[3], e = f[4], g = f[5], h = f[6], i = f[7], j = f[8];
+  return a * (e * j - g * i) - b * (d * j - g * h) + c * (d * i - e * h);
+}
+
+snow_status fast_upload_soa(snow_scene* s, const std::vector<float4>& xm, const std::vector<float4>& vv,
+                            const std::vector<float4>& fa, const std::vector<float4>& fb,
+                            const std::vector<float2>& fc) {
+  snow_ctx* ctx = s->ctx;
+  const size_t n = xm.size();
+  std::vector<uint32_t> pid(n);
+  for (size_t i = 0; i < n; i++) pid[i] = (uint32_t)i;
+  CK(cudaMemcpyAsync(s->sd.xm, xm.data(), n * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(s->sd.vv, vv.data(), n * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(s->sd.fa, fa.data(), n * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(s->sd.fb, fb.data(), n * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(s->sd.fc, fc.data(), n * sizeof(float2), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(s->sd.pid, pid.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SNOW_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+void snow_params_default(snow_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof *p);
+  // src/snow/utils/defines.hpp:14-54
+  p->grid_pos[0] = 0.5125f;
+  p->grid_pos[1] = 0.5125f;
+  p->grid_pos[2] = 1.5125f;
+  p->grid_dim[0] = p->grid_dim[1] = p->grid_dim[2] = 201;
+  p->grid_spacing = 0.05f;
+  p->young = 6e6f;
+  p->poisson = 0.2f;
+  p->hardening = 30.0f;
+  p->crit_compression = 1.0e-2f;
+  p->crit_stretch = 1e-3f;
+  p->alpha = 0.95f;  // g2pTransfer.glsl:2, particleAdvance.glsl:2
+  p->gravity[0] = 0.0f;
+  p->gravity[1] = -9.81f;  // gForceCompute.glsl:39
+  p->gravity[2] = 0.0f;
+  p->mode = SNOW_MODE_FAST;
+  p->sort_interval = 0;
+}
+
+int snow_default_walls(const snow_params* p, snow_collider out[6]) {
+  // explicit.cpp:9-67: positions formed in double, stored as float; normals
+  // +x, +y, +z at offset 4 nodes, -x, -y, -z at dim - 4 nodes; friction 0.2.
+  const int off = 4;
+  for (int w = 0; w < 6; w++) {
+    snow_collider& c = out[w];
+    std::memset(&c, 0, sizeof c);
+    const bool hi = w >= 3;
+    for (int k = 0; k < 3; k++)
+      c.pos[k] = (float)((double)p->grid_pos[k] + (double)(hi ? p->grid_dim[k] - off : off) * (double)p->grid_spacing);
+    c.normal[w % 3] = hi ? -1.0f : 1.0f;
+    c.type = 0;
+    c.radius = 0.0f;
+    c.friction = 0.2f;
+  }
+  return 6;
+}
+
+snow_status snow_ctx_create(int device, size_t hbm_budget_bytes, snow_ctx** out) {
+  if (!out) return SNOW_EINVAL;
+  *out = nullptr;
+  snow_ctx* ctx = new snow_ctx();
+  ctx->device = device;
+  ctx->budget = hbm_budget_bytes;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_stats, sizeof(StatsAccum));
+  if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_stats, sizeof(StatsAccum));
+  if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_counters, kCounterStride * sizeof(int));
+  for (int i = 0; i < 8 && e == cudaSuccess; i++) e = cudaEventCreate(&ctx->ev[i]);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    snow_ctx_destroy(ctx);
+    return SNOW_ECUDA;
+  }
+  *out = ctx;
+  return SNOW_OK;
+}
+
+void snow_ctx_destroy(snow_ctx* ctx) {
+  if (!ctx) return;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  while (!ctx->batches.empty()) snow_batch_destroy(*ctx->batches.begin());
+  while (!ctx->scenes.empty()) snow_scene_destroy(*ctx->scenes.begin());
+  for (int i = 0; i < 8; i++)
+    if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+  if (ctx->d_stats) cudaFree(ctx->d_stats);
+  if (ctx->h_stats) cudaFreeHost(ctx->h_stats);
+  if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+const char* snow_last_error(const snow_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+size_t snow_ctx_bytes_in_use(const snow_ctx* ctx) { return ctx ? ctx->used : 0; }
+snow_status snow_ctx_set_profiling(snow_ctx* ctx, int on) {
+  if (!ctx) return SNOW_EINVAL;
+  ctx->profiling = on != 0;
+  return SNOW_OK;
+}
+void* snow_ctx_stream(const snow_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+snow_status snow_ctx_synchronize(snow_ctx* ctx) {
+  if (!ctx) return SNOW_EINVAL;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SNOW_OK;
+}
+
+size_t snow_scene_footprint(const snow_params* p, size_t n) {
+  if (!valid_params(p)) return 0;
+  const double G = (double)p->grid_dim[0] * p->grid_dim[1] * p->grid_dim[2];
+  if (p->mode == SNOW_MODE_REFERENCE) return (size_t)(n * (16.0 * 6 + 128.0) + G * 48.0);
+  const double nb = (double)((p->grid_dim[0] + 3) / 4) * ((p->grid_dim[1] + 3) / 4) * ((p->grid_dim[2] + 3) / 4);
+  // particle streams + binning scratch + block tables + an initial pool estimate
+  const double pool = std::min(nb, 2.0 * (double)n / 64.0 * 4.0 + 4096.0);
+  return (size_t)(n * (76.0 + 4.0 * 4 + 76.0 + 4.0 / 256 * 256 + 24) + nb * 20.0 + pool * (448 + 384 + 4) * 4.0);
+}
+
+snow_status snow_scene_create(snow_ctx* ctx, const snow_params* p, const snow_collider* colliders, int n_colliders,
+                              size_t capacity, snow_scene** out) {
+  if (!ctx || !out || !valid_params(p) || n_colliders < 0 || (n_colliders > 0 && !colliders))
+    return fail(ctx, SNOW_EINVAL, "snow_scene_create: invalid argument");
+  *out = nullptr;
+  CK(cudaSetDevice(ctx->device));
+  snow_scene* s = new snow_scene();
+  s->ctx = ctx;
+  s->p = *p;
+  s->mode = p->mode;
+  s->G = (long long)p->grid_dim[0] * p->grid_dim[1] * p->grid_dim[2];
+  s->coll_h.assign(colliders, colliders + n_colliders);
+  s->ncoll = n_colliders;
+  if (p->sort_interval > 0) s->tune.sort_interval = p->sort_interval;
+  snow_status st = SNOW_OK;
+  if (n_colliders > 0) st = salloc(s, (size_t)n_colliders, &s->coll_d);
+  if (!st && n_colliders > 0)
+    if (cudaMemcpy(s->coll_d, colliders, sizeof(snow_collider) * n_colliders, cudaMemcpyHostToDevice) != cudaSuccess)
+      st = cuda_fail(ctx, cudaGetLastError(), "collider upload");
+  if (!st && s->mode == SNOW_MODE_FAST) {
+    fill_sd_params(s);
+    s->sd.dt = 1e-3f;
+    s->key_bits = ceil_log2((unsigned long long)s->sd.nblocks * 64ull);
+    st = fast_alloc_grid(s);
+  }
+  if (!st && capacity > 0) st = ensure_capacity(s, capacity);
+  ctx->scenes.insert(s);
+  if (st) {
+    snow_scene_destroy(s);
+    return st;
+  }
+  *out = s;
+  return SNOW_OK;
+}
+
+void snow_scene_destroy(snow_scene* s) {
+  if (!s) return;
+  snow_ctx* ctx = s->ctx;
+  cudaStreamSynchronize(ctx->stream);
+  // a batch that holds this scene can no longer step
+  std::vector<snow_batch*> holders;
+  for (snow_batch* b : ctx->batches)
+    if (std::find(b->scenes.begin(), b->scenes.end(), s) != b->scenes.end()) holders.push_back(b);
+  for (snow_batch* b : holders) snow_batch_destroy(b);
+  drop_graphs(s);
+  dfree_all(ctx, s->allocs, s->bytes);
+  ctx->scenes.erase(s);
+  delete s;
+}
+
+size_t snow_scene_size(const snow_scene* s) { return s ? s->n : 0; }
+
+snow_status snow_scene_upload(snow_scene* s, const float* x, const float* v, const float* m, const float* FE,
+                              const float* FP, size_t n) {
+  if (!s || !x || !v || !m) return fail(s ? s->ctx : nullptr, SNOW_EINVAL, "snow_scene_upload: null array");
+  snow_ctx* ctx = s->ctx;
+  snow_status st = ensure_capacity(s, n);
+  if (st) return st;
+  s->n = n;
+  s->initialized = false;
+  s->volume_given = false;
+  if (s->mode == SNOW_MODE_REFERENCE) {
+    // ParticleSystem::initSSBO: pxm = (x, m), pv = (v * 1e8, 0), FE / FP mat4
+    std::vector<float4> pxm(n), pfe(4 * n), pfp(4 * n);
+    std::vector<int4> pv(n), zero(n);
+    for (size_t i = 0; i < n; i++) {
+      pxm[i] = make_float4(x[3 * i], x[3 * i + 1], x[3 * i + 2], m[i]);
+      pv[i] = make_int4((int)((double)v[3 * i] * 1e8), (int)((double)v[3 * i + 1] * 1e8),
+                        (int)((double)v[3 * i + 2] * 1e8), 0);
+      zero[i] = make_int4(0, 0, 0, 0);
+      for (int c = 0; c < 4; c++) {
+        float fe[4] = {0, 0, 0, 0}, fp[4] = {0, 0, 0, 0};
+        for (int r = 0; r < 3 && c < 3; r++) {
+          fe[r] = FE ? FE[9 * i + 3 * r + c] : (r == c ? 1.0f : 0.0f);
+          fp[r] = FP ? FP[9 * i + 3 * r + c] : (r == c ? 1.0f : 0.0f);
+        }
+        pfe[4 * i + c] = make_float4(fe[0], fe[1], fe[2], fe[3]);
+        pfp[4 * i + c] = make_float4(fp[0], fp[1], fp[2], fp[3]);
+      }
+    }
+    RefArgs& a = ref_args(s);
+    CK(cudaMemcpy(a.pxm, pxm.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(a.pv, pv.data(), n * sizeof(int4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(a.pfe, pfe.data(), 4 * n * sizeof(float4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(a.pfp, pfp.data(), 4 * n * sizeof(float4), cudaMemcpyHostToDevice));
+    for (int4* acc : {a.pvn, a.pd0, a.pd1, a.pd2}) CK(cudaMemcpy(acc, zero.data(), n * sizeof(int4), cudaMemcpyHostToDevice));
+    s->uploaded = true;
+    return SNOW_OK;
+  }
+  std::vector<float4> xm(n), vv(n), fa(n), fb(n);
+  std::vector<float2> fc(n);
+  static const float I[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  for (size_t i = 0; i < n; i++) {
+    xm[i] = make_float4(x[3 * i], x[3 * i + 1], x[3 * i + 2], m[i]);
+    vv[i] = make_float4(v[3 * i], v[3 * i + 1], v[3 * i + 2], 0.0f);
+    const float* F = FE ? FE + 9 * i : I;
+    fa[i] = make_float4(F[0], F[3], F[6], F[1]);
+    fb[i] = make_float4(F[4], F[7], F[2], F[5]);
+    fc[i] = make_float2(F[8], FP ? (float)det_rowmajor(FP + 9 * i) : 1.0f);
+  }
+  s->sd.n = (int)n;
+  st = fast_upload_soa(s, xm, vv, fa, fb, fc);
+  if (st) return st;
+  s->uploaded = true;
+  return SNOW_OK;
+}
+
+snow_status snow_scene_upload_std140(snow_scene* s, const float* pxm, const int32_t* pv, const float* pFE,
+                                     const float* pFP, size_t n) {
+  if (!s || !pxm || !pv || !pFE || !pFP) return fail(s ? s->ctx : nullptr, SNOW_EINVAL, "null buffer");
+  snow_ctx* ctx = s->ctx;
+  snow_status st = ensure_capacity(s, n);
+  if (st) return st;
+  s->n = n;
+  s->initialized = false;
+  s->volume_given = false;
+  if (s->mode == SNOW_MODE_REFERENCE) {
+    RefArgs& a = ref_args(s);
+    CK(cudaMemcpy(a.pxm, pxm, n * sizeof(float4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(a.pv, pv, n * sizeof(int4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(a.pfe, pFE, n * 16 * sizeof(float), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(a.pfp, pFP, n * 16 * sizeof(float), cudaMemcpyHostToDevice));
+    for (int4* acc : {a.pvn, a.pd0, a.pd1, a.pd2}) CK(cudaMemset(acc, 0, n * sizeof(int4)));
+    s->uploaded = true;
+    return SNOW_OK;
+  }
+  std::vector<float4> xm(n), vv(n), fa(n), fb(n);
+  std::vector<float2> fc(n);
+  for (size_t i = 0; i < n; i++) {
+    xm[i] = make_float4(pxm[4 * i], pxm[4 * i + 1], pxm[4 * i + 2], pxm[4 * i + 3]);
+    vv[i] = make_float4((float)pv[4 * i] * 1e-8f, (float)pv[4 * i + 1] * 1e-8f, (float)pv[4 * i + 2] * 1e-8f, 0.0f);
+    const float* F = pFE + 16 * i;  // column-major mat4: m[c][r] at 4c + r
+    float Fp[9];
+    for (int r = 0; r < 3; r++)
+      for (int c = 0; c < 3; c++) Fp[3 * r + c] = pFP[16 * i + 4 * c + r];
+    fa[i] = make_float4(F[0], F[1], F[2], F[4]);
+    fb[i] = make_float4(F[5], F[6], F[8], F[9]);
+    fc[i] = make_float2(F[10], (float)det_rowmajor(Fp));
+  }
+  s->sd.n = (int)n;
+  st = fast_upload_soa(s, xm, vv, fa, fb, fc);
+  if (st) return st;
+  s->uploaded = true;
+  return SNOW_OK;
+}
+
+snow_status snow_scene_set_volume(snow_scene* s, const float* volume, size_t n) {
+  if (!s || !volume) return SNOW_EINVAL;
+  snow_ctx* ctx = s->ctx;
+  if (!s->uploaded || n != s->n) return fail(ctx, SNOW_ESTATE, "snow_scene_set_volume needs an upload of n particles");
+  if (s->mode == SNOW_MODE_REFERENCE) {
+    // density rho0 = m / V0, stored as int(rho0 * 1e6) in pv.w
+    std::vector<float4> pxm(n);
+    std::vector<int4> pv(n);
+    RefArgs& a = ref_args(s);
+    CK(cudaMemcpy(pxm.data(), a.pxm, n * sizeof(float4), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(pv.data(), a.pv, n * sizeof(int4), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; i++) pv[i].w = volume[i] > 0.0f ? (int)(pxm[i].w / volume[i] * 1e6f) : 0;
+    CK(cudaMemcpy(a.pv, pv.data(), n * sizeof(int4), cudaMemcpyHostToDevice));
+  } else {
+    std::vector<float4> vv(n);
+    std::vector<uint32_t> pid(n);
+    CK(cudaMemcpy(vv.data(), s->sd.vv, n * sizeof(float4), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(pid.data(), s->sd.pid, n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; i++) vv[i].w = volume[pid[i]];
+    CK(cudaMemcpy(s->sd.vv, vv.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+  }
+  s->volume_given = true;
+  return SNOW_OK;
+}
+
+snow_status snow_scene_init(snow_scene* s) {
+  if (!s) return SNOW_EINVAL;
+  snow_ctx* ctx = s->ctx;
+  if (!s->uploaded) return fail(ctx, SNOW_ESTATE, "snow_scene_init before upload");
+  if (s->mode == SNOW_MODE_REFERENCE) {
+    RefArgs& a = ref_args(s);
+    ref_reset(a, ctx->stream);
+    ref_p2g(a, true, ctx->stream);
+    if (!s->volume_given) ref_volume(a, ctx->stream);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ctx->stream));
+  } else {
+    snow_status st = fast_init(s);
+    if (st) return st;
+  }
+  s->initialized = true;
+  return SNOW_OK;
+}
+
+snow_status snow_dispatch(snow_scene* s, int kernel, double dt) {
+  if (!s) return SNOW_EINVAL;
+  snow_ctx* ctx = s->ctx;
+  if (!s->uploaded) return fail(ctx, SNOW_ESTATE, "dispatch before upload");
+  const float fdt = (float)dt;  // glUniform1f of the double dt
+  cudaStream_t st = ctx->stream;
+  if (s->mode == SNOW_MODE_REFERENCE) {
+    RefArgs& a = ref_args(s);
+    switch (kernel) {
+      case SNOW_K_RIGID_ADVANCE: ref_rigid(s->coll_d, s->ncoll, fdt, st); break;
+      case SNOW_K_G_RESET: ref_reset(a, st); break;
+      case SNOW_K_P2G: ref_p2g(a, false, st); break;
+      case SNOW_K_G_FORCE: ref_grid(a, fdt, st); break;
+      case SNOW_K_G2P: ref_g2p(a, st); break;
+      case SNOW_K_P_ADVANCE: ref_advance(a, fdt, st); break;
+      case SNOW_K_G_MASS: ref_p2g(a, true, st); break;
+      case SNOW_K_P_VOLUME: ref_volume(a, st); break;
+      default: return fail(ctx, SNOW_EINVAL, "unknown kernel");
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
+    return SNOW_OK;
+  }
+  if (!s->initialized && kernel != SNOW_K_G_MASS && kernel != SNOW_K_P_VOLUME && kernel != SNOW_K_RIGID_ADVANCE)
+    return fail(ctx, SNOW_ESTATE, "dispatch before init");
+  snow_status r = set_dt(s, fdt);
+  if (r) return r;
+  switch (kernel) {
+    case SNOW_K_RIGID_ADVANCE:
+      if (s->ncoll > 0) fast_rigid(s->sd_dev, 1, nullptr, st);
+      break;
+    case SNOW_K_G_RESET: break;
+    case SNOW_K_P2G: {
+      const bool bin = s->steps_since_sort >= s->tune.sort_interval;
+      fast_enqueue_p2g(s, bin, false, st);
+      if (bin) s->steps_since_sort = 0;
+      break;
+    }
+    case SNOW_K_G_FORCE: fast_enqueue_grid(s, st); break;
+    case SNOW_K_G2P:
+      fast_enqueue_g2p(s, st);
+      s->steps_since_sort++;
+      break;
+    case SNOW_K_P_ADVANCE: break;
+    case SNOW_K_G_MASS:
+    case SNOW_K_P_VOLUME: return snow_scene_init(s);
+    default: return fail(ctx, SNOW_EINVAL, "unknown kernel");
+  }
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(st));
+  return SNOW_OK;
+}
+
+snow_status snow_scene_step(snow_scene* s, double dt, int n_steps) {
+  if (!s || n_steps < 0) return SNOW_EINVAL;
+  snow_ctx* ctx = s->ctx;
+  if (!s->initialized) return fail(ctx, SNOW_ESTATE, "snow_scene_step before snow_scene_init");
+  const float fdt = (float)dt;
+  cudaStream_t st = ctx->stream;
+  s->last_dt = fdt;
+  if (s->mode == SNOW_MODE_REFERENCE) {
+    RefArgs& a = ref_args(s);
+    for (int i = 0; i < n_steps; i++) {
+      ref_rigid(s->coll_d, s->ncoll, fdt, st);
+      ref_reset(a, st);
+      ref_p2g(a, false, st);
+      ref_grid(a, fdt, st);
+      ref_g2p(a, st);
+      ref_advance(a, fdt, st);
+    }
+    CK(cudaGetLastError());
+    return SNOW_OK;
+  }
+  snow_status r = set_dt(s, fdt);
+  if (r) return r;
+  for (int i = 0; i < n_steps; i++) {
+    const bool bin = s->steps_since_sort >= s->tune.sort_interval;
+    if (bin) {
+      // binning points are where the host looks at the device counters
+      if (s->steps_since_sort < (1 << 30)) {
+        r = fast_check(s);
+        if (r) return r;
+      }
+    }
+    if (ctx->profiling) {
+      cudaEvent_t* ev = ctx->ev;
+      CK(cudaEventRecord(ev[0], st));
+      if (s->ncoll > 0) fast_rigid(s->sd_dev, 1, nullptr, st);
+      if (bin) fast_bin(s, st);
+      CK(cudaEventRecord(ev[1], st));
+      fast_enqueue_p2g(s, false, false, st);
+      CK(cudaEventRecord(ev[2], st));
+      fast_enqueue_grid(s, st);
+      CK(cudaEventRecord(ev[3], st));
+      fast_enqueue_g2p(s, st);
+      CK(cudaEventRecord(ev[4], st));
+      CK(cudaEventSynchronize(ev[4]));
+      float t[4];
+      for (int k = 0; k < 4; k++) cudaEventElapsedTime(&t[k], ev[k], ev[k + 1]);
+      s->times.sort_ms += t[0];
+      s->times.p2g_ms += t[1];
+      s->times.grid_ms += t[2];
+      s->times.g2p_ms += t[3];
+      s->times.total_ms += t[0] + t[1] + t[2] + t[3];
+      s->times.steps++;
+    } else {
+      cudaGraphExec_t& g = bin ? s->g_sort : s->g_plain;
+      if (!g || s->g_dt != fdt) {
+        if (s->g_dt != fdt) drop_graphs(s);
+        cudaGraph_t graph;
+        CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        fast_enqueue_step(s, bin, st);
+        CK(cudaStreamEndCapture(st, &graph));
+        CK(cudaGraphInstantiate(&g, graph, 0));
+        cudaGraphDestroy(graph);
+        s->g_dt = fdt;
+      }
+      CK(cudaGraphLaunch(g, st));
+    }
+    if (bin) s->steps_since_sort = 0;
+    s->steps_since_sort++;
+  }
+  CK(cudaGetLastError());
+  return SNOW_OK;
+}
+
+snow_status snow_scene_download(snow_scene* s, float* x, float* v, float* FE, float* FP, float* Jp, float* volume) {
+  if (!s) return SNOW_EINVAL;
+  snow_ctx* ctx = s->ctx;
+  const size_t n = s->n;
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (s->mode == SNOW_MODE_REFERENCE) {
+    std::vector<float4> pxm(n), pfe(4 * n), pfp(4 * n);
+    std::vector<int4> pv(n);
+    RefArgs& a = ref_args(s);
+    CK(cudaMemcpy(pxm.data(), a.pxm, n * sizeof(float4), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(pv.data(), a.pv, n * sizeof(int4), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(pfe.data(), a.pfe, 4 * n * sizeof(float4), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(pfp.data(), a.pfp, 4 * n * sizeof(float4), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; i++) {
+      const float* fe = &pfe[4 * i].x;
+      const float* fp = &pfp[4 * i].x;
+      float fpr[9];
+      for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) {
+          if (FE) FE[9 * i + 3 * r + c] = fe[4 * c + r];
+          fpr[3 * r + c] = fp[4 * c + r];
+          if (FP) FP[9 * i + 3 * r + c] = fpr[3 * r + c];
+        }
+      if (x) {
+        x[3 * i] = pxm[i].x;
+        x[3 * i + 1] = pxm[i].y;
+        x[3 * i + 2] = pxm[i].z;
+      }
+      if (v) {
+        v[3 * i] = (float)pv[i].x * 1e-8f;
+        v[3 * i + 1] = (float)pv[i].y * 1e-8f;
+        v[3 * i + 2] = (float)pv[i].z * 1e-8f;
+      }
+      if (Jp) Jp[i] = (float)det_rowmajor(fpr);
+      if (volume) {
+        const float rho = (float)pv[i].w * 1e-6f;
+        volume[i] = rho > 0.0f ? pxm[i].w / rho : 0.0f;
+      }
+    }
+    return SNOW_OK;
+  }
+  if (FP) return fail(ctx, SNOW_EUNSUPPORTED, "F_P is not kept in SNOW_MODE_FAST (J_p is)");
+  std::vector<float4> xm(n), vv(n), fa(n), fb(n);
+  std::vector<float2> fc(n);
+  std::vector<uint32_t> pid(n);
+  CK(cudaMemcpy(xm.data(), s->sd.xm, n * sizeof(float4), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(vv.data(), s->sd.vv, n * sizeof(float4), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(fa.data(), s->sd.fa, n * sizeof(float4), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(fb.data(), s->sd.fb, n * sizeof(float4), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(fc.data(), s->sd.fc, n * sizeof(float2), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(pid.data(), s->sd.pid, n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  for (size_t i = 0; i < n; i++) {
+    const size_t j = pid[i];
+    if (j >= n) return fail(ctx, SNOW_ECUDA, "corrupt particle index stream");
+    if (x) {
+      x[3 * j] = xm[i].x;
+      x[3 * j + 1] = xm[i].y;
+      x[3 * j + 2] = xm[i].z;
+    }
+    if (v) {
+      v[3 * j] = vv[i].x;
+      v[3 * j + 1] = vv[i].y;
+      v[3 * j + 2] = vv[i].z;
+    }
+    if (FE) {
+      // fa = (m00, m01, m02, m10), fb = (m11, m12, m20, m21), fc = (m22, Jp); m[c][r]
+      const float mcr[9] = {fa[i].x, fa[i].y, fa[i].z, fa[i].w, fb[i].x, fb[i].y, fb[i].z, fb[i].w, fc[i].x};
+      for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) FE[9 * j + 3 * r + c] = mcr[3 * c + r];
+    }
+    if (Jp) Jp[j] = fc[i].y;
+    if (volume) volume[j] = vv[i].w;
+  }
+  return SNOW_OK;
+}
+
+snow_status snow_scene_download_std140(snow_scene* s, float* pxm, int32_t* pv, float* pFE, float* pFP) {
+  if (!s) return SNOW_EINVAL;
+  snow_ctx* ctx = s->ctx;
+  if (s->mode != SNOW_MODE_REFERENCE) return fail(ctx, SNOW_EUNSUPPORTED, "std140 download needs SNOW_MODE_REFERENCE");
+  const size_t n = s->n;
+  CK(cudaStreamSynchronize(ctx->stream));
+  RefArgs& a = ref_args(s);
+  if (pxm) CK(cudaMemcpy(pxm, a.pxm, n * sizeof(float4), cudaMemcpyDeviceToHost));
+  if (pv) CK(cudaMemcpy(pv, a.pv, n * sizeof(int4), cudaMemcpyDeviceToHost));
+  if (pFE) CK(cudaMemcpy(pFE, a.pfe, n * 16 * sizeof(float), cudaMemcpyDeviceToHost));
+  if (pFP) CK(cudaMemcpy(pFP, a.pfp, n * 16 * sizeof(float), cudaMemcpyDeviceToHost));
+  return SNOW_OK;
+}
+
+snow_status snow_scene_download_grid(snow_scene* s, float* mass, float* momentum, float* force, float* vstar) {
+  if (!s) return SNOW_EINVAL;
+  snow_ctx* ctx = s->ctx;
+  CK(cudaStreamSynchronize(ctx->stream));
+  const size_t G = (size_t)s->G;
+  if (s->mode == SNOW_MODE_REFERENCE) {
+    std::vector<int4> gv(G), gf(G);
+    std::vector<float4> gvn(G);
+    RefArgs& a = ref_args(s);
+    CK(cudaMemcpy(gv.data(), a.gv, G * sizeof(int4), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(gf.data(), a.gf, G * sizeof(int4), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(gvn.data(), a.gvn, G * sizeof(float4), cudaMemcpyDeviceToHost));
+    for (size_t g = 0; g < G; g++) {
+      if (mass) mass[g] = (float)gv[g].w * 1e-8f;
+      const float pm[3] = {(float)gv[g].x * 1e-8f, (float)gv[g].y * 1e-8f, (float)gv[g].z * 1e-8f};
+      const float fo[3] = {(float)gf[g].x * 1e-6f, (float)gf[g].y * 1e-6f, (float)gf[g].z * 1e-6f};
+      const float vs[3] = {gvn[g].x, gvn[g].y, gvn[g].z};
+      for (int k = 0; k < 3; k++) {
+        if (momentum) momentum[3 * g + k] = pm[k];
+        if (force) force[3 * g + k] = fo[k];
+        if (vstar) vstar[3 * g + k] = vs[k];
+      }
+    }
+    return SNOW_OK;
+  }
+  float *dm = nullptr, *dp = nullptr, *df = nullptr, *dv = nullptr;
+  std::vector<std::pair<void*, size_t>> tmp;
+  size_t tb = 0;
+  snow_status r;
+  if ((r = dalloc(ctx, tmp, tb, G * sizeof(float), (void**)&dm)) || (r = dalloc(ctx, tmp, tb, 3 * G * sizeof(float), (void**)&dp)) ||
+      (r = dalloc(ctx, tmp, tb, 3 * G * sizeof(float), (void**)&df)) || (r = dalloc(ctx, tmp, tb, 3 * G * sizeof(float), (void**)&dv))) {
+    dfree_all(ctx, tmp, tb);
+    return r;
+  }
+  cudaMemsetAsync(dm, 0, G * sizeof(float), ctx->stream);
+  cudaMemsetAsync(dp, 0, 3 * G * sizeof(float), ctx->stream);
+  cudaMemsetAsync(df, 0, 3 * G * sizeof(float), ctx->stream);
+  cudaMemsetAsync(dv, 0, 3 * G * sizeof(float), ctx->stream);
+  fast_download_grid(s->sd_dev, (long long)G, dm, dp, df, dv, ctx->stream);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e == cudaSuccess && mass) e = cudaMemcpy(mass, dm, G * sizeof(float), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && momentum) e = cudaMemcpy(momentum, dp, 3 * G * sizeof(float), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && force) e = cudaMemcpy(force, df, 3 * G * sizeof(float), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && vstar) e = cudaMemcpy(vstar, dv, 3 * G * sizeof(float), cudaMemcpyDeviceToHost);
+  dfree_all(ctx, tmp, tb);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "grid download");
+  return SNOW_OK;
+}
+
+snow_status snow_scene_download_colliders(snow_scene* s, snow_collider* out) {
+  if (!s || !out) return SNOW_EINVAL;
+  snow_ctx* ctx = s->ctx;
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (s->ncoll > 0) CK(cudaMemcpy(out, s->coll_d, s->ncoll * sizeof(snow_collider), cudaMemcpyDeviceToHost));
+  return SNOW_OK;
+}
+
+snow_status snow_scene_stats(snow_scene* s, snow_stats* out) {
+  if (!s || !out) return SNOW_EINVAL;
+  snow_ctx* ctx = s->ctx;
+  StatsAccum init{};
+  for (int k = 0; k < 3; k++) {
+    init.bmin_key[k] = 0x7fffffff;
+    init.bmax_key[k] = (int)0x80000000;
+  }
+  CK(cudaMemcpyAsync(ctx->d_stats, &init, sizeof init, cudaMemcpyHostToDevice, ctx->stream));
+  if (s->mode == SNOW_MODE_REFERENCE)
+    ref_stats(ref_args(s), ctx->d_stats, ctx->stream);
+  else
+    fast_stats(s->sd_dev, (int)s->n, ctx->d_stats, ctx->stream);
+  CK(cudaMemcpyAsync(ctx->h_stats, ctx->d_stats, sizeof(StatsAccum), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  const StatsAccum& a = *ctx->h_stats;
+  std::memset(out, 0, sizeof *out);
+  out->mass = a.mass;
+  for (int k = 0; k < 3; k++) {
+    out->momentum[k] = a.mom[k];
+    out->center_of_mass[k] = a.mass > 0 ? a.com[k] / a.mass : 0.0;
+    const int kmin = a.bmin_key[k] >= 0 ? a.bmin_key[k] : a.bmin_key[k] ^ 0x7fffffff;
+    const int kmax = a.bmax_key[k] >= 0 ? a.bmax_key[k] : a.bmax_key[k] ^ 0x7fffffff;
+    float fmin, fmax;
+    std::memcpy(&fmin, &kmin, 4);
+    std::memcpy(&fmax, &kmax, 4);
+    out->bbox_min[k] = fmin;
+    out->bbox_max[k] = fmax;
+  }
+  out->kinetic_energy = a.ke;
+  out->nonfinite = a.nonfinite;
+  out->n = s->n;
+  out->mean_jp = s->n > a.nonfinite ? a.jp / (double)(s->n - a.nonfinite) : 0.0;
+  return SNOW_OK;
+}
+
+snow_status snow_scene_cell_keys(snow_scene* s, uint32_t* keys, uint32_t* perm) {
+  if (!s || !keys) return SNOW_EINVAL;
+  snow_ctx* ctx = s->ctx;
+  if (s->mode != SNOW_MODE_FAST) return fail(ctx, SNOW_EUNSUPPORTED, "binning runs in SNOW_MODE_FAST");
+  const size_t n = s->n;
+  cudaStream_t st = ctx->stream;
+  // keys of the current positions, then placed at each particle's upload
+  // index so the stable sort sees the caller's order
+  fast_sort_keys(s->sd, s->sd_dev, s->bin, 0, st);  // keys only (0 bits: no passes)
+  std::vector<uint32_t> k(n), pid(n);
+  CK(cudaMemcpyAsync(k.data(), s->bin.keys[0], n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(pid.data(), s->sd.pid, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  std::vector<uint32_t> ko(n), vo(n);
+  for (size_t i = 0; i < n; i++) {
+    ko[pid[i]] = k[i];
+    vo[i] = (uint32_t)i;
+  }
+  std::memcpy(keys, ko.data(), n * sizeof(uint32_t));
+  if (perm) {
+    CK(cudaMemcpyAsync(s->bin.keys[0], ko.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(s->bin.vals[0], vo.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    radix_sort_pairs(s->bin.keys, s->bin.vals, n, s->key_bits, s->bin.hist, s->bin.scan_tmp, st);
+    CK(cudaMemcpyAsync(perm, s->bin.vals[0], n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+  }
+  CK(cudaGetLastError());
+  return SNOW_OK;
+}
+
+snow_status snow_scene_phase_times(snow_scene* s, snow_phase_times* out, int reset) {
+  if (!s || !out) return SNOW_EINVAL;
+  *out = s->times;
+  if (reset) s->times = snow_phase_times{};
+  return SNOW_OK;
+}
+
+// ---- batches ----------------------------------------------------------------
+snow_status snow_batch_create(snow_ctx* ctx, snow_scene* const* scenes, int n, snow_batch** out) {
+  if (!ctx || !scenes || n <= 0 || !out) return fail(ctx, SNOW_EINVAL, "snow_batch_create: invalid argument");
+  *out = nullptr;
+  for (int i = 0; i < n; i++)
+    if (!scenes[i] || scenes[i]->mode != SNOW_MODE_FAST || !scenes[i]->initialized || scenes[i]->ctx != ctx)
+      return fail(ctx, SNOW_EINVAL, "batch scenes must be initialised SNOW_MODE_FAST scenes of this context");
+  snow_batch* b = new snow_batch();
+  b->ctx = ctx;
+  b->scenes.assign(scenes, scenes + n);
+  snow_status st;
+  if ((st = dalloc(ctx, b->allocs, b->bytes, sizeof(SceneDev) * n, (void**)&b->d_scenes)) ||
+      (st = dalloc(ctx, b->allocs, b->bytes, sizeof(int) * 4 * (n + 1), (void**)&b->d_prefix))) {
+    snow_batch_destroy(b);
+    return st;
+  }
+  ctx->batches.insert(b);
+  *out = b;
+  return SNOW_OK;
+}
+
+void snow_batch_destroy(snow_batch* b) {
+  if (!b) return;
+  cudaStreamSynchronize(b->ctx->stream);
+  for (auto& g : b->graphs) cudaGraphExecDestroy(g.second);
+  dfree_all(b->ctx, b->allocs, b->bytes);
+  b->ctx->batches.erase(b);
+  delete b;
+}
+
+namespace {
+
+snow_status batch_refresh(snow_batch* b, const double* dt) {
+  snow_ctx* ctx = b->ctx;
+  const int n = (int)b->scenes.size();
+  bool changed = (int)b->versions.size() != n;
+  std::vector<float> want(n);
+  for (int i = 0; i < n; i++) {
+    snow_scene* s = b->scenes[i];
+    want[i] = dt ? (float)dt[i] : s->last_dt;
+    if (!changed && b->versions[i] != s->version) changed = true;
+  }
+  if (want != b->g_dt) changed = true;
+  if (!changed) return SNOW_OK;
+  std::vector<SceneDev> sds(n);
+  std::vector<int> pre(4 * (n + 1), 0);
+  long long chunks = 0, blocks = 0;
+  for (int i = 0; i < n; i++) {
+    snow_scene* s = b->scenes[i];
+    s->sd.dt = want[i];
+    s->last_dt = want[i];
+    sds[i] = s->sd;
+    const int chunk = s->tune.g2p_threads;
+    pre[2 * (n + 1) + i] = (int)chunks;
+    pre[3 * (n + 1) + i] = (int)blocks;
+    chunks += (long long)((s->n + chunk - 1) / chunk);
+    blocks += s->sd.nblocks;
+  }
+  pre[2 * (n + 1) + n] = (int)chunks;
+  pre[3 * (n + 1) + n] = (int)blocks;
+  b->total_chunks = chunks;
+  b->total_blocks = blocks;
+  CK(cudaMemcpyAsync(b->d_scenes, sds.data(), sizeof(SceneDev) * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(b->d_prefix, pre.data(), sizeof(int) * pre.size(), cudaMemcpyHostToDevice, ctx->stream));
+  for (int i = 0; i < n; i++) {
+    snow_scene* s = b->scenes[i];
+    CK(cudaMemcpyAsync(s->sd_dev, &s->sd, sizeof(SceneDev), cudaMemcpyHostToDevice, ctx->stream));
+    drop_graphs(s);
+    s->version++;
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  b->versions.resize(n);
+  for (int i = 0; i < n; i++) b->versions[i] = b->scenes[i]->version;
+  b->g_dt = want;
+  for (auto& g : b->graphs) cudaGraphExecDestroy(g.second);
+  b->graphs.clear();
+  return SNOW_OK;
+}
+
+void batch_enqueue_step(snow_batch* b, int phase, int interval, cudaStream_t st) {
+  const int n = (int)b->scenes.size();
+  int* pre = b->d_prefix;
+  int* items = pre;
+  int* active = pre + (n + 1);
+  int* chunks = pre + 2 * (n + 1);
+  int* blocks = pre + 3 * (n + 1);
+  fast_rigid(b->d_scenes, n, nullptr, st);
+  // re-bin a staggered subset of scenes each step
+  for (int i = 0; i < n; i++)
+    if ((i % interval) == phase) fast_bin(b->scenes[i], st);
+  fast_begin_step(b->d_scenes, n, st);
+  fast_compact(b->d_scenes, blocks, n, b->total_blocks, st);
+  fast_prefix(b->d_scenes, n, CNT_ITEMS, items, st);
+  fast_prefix(b->d_scenes, n, CNT_ACTIVE, active, st);
+  const int threads = b->scenes[0]->tune.p2g_threads;
+  fast_p2g(b->d_scenes, items, n, num_sms() * (threads >= 256 ? 4 : 8), false, threads, st);
+  fast_grid(b->d_scenes, active, n, num_sms() * 8, false, st);
+  fast_g2p_advance(b->d_scenes, chunks, n, b->total_chunks, b->scenes[0]->tune.g2p_threads, st);
+}
+
+}  // namespace
+
+snow_status snow_batch_step(snow_batch* b, const double* dt, int n_steps) {
+  if (!b || n_steps < 0) return SNOW_EINVAL;
+  snow_ctx* ctx = b->ctx;
+  snow_status r = batch_refresh(b, dt);
+  if (r) return r;
+  const int interval = std::max(1, b->scenes[0]->tune.sort_interval);
+  cudaStream_t st = ctx->stream;
+  for (int i = 0; i < n_steps; i++) {
+    const int phase = b->step_count % interval;
+    if (phase == 0 && b->step_count > 0) {
+      for (snow_scene* s : b->scenes) {
+        r = fast_check(s);
+        if (r) return r;
+      }
+      r = batch_refresh(b, dt);
+      if (r) return r;
+    }
+    auto it = b->graphs.find(phase);
+    if (it == b->graphs.end()) {
+      cudaGraph_t graph;
+      cudaGraphExec_t exec;
+      CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      batch_enqueue_step(b, phase, interval, st);
+      CK(cudaStreamEndCapture(st, &graph));
+      CK(cudaGraphInstantiate(&exec, graph, 0));
+      cudaGraphDestroy(graph);
+      it = b->graphs.emplace(phase, exec).first;
+    }
+    CK(cudaGraphLaunch(it->second, st));
+    b->step_count++;
+  }
+  for (snow_scene* s : b->scenes) s->steps_since_sort = 1;  // single-scene stepping re-bins on its own schedule
+  CK(cudaGetLastError());
+  return SNOW_OK;
+}
+
+snow_status snow_batch_autotune(snow_batch* b, const double* dt, int* choice_out) {
+  if (!b) return SNOW_EINVAL;
+  (void)dt;
+  if (choice_out) *choice_out = b->scenes[0]->tune.sort_interval;
+  return SNOW_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,168 @@
+// Internal interfaces between the host runtime (snow_api.cpp) and the CUDA
+// kernel files (ref_kernels.cu, fast_kernels.cu, sort.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/snow_mpm.h"
+
+namespace snow {
+
+// ---------------------------------------------------------------------------
+// Reference mode: the shaders' buffers, byte for byte (std140).
+// ---------------------------------------------------------------------------
+struct RefArgs {
+  float gpos[3];
+  int dim[3];
+  float h;
+  float young, poisson, hardening, crit_c, crit_s, alpha;
+  float grav[3];
+  int ncoll;
+  snow_collider* coll;
+  int n;
+  float4* pxm;   // (x, m)
+  int4* pv;      // (v * 1e8, rho0 * 1e6)
+  float4* pfe;   // mat4 per particle, 4 columns
+  float4* pfp;
+  int4* pvn;     // G2P accumulators (g2pTransfer.glsl bindings 6, 13-15)
+  int4* pd0;
+  int4* pd1;
+  int4* pd2;
+  long long G;
+  int4* gv;      // (p * 1e8, m * 1e8)
+  int4* gf;      // (f * 1e6, 0)
+  float4* gvn;   // (v*, 0)
+};
+
+void ref_rigid(snow_collider* coll, int ncoll, float dt, cudaStream_t st);
+void ref_reset(const RefArgs& a, cudaStream_t st);
+void ref_p2g(const RefArgs& a, bool mass_only, cudaStream_t st);
+void ref_volume(const RefArgs& a, cudaStream_t st);
+void ref_grid(const RefArgs& a, float dt, cudaStream_t st);
+void ref_g2p(const RefArgs& a, cudaStream_t st);
+void ref_advance(const RefArgs& a, float dt, cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// Fast mode.
+// ---------------------------------------------------------------------------
+constexpr int kBlockNodes = 64;            // 4 x 4 x 4 nodes per grid block
+constexpr int kAccFields = 7;              // m, p (3), f (3)
+constexpr int kOutFields = 6;              // v* (3), d = v* - alpha p/m (3)
+constexpr int kAccBlockFloats = kAccFields * kBlockNodes;  // 448
+constexpr int kOutBlockFloats = kOutFields * kBlockNodes;  // 384
+
+// Per-scene counters (int32), one row of kCounterStride per scene.
+enum {
+  CNT_ACTIVE = 0,     // active grid blocks this step
+  CNT_OVERFLOW = 1,   // blocks that found no slot in the pool
+  CNT_ITEMS = 2,      // P2G work items since the last binning
+  CNT_NONFINITE = 3,  // particles with a non-finite field (cumulative)
+  CNT_HOME = 4,       // occupied home blocks at the last binning
+  CNT_FALLBACK = 5,   // particles that left their P2G tile (diagnostic, cumulative)
+  kCounterStride = 8
+};
+
+// Device-resident description of one FAST scene (read by every kernel).
+struct SceneDev {
+  float gpos[3];
+  float h;
+  int dim[3];
+  int bdim[3];
+  int nblocks;
+  float young, poisson, hardening, crit_lo, crit_hi, alpha;
+  float grav[3];
+  float dt;
+  int ncoll;
+  snow_collider* coll;
+  int n;
+  // particle streams (SoA): xm = (x, m), vv = (v, V0),
+  // fa = (FE00, FE10, FE20, FE01), fb = (FE11, FE21, FE02, FE12),
+  // fc = (FE22, Jp); FE stored column-major (m[c][r]).
+  float4* xm;
+  float4* vv;
+  float4* fa;
+  float4* fb;
+  float2* fc;
+  uint32_t* pid;    // upload index of the particle now stored at each slot
+  // sparse grid
+  int* blk_slot;    // nblocks: slot in the pool this step, -1 if inactive
+  int* blk_flag;    // nblocks: marked for the next step
+  int* active;      // pool_cap: block id of each slot
+  float* acc;       // pool_cap x 448: P2G accumulators, field-major per block
+  float* gout;      // pool_cap x 384: grid-update output
+  int pool_cap;
+  // P2G work items: (home block, first particle, count, 0)
+  int4* items;
+  int item_cap;
+  int* counters;    // kCounterStride ints
+};
+
+struct FastTuning {
+  int p2g_items_max = 256;     // particles per P2G work item
+  int p2g_threads = 256;
+  int g2p_threads = 128;
+  int sort_interval = 8;
+};
+
+// Work spaces over a batch: prefix[s] .. prefix[s+1] are scene s's units.
+// For counts only known on the device (items, active blocks) the prefix is
+// computed on the device by fast_prefix().
+void fast_prefix(const SceneDev* scenes, int nscenes, int counter, int* prefix, cudaStream_t st);
+void fast_compact(const SceneDev* scenes, const int* block_prefix, int nscenes, long long total_blocks,
+                  cudaStream_t st);
+void fast_mark(const SceneDev* scenes, const int* chunk_prefix, int nscenes, long long total_chunks,
+               cudaStream_t st);
+void fast_p2g(const SceneDev* scenes, const int* item_prefix, int nscenes, int grid_ctas, bool mass_only,
+              int threads, cudaStream_t st);
+void fast_grid(const SceneDev* scenes, const int* active_prefix, int nscenes, int grid_ctas, bool clear_only,
+               cudaStream_t st);
+void fast_volume(const SceneDev* scenes, const int* chunk_prefix, int nscenes, long long total_chunks,
+                 cudaStream_t st);
+void fast_g2p_advance(const SceneDev* scenes, const int* chunk_prefix, int nscenes, long long total_chunks,
+                      int threads, cudaStream_t st);
+void fast_rigid(const SceneDev* scenes, int nscenes, const snow_collider* dummy, cudaStream_t st);
+// Zeroes the per-step counters (active blocks, overflow) of every scene.
+void fast_begin_step(const SceneDev* scenes, int nscenes, cudaStream_t st);
+// Counts flagged blocks of one scene into counters[CNT_ACTIVE] (pool sizing).
+void fast_count_flags(const SceneDev* sd_dev, int nblocks, cudaStream_t st);
+
+// Binning of one scene (host-side sizes known): keys -> radix sort ->
+// permutation of the particle streams -> P2G work items.
+struct BinScratch {
+  uint32_t* keys[2];
+  uint32_t* vals[2];
+  uint32_t* hist;      // 256 x tiles
+  uint32_t* scan_tmp;  // partial sums of the scan
+  int* bstart;         // nblocks
+  int* bend;           // nblocks
+  int* home;           // nblocks
+  float4* tmp4[4];     // permutation targets for xm, vv, fa, fb
+  float2* tmp2;        // ... and fc
+  uint32_t* tmp_pid;   // ... and pid
+  size_t n_cap;
+};
+size_t radix_tiles(size_t n);
+// Sorts (key, index) pairs for the first n particles of scene `sd` (a host
+// copy of the device descriptor) and leaves the sorted keys in keys[0] and
+// the permutation in vals[0].
+void fast_sort_keys(const SceneDev& sd, const SceneDev* sd_dev, BinScratch& b, int key_bits, cudaStream_t st);
+void fast_apply_bins(const SceneDev& sd, const SceneDev* sd_dev, BinScratch& b, int items_max, cudaStream_t st);
+
+// Radix sort of arbitrary (key, value) pairs; the result lands in k[0]/v[0].
+void radix_sort_pairs(uint32_t* k[2], uint32_t* v[2], size_t n, int key_bits, uint32_t* hist, uint32_t* scan_tmp,
+                      cudaStream_t st);
+
+// Bulk statistics of one scene.
+struct StatsAccum {
+  double mass, mom[3], ke, com[3], jp;
+  int bmin_key[3], bmax_key[3];  // order-preserving int keys of the bbox floats
+  unsigned long long nonfinite;
+};
+void fast_stats(const SceneDev* sd_dev, int n, StatsAccum* out_dev, cudaStream_t st);
+void ref_stats(const RefArgs& a, StatsAccum* out_dev, cudaStream_t st);
+void fast_download_grid(const SceneDev* sd_dev, long long G, float* mass, float* mom, float* force, float* vstar,
+                        cudaStream_t st);
+
+int num_sms();
+
+}  // namespace snow

@@ -1,0 +1,119 @@
+"""ctypes bindings of include/snow_mpm.h (the library's C ABI).
+
+Loading fails loudly when the CUDA library is missing: there is no CPU
+fallback in the product."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libsnow_gb300.so")
+
+SNOW_OK = 0
+STATUS_NAMES = {0: "SNOW_OK", -1: "SNOW_EINVAL", -2: "SNOW_ENOMEM", -3: "SNOW_EBUDGET", -4: "SNOW_ETIMEDOUT",
+                -5: "SNOW_ENUMERIC", -6: "SNOW_ECUDA", -7: "SNOW_ESTATE", -8: "SNOW_EUNSUPPORTED",
+                -9: "SNOW_ECAPACITY"}
+MODE_REFERENCE, MODE_FAST = 0, 1
+(K_RIGID_ADVANCE, K_G_RESET, K_P2G, K_G_FORCE, K_G2P, K_P_ADVANCE, K_G_MASS, K_P_VOLUME) = range(8)
+
+# Every symbol include/snow_mpm.h declares.
+EXPORTS = [
+    "snow_params_default", "snow_default_walls", "snow_ctx_create", "snow_ctx_destroy", "snow_last_error",
+    "snow_ctx_bytes_in_use", "snow_ctx_set_profiling", "snow_ctx_stream", "snow_ctx_synchronize","snow_scene_create",
+    "snow_scene_destroy", "snow_scene_footprint", "snow_scene_upload", "snow_scene_upload_std140",
+    "snow_scene_set_volume", "snow_scene_init", "snow_scene_step", "snow_dispatch", "snow_scene_download", "snow_scene_download_std140",
+    "snow_scene_download_grid", "snow_scene_download_colliders", "snow_scene_stats", "snow_scene_size",
+    "snow_scene_cell_keys", "snow_scene_phase_times", "snow_batch_create", "snow_batch_destroy",
+    "snow_batch_step", "snow_batch_autotune",
+]
+
+
+class SnowParams(C.Structure):
+    _fields_ = [("grid_pos", C.c_float * 3), ("grid_dim", C.c_int * 3), ("grid_spacing", C.c_float),
+                ("young", C.c_float), ("poisson", C.c_float), ("hardening", C.c_float),
+                ("crit_compression", C.c_float), ("crit_stretch", C.c_float), ("alpha", C.c_float),
+                ("gravity", C.c_float * 3), ("mode", C.c_int), ("sort_interval", C.c_int)]
+
+
+class SnowCollider(C.Structure):
+    _fields_ = [("pos", C.c_float * 3), ("type", C.c_int32), ("vel", C.c_float * 3), ("radius", C.c_float),
+                ("normal", C.c_float * 3), ("friction", C.c_float)]
+
+
+class SnowStats(C.Structure):
+    _fields_ = [("mass", C.c_double), ("momentum", C.c_double * 3), ("kinetic_energy", C.c_double),
+                ("center_of_mass", C.c_double * 3), ("bbox_min", C.c_double * 3), ("bbox_max", C.c_double * 3),
+                ("mean_jp", C.c_double), ("nonfinite", C.c_uint64), ("n", C.c_uint64)]
+
+
+class SnowPhaseTimes(C.Structure):
+    _fields_ = [("sort_ms", C.c_double), ("p2g_ms", C.c_double), ("grid_ms", C.c_double), ("g2p_ms", C.c_double),
+                ("other_ms", C.c_double), ("total_ms", C.c_double), ("steps", C.c_uint64)]
+
+
+class SnowError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Loads the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} missing: build it with snow_gb300.build.build() (needs nvcc)")
+    L = C.CDLL(path)
+    vp, fp, ip, up, sz = C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_int32), C.POINTER(C.c_uint32), C.c_size_t
+    L.snow_params_default.argtypes = [C.POINTER(SnowParams)]
+    L.snow_params_default.restype = None
+    L.snow_default_walls.argtypes = [C.POINTER(SnowParams), C.POINTER(SnowCollider)]
+    L.snow_ctx_create.argtypes = [C.c_int, sz, C.POINTER(vp)]
+    L.snow_ctx_destroy.argtypes = [vp]
+    L.snow_ctx_destroy.restype = None
+    L.snow_last_error.argtypes = [vp]
+    L.snow_last_error.restype = C.c_char_p
+    L.snow_ctx_bytes_in_use.argtypes = [vp]
+    L.snow_ctx_bytes_in_use.restype = sz
+    L.snow_ctx_set_profiling.argtypes = [vp, C.c_int]
+    L.snow_ctx_synchronize.argtypes = [vp]
+    L.snow_ctx_stream.argtypes = [vp]
+    L.snow_ctx_stream.restype = vp
+    L.snow_scene_create.argtypes = [vp, C.POINTER(SnowParams), C.POINTER(SnowCollider), C.c_int, sz, C.POINTER(vp)]
+    L.snow_scene_destroy.argtypes = [vp]
+    L.snow_scene_destroy.restype = None
+    L.snow_scene_footprint.argtypes = [C.POINTER(SnowParams), sz]
+    L.snow_scene_footprint.restype = sz
+    L.snow_scene_upload.argtypes = [vp, fp, fp, fp, fp, fp, sz]
+    L.snow_scene_upload_std140.argtypes = [vp, fp, ip, fp, fp, sz]
+    L.snow_scene_set_volume.argtypes = [vp, fp, sz]
+    L.snow_scene_init.argtypes = [vp]
+    L.snow_scene_step.argtypes = [vp, C.c_double, C.c_int]
+    L.snow_dispatch.argtypes = [vp, C.c_int, C.c_double]
+    L.snow_scene_download.argtypes = [vp, fp, fp, fp, fp, fp, fp]
+    L.snow_scene_download_std140.argtypes = [vp, fp, ip, fp, fp]
+    L.snow_scene_download_grid.argtypes = [vp, fp, fp, fp, fp]
+    L.snow_scene_download_colliders.argtypes = [vp, C.POINTER(SnowCollider)]
+    L.snow_scene_stats.argtypes = [vp, C.POINTER(SnowStats)]
+    L.snow_scene_size.argtypes = [vp]
+    L.snow_scene_size.restype = sz
+    L.snow_scene_cell_keys.argtypes = [vp, up, up]
+    L.snow_scene_phase_times.argtypes = [vp, C.POINTER(SnowPhaseTimes), C.c_int]
+    L.snow_batch_create.argtypes = [vp, C.POINTER(vp), C.c_int, C.POINTER(vp)]
+    L.snow_batch_destroy.argtypes = [vp]
+    L.snow_batch_destroy.restype = None
+    L.snow_batch_step.argtypes = [vp, C.POINTER(C.c_double), C.c_int]
+    L.snow_batch_autotune.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_int)]
+    _lib = L
+    return L
+
+
+def ptr(a, t=C.c_float):
+    return None if a is None else a.ctypes.data_as(C.POINTER(t))

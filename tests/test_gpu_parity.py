@@ -1,0 +1,233 @@
+"""GPU parity tests through the C ABI (snow_gb300 on sm_103a) against the
+oracle on the same seeded inputs.
+
+Tolerances:
+  * SNOW_MODE_REFERENCE vs the FAITHFUL32 oracle (the shaders' arithmetic,
+    pinned bit-for-bit to the reference's own shader code): the kernels round
+    every operation like the oracle (no FMA); only expf (CUDA's, <= 2 ulp vs
+    glibc) differs, which moves the truncated int32 force contributions by a
+    count now and then. Density after init is bit-exact (no expf on that
+    path); after steps: |dx| <= 1e-6 m, |dv| <= 1e-4 m/s, |dF| <= 1e-5.
+  * SNOW_MODE_FAST vs the EXACT64 oracle (FP64, no fixed point, no V
+    rounding), one step: per-field relative error <= 1e-5 with denominators
+    floored at the field's scale:
+        x  : |dx| / max(|x|, 1e-3)
+        v  : |dv| / max(|v|, 1e-3 m/s)
+        F_E: max|dF| / max|F| per particle
+        J_p: |dJ| / |J|
+  * binning: keys and stable permutation bit-exact vs std::stable_sort.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from snow_gb300 import scenes
+from tests._util import golden_names, load_golden, mat3x3_from_std140
+
+gpu = pytest.mark.gpu
+
+REL_TOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from snow_gb300 import api
+    return api.Context(0)
+
+
+def sim(ctx, scene, mode, **kw):
+    from snow_gb300 import api
+    return api.SimScene(ctx, scene, mode=mode, **kw)
+
+
+def field_errors(gpu_state, ref):
+    """Relative errors per field as documented in the module docstring."""
+    x, v = gpu_state["x"].astype(np.float64), gpu_state["v"].astype(np.float64)
+    ex = np.abs(x - ref["x"]) / np.maximum(np.abs(ref["x"]), 1e-3)
+    ev = np.linalg.norm(v - ref["v"], axis=1) / np.maximum(np.linalg.norm(ref["v"], axis=1), 1e-3)
+    fe, rfe = gpu_state["FE"].astype(np.float64), ref["FE"]
+    ef = np.abs(fe - rfe).max((1, 2)) / np.abs(rfe).max((1, 2))
+    ej = np.abs(gpu_state["Jp"].astype(np.float64) - ref["Jp"]) / np.abs(ref["Jp"])
+    w = int(np.argmax(ev))
+    return dict(x=ex.max(), v=ev.max(), FE=ef.max(), Jp=ej.max(),
+                x_p99=np.percentile(ex, 99), v_p99=np.percentile(ev, 99), FE_p99=np.percentile(ef, 99),
+                v_worst_ref=ref["v"][w].tolist(), v_worst_gpu=v[w].tolist(), x_worst=ref["x"][w].tolist())
+
+
+# ---------------------------------------------------------------------------
+@gpu
+@pytest.mark.parametrize("name", golden_names())
+def test_reference_mode_matches_golden_and_faithful_oracle(ctx, name):
+    from snow_gb300 import native as N
+    s, z = load_golden(name)
+    bufs = (z["pxm0"], z["pv0"]) + s.std140()[2:]
+    g = sim(ctx, s, N.MODE_REFERENCE).upload_std140(*bufs).init()
+    _, pv, _, _ = g.download_std140()
+    assert np.array_equal(pv[:, 3], z["pv_init"][:, 3]), "density after init must be bit-exact"
+    for k in range(1, int(z["steps"]) + 1):
+        g.step(s.dt, 1)
+        pxm, pv, fe, fp = g.download_std140()
+        assert np.abs(pxm[:, :3] - z[f"pxm_{k}"][:, :3]).max() <= 1e-6
+        assert np.abs(pv[:, :3].astype(np.int64) - z[f"pv_{k}"][:, :3]).max() <= 1e4  # 1e-4 m/s
+        fe9 = fe.reshape(-1, 4, 4)[:, :3, :3].reshape(-1, 9)
+        fp9 = fp.reshape(-1, 4, 4)[:, :3, :3].reshape(-1, 9)
+        assert np.abs(fe9 - z[f"fe_{k}"]).max() <= 1e-5
+        assert np.abs(fp9 - z[f"fp_{k}"]).max() <= 1e-5
+
+
+@gpu
+def test_reference_mode_kernels_one_by_one(ctx):
+    """Each reference-mode kernel against the same oracle phase."""
+    from snow_gb300 import native as N
+    s = scenes.small_scene(n=3000, grid_edge=32, seed=21, v0=(0.5, -3.0, 0.25))
+    bufs = s.std140()
+    g = sim(ctx, s, N.MODE_REFERENCE).upload_std140(*bufs).init()
+    o = O.OracleSim(s, mode=O.FAITHFUL32).upload_std140(*bufs).init()
+    o.step()
+    g.step(s.dt, 1)  # leave the identity deformation behind
+    for kern, ph in [(N.K_RIGID_ADVANCE, O.PH_RIGID), (N.K_G_RESET, O.PH_RESET), (N.K_P2G, O.PH_P2G)]:
+        g.dispatch(kern, s.dt)
+        o.phase(ph)
+    gd, od = g.grid(), o.grid()
+    assert np.abs(gd["mass"] - od["mass"]).max() <= 1e-8 * 2  # exact int sums, 1 count = 1e-8
+    assert np.abs(gd["mom"] - od["mom"]).max() <= 64 * 1e-8
+    assert np.abs(gd["force"] - od["force"]).max() <= 64 * 1e-6
+    g.dispatch(N.K_G_FORCE, s.dt)
+    o.phase(O.PH_GRID)
+    gd, od = g.grid(), o.grid()
+    assert np.abs(gd["vstar"] - od["vstar"]).max() <= 1e-5
+    for kern, ph in [(N.K_G2P, O.PH_G2P), (N.K_P_ADVANCE, O.PH_ADVANCE)]:
+        g.dispatch(kern, s.dt)
+        o.phase(ph)
+    a = g.download(fp=True)
+    b = o.state()
+    assert np.abs(a["x"] - b["x"]).max() <= 1e-6
+    assert np.abs(a["v"] - b["v"]).max() <= 1e-4
+    assert np.abs(a["FE"] - b["FE"]).max() <= 1e-5
+
+
+# ---------------------------------------------------------------------------
+def _exact_oracle(s, vround=False):
+    return O.OracleSim(s, mode=O.EXACT64, vround=vround)
+
+
+@gpu
+@pytest.mark.parametrize("seed,n,edge,v0", [(31, 4000, 32, (0.0, -2.0, 0.0)), (32, 6000, 40, (1.0, -4.0, 0.5)),
+                                            (33, 2500, 24, (3.0, 0.0, -2.0))])
+def test_fast_single_step_from_rest_within_1e5(ctx, seed, n, edge, v0):
+    from snow_gb300 import native as N
+    s = scenes.small_scene(n=n, grid_edge=edge, seed=seed, v0=v0)
+    g = sim(ctx, s, N.MODE_FAST).upload().init().step(s.dt, 1)
+    o = _exact_oracle(s).upload().init().step()
+    e = field_errors(g.download(), o.state())
+    assert max(e["x"], e["v"], e["FE"], e["Jp"]) <= REL_TOL, e
+
+
+@gpu
+@pytest.mark.parametrize("warm_steps", [5, 20])
+def test_fast_single_step_from_deformed_state_within_1e5(ctx, warm_steps):
+    """Advance the FP64 oracle, restart both from its (float-rounded) state
+    and compare one step."""
+    from snow_gb300 import native as N
+    s = scenes.small_scene(n=4000, grid_edge=32, seed=41, v0=(0.5, -6.0, 0.3), center=(0.5, 0.22, 0.5))
+    warm = _exact_oracle(s).upload().init().step(n=warm_steps).state()
+    s2 = scenes.Scene(**{k: getattr(s, k) for k in ("grid_pos", "grid_dim", "grid_spacing", "young", "poisson",
+                                                    "hardening", "crit_compression", "crit_stretch", "alpha",
+                                                    "gravity", "dt", "colliders")})
+    s2.x = warm["x"].astype(np.float32)
+    s2.v = warm["v"].astype(np.float32)
+    s2.m = s.m.copy()
+    fe = warm["FE"].astype(np.float32)
+    fp = warm["FP"].astype(np.float32)
+    rho = warm["rho"]
+    assert np.abs(fe - np.eye(3)).max() > 1e-4, "the warm-up must deform the snow"
+    o = _exact_oracle(s2).upload(FE=fe.astype(np.float64), FP=fp.astype(np.float64)).set_density(rho).step()
+    g = sim(ctx, s2, N.MODE_FAST).upload(FE=fe.reshape(-1, 9), FP=fp.reshape(-1, 9))
+    g.set_volume((s2.m / rho).astype(np.float32)).init().step(s.dt, 1)
+    e = field_errors(g.download(), o.state())
+    assert max(e["x"], e["v"], e["FE"], e["Jp"]) <= REL_TOL, e
+
+
+@gpu
+def test_fast_grid_after_p2g_and_grid_update(ctx):
+    from snow_gb300 import native as N
+    s = scenes.small_scene(n=5000, grid_edge=32, seed=51, v0=(0.2, -2.0, 0.1))
+    g = sim(ctx, s, N.MODE_FAST).upload().init().step(s.dt, 2)
+    o = _exact_oracle(s).upload().init().step(n=2)
+    for kern, ph in [(N.K_RIGID_ADVANCE, O.PH_RIGID), (N.K_G_RESET, O.PH_RESET), (N.K_P2G, O.PH_P2G)]:
+        g.dispatch(kern, s.dt)
+        o.phase(ph)
+    gd, od = g.grid(), o.grid()
+    mscale = od["mass"].max()
+    assert np.abs(gd["mass"] - od["mass"]).max() <= REL_TOL * mscale
+    pscale = np.abs(od["mom"]).max()
+    assert np.abs(gd["mom"] - od["mom"]).max() <= REL_TOL * pscale
+    fscale = np.abs(od["force"]).max()
+    assert np.abs(gd["force"] - od["force"]).max() <= 1e-4 * fscale
+    assert abs(gd["mass"].sum() - s.m.astype(np.float64).sum()) <= 1e-5 * s.m.sum()
+    g.dispatch(N.K_G_FORCE, s.dt)
+    o.phase(O.PH_GRID)
+    vs = o.grid()["vstar"]
+    has = od["mass"] > 1e-6 * mscale
+    vscale = np.abs(vs[has]).max()
+    assert np.abs(g.grid()["vstar"][has] - vs[has]).max() <= REL_TOL * max(vscale, 1.0)
+
+
+@gpu
+def test_fast_short_horizon_bulk_statistics(ctx):
+    """100 steps of the cfg1-like snowball: trajectories diverge, bulk
+    quantities agree."""
+    from snow_gb300 import native as N
+    s = scenes.small_scene(n=8000, grid_edge=48, seed=61, v0=(0.0, -2.0, 0.0), center=(0.5, 0.3, 0.5))
+    g = sim(ctx, s, N.MODE_FAST).upload().init().step(s.dt, 100)
+    o = _exact_oracle(s).upload().init().step(n=100)
+    st = g.stats()
+    ref = o.state()
+    m = s.m.astype(np.float64)
+    com = (m[:, None] * ref["x"]).sum(0) / m.sum()
+    mom = (m[:, None] * ref["v"]).sum(0)
+    ke = 0.5 * (m * (ref["v"] ** 2).sum(1)).sum()
+    assert st["nonfinite"] == 0
+    assert np.abs(st["center_of_mass"] - com).max() <= 1e-4
+    assert np.abs(st["momentum"] - mom).max() <= 1e-3 * np.abs(mom).max() + 1e-9
+    assert abs(st["kinetic_energy"] - ke) <= 1e-3 * ke
+    assert abs(st["mean_jp"] - ref["Jp"].mean()) <= 1e-4
+    assert np.abs(st["bbox_min"] - ref["x"].min(0)).max() <= 1e-3
+    assert np.abs(st["bbox_max"] - ref["x"].max(0)).max() <= 1e-3
+
+
+# ---------------------------------------------------------------------------
+@gpu
+@pytest.mark.parametrize("steps", [0, 7])
+def test_cell_keys_and_binning_bit_exact(ctx, steps):
+    from snow_gb300 import native as N
+    s = scenes.small_scene(n=20000, grid_edge=64, seed=71, v0=(1.0, -3.0, 2.0))
+    g = sim(ctx, s, N.MODE_FAST).upload().init()
+    if steps:
+        g.step(s.dt, steps)
+    x = g.download()["x"]
+    keys, perm = g.cell_keys()
+    lin, blk, cperm = O.cell_keys(x, s.grid_pos, s.grid_dim, s.grid_spacing)
+    assert np.array_equal(keys, blk)
+    assert np.array_equal(perm, cperm)
+
+
+@gpu
+def test_binning_edge_cases(ctx):
+    """Particles outside the grid (clamped keys), duplicates, a single
+    particle and a grid whose edge is not a multiple of the block size."""
+    from snow_gb300 import native as N
+    rng = np.random.default_rng(5)
+    s = scenes.unit_box_scene(37, dt=1e-4)
+    x = rng.uniform(-0.1, 1.1, size=(3001, 3)).astype(np.float32)
+    x[1000:1010] = x[999]
+    s.x, s.v, s.m = x, np.zeros_like(x), np.full(len(x), 1e-6, np.float32)
+    g = sim(ctx, s, N.MODE_FAST).upload()
+    g.init()
+    keys, perm = g.cell_keys()
+    _, blk, cperm = O.cell_keys(x, s.grid_pos, s.grid_dim, s.grid_spacing)
+    assert np.array_equal(keys, blk) and np.array_equal(perm, cperm)
+    one = scenes.unit_box_scene(16, dt=1e-4)
+    one.x, one.v, one.m = x[:1].clip(0.3, 0.7), np.zeros((1, 3), np.float32), np.ones(1, np.float32) * 1e-4
+    g1 = sim(ctx, one, N.MODE_FAST).upload().init().step(1e-4, 3)
+    assert g1.stats()["nonfinite"] == 0
