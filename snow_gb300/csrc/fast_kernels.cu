@@ -279,75 +279,221 @@ __device__ __forceinline__ void scatter_particle(const P2GParticle& q, const flo
   }
 }
 
+// P2G work item: up to kItemMax particles binned to one home block b. The
+// tile covers nodes [4b-2, 4b+6] per axis, so a particle whose base cell
+// lies in [4b-1, 4b+4] (its home block plus one cell of drift each way)
+// scatters into it; such a base cell has tile-local coordinates
+// lc = base - (4b-2) - 1 in [0, 5]^3 (216 cells).
+constexpr int kItemMax = 256;
+constexpr int kCellsPerAxis = kTile - 3;  // 6
+constexpr int kCells = kCellsPerAxis * kCellsPerAxis * kCellsPerAxis;
+constexpr int kPd = 10;  // float4 per particle in shared memory
+
+struct P2GShared {
+  float tile[kAccFields * kTile3];
+  // per particle: [m, mv] [A00 A01 A02 A10] [A11 A12 A20 A21] [A22 - - -]
+  //               [wx0..3] [gx0..3] [wy0..3] [gy0..3] [wz0..3] [gz0..3]
+  float4 pd[kItemMax][kPd];
+  short plist[kItemMax];
+  short cells[kCells];
+  int cstart[kCells + 1];
+  int ccount[kCells];
+  int slots[27];
+  int ncells;
+};
+
+// P2G (p2gTransfer.glsl:44-151, or gMassCompute.glsl:33-84 when MASS_ONLY),
+// cell-centric: each particle's stress and axis weights are computed once
+// and parked in shared memory; the CTA buckets its particles by current
+// cell; then each half-warp owns one cell's 4x4x4 stencil (lane = one x-row
+// of 4 nodes, (b, c) = (lane & 3, lane >> 2)), sums the cell's particles in
+// registers and adds the row to the shared tile. The tile's non-empty nodes
+// are then added to the block pool with global atomics.
 template <bool MASS_ONLY>
 __global__ void __launch_bounds__(256) k_p2g(const SceneDev* __restrict__ scenes, const int* __restrict__ item_prefix,
                                              int nscenes) {
-  __shared__ float tile[kAccFields][kTile3];
-  __shared__ int slots[27];
+  extern __shared__ float4 smem_raw[];
+  P2GShared& sh = *reinterpret_cast<P2GShared*>(smem_raw);
   constexpr int nf = MASS_ONLY ? 1 : kAccFields;
   const int total = item_prefix[nscenes];
   const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
   for (int u = blockIdx.x; u < total; u += gridDim.x) {
     const int s = find_scene(item_prefix, nscenes, u);
     const SceneDev& S = scenes[s];
     const int4 it = S.items[u - item_prefix[s]];
-    const int blk = it.x, start = it.y, cnt = it.z;
+    const int blk = it.x, start = it.y, cnt = min(it.z, kItemMax);
     const int bx = blk % S.bdim[0], by = (blk / S.bdim[0]) % S.bdim[1], bz = blk / (S.bdim[0] * S.bdim[1]);
     const int ox = 4 * bx - 2, oy = 4 * by - 2, oz = 4 * bz - 2;
-    for (int i = threadIdx.x; i < nf * kTile3; i += blockDim.x) (&tile[0][0])[i] = 0.0f;
+    for (int i = threadIdx.x; i < nf * kTile3; i += blockDim.x) sh.tile[i] = 0.0f;
+    for (int i = threadIdx.x; i < kCells; i += blockDim.x) sh.ccount[i] = 0;
     if (threadIdx.x < 27) {
       const int k = threadIdx.x;
       const int cx = bx - 1 + k % 3, cy = by - 1 + (k / 3) % 3, cz = bz - 1 + k / 9;
-      slots[k] = (cx >= 0 && cy >= 0 && cz >= 0 && cx < S.bdim[0] && cy < S.bdim[1] && cz < S.bdim[2])
-                     ? S.blk_slot[block_id(S, cx, cy, cz)]
-                     : -1;
+      sh.slots[k] = (cx >= 0 && cy >= 0 && cz >= 0 && cx < S.bdim[0] && cy < S.bdim[1] && cz < S.bdim[2])
+                        ? S.blk_slot[block_id(S, cx, cy, cz)]
+                        : -1;
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+    // ---- phase 1: one thread per particle -------------------------------
+    int my_cell = -1, my_rank = 0;
+    const int i = threadIdx.x;
+    if (i < cnt) {
       const int p = start + i;
       const float4 xm = S.xm[p];
-      if (!MASS_ONLY && fabsf(xm.w) > 100.0f) continue;  // p2gTransfer.glsl:64-66
-      const float pg[3] = {(xm.x - S.gpos[0]) / S.h, (xm.y - S.gpos[1]) / S.h, (xm.z - S.gpos[2]) / S.h};
-      const int base[3] = {(int)pg[0], (int)pg[1], (int)pg[2]};
-      float wx[4], gx[4], wy[4], gy[4], wz[4], gz[4];
-      axis_weights(pg[0], base[0], wx, gx);
-      axis_weights(pg[1], base[1], wy, gy);
-      axis_weights(pg[2], base[2], wz, gz);
-      const P2GParticle q = p2g_particle(S, p, xm, MASS_ONLY);
-      const int tx = base[0] - 1 - ox, ty = base[1] - 1 - oy, tz = base[2] - 1 - oz;
-      if (tx >= 0 && ty >= 0 && tz >= 0 && tx <= kTile - 4 && ty <= kTile - 4 && tz <= kTile - 4) {
-        const int t0 = tx + kTile * ty + kTile * kTile * tz;
-        scatter_particle<MASS_ONLY>(q, wx, gx, wy, gy, wz, gz, lane,
-                                    [&](int f, int a, int b, int c, float v) {
-                                      atomicAdd(&tile[f][t0 + a + kTile * b + kTile * kTile * c], v);
-                                    });
-      } else {
-        // The particle left its home block's tile since the last binning:
-        // scatter straight into the pool.
-        atomicAdd(&S.counters[CNT_FALLBACK], 1);
-        scatter_particle<MASS_ONLY>(q, wx, gx, wy, gy, wz, gz, lane, [&](int f, int a, int b, int c, float v) {
-          const int g0 = base[0] - 1 + a, g1 = base[1] - 1 + b, g2 = base[2] - 1 + c;
-          if (g0 < 0 || g1 < 0 || g2 < 0 || g0 >= S.dim[0] || g1 >= S.dim[1] || g2 >= S.dim[2]) return;
-          const int sl = S.blk_slot[block_id(S, g0 >> 2, g1 >> 2, g2 >> 2)];
-          if (sl < 0) return;
-          atomicAdd(&S.acc[(size_t)sl * kAccBlockFloats + f * kBlockNodes + (g0 & 3) + 4 * (g1 & 3) + 16 * (g2 & 3)],
-                    v);
-        });
+      if (MASS_ONLY || fabsf(xm.w) <= 100.0f) {  // p2gTransfer.glsl:64-66
+        const float pg[3] = {(xm.x - S.gpos[0]) / S.h, (xm.y - S.gpos[1]) / S.h, (xm.z - S.gpos[2]) / S.h};
+        const int base[3] = {(int)pg[0], (int)pg[1], (int)pg[2]};
+        float wx[4], gx[4], wy[4], gy[4], wz[4], gz[4];
+        axis_weights(pg[0], base[0], wx, gx);
+        axis_weights(pg[1], base[1], wy, gy);
+        axis_weights(pg[2], base[2], wz, gz);
+        const P2GParticle q = p2g_particle(S, p, xm, MASS_ONLY);
+        const int lx = base[0] - 1 - ox, ly = base[1] - 1 - oy, lz = base[2] - 1 - oz;
+        if (lx >= 0 && ly >= 0 && lz >= 0 && lx < kCellsPerAxis && ly < kCellsPerAxis && lz < kCellsPerAxis) {
+          my_cell = lx + kCellsPerAxis * ly + kCellsPerAxis * kCellsPerAxis * lz;
+          my_rank = atomicAdd(&sh.ccount[my_cell], 1);
+          float4* d = sh.pd[i];
+          if (MASS_ONLY) {
+            d[0] = make_float4(q.m, 0.0f, 0.0f, 0.0f);
+          } else {
+            const bool f = q.force;
+            d[0] = make_float4(q.m, q.mv[0], q.mv[1], q.mv[2]);
+            d[1] = f ? make_float4(q.A[0][0], q.A[0][1], q.A[0][2], q.A[1][0]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            d[2] = f ? make_float4(q.A[1][1], q.A[1][2], q.A[2][0], q.A[2][1]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            d[3] = make_float4(f ? q.A[2][2] : 0.0f, 0.0f, 0.0f, 0.0f);
+          }
+          d[4] = make_float4(wx[0], wx[1], wx[2], wx[3]);
+          d[5] = make_float4(gx[0], gx[1], gx[2], gx[3]);
+          d[6] = make_float4(wy[0], wy[1], wy[2], wy[3]);
+          d[7] = make_float4(gy[0], gy[1], gy[2], gy[3]);
+          d[8] = make_float4(wz[0], wz[1], wz[2], wz[3]);
+          d[9] = make_float4(gz[0], gz[1], gz[2], gz[3]);
+        } else {
+          // The particle drifted out of its home block's tile since the last
+          // binning: scatter it straight into the pool.
+          atomicAdd(&S.counters[CNT_FALLBACK], 1);
+          scatter_particle<MASS_ONLY>(q, wx, gx, wy, gy, wz, gz, lane, [&](int fld, int a, int b, int c, float v) {
+            const int g0 = base[0] - 1 + a, g1 = base[1] - 1 + b, g2 = base[2] - 1 + c;
+            if (g0 < 0 || g1 < 0 || g2 < 0 || g0 >= S.dim[0] || g1 >= S.dim[1] || g2 >= S.dim[2]) return;
+            const int sl = S.blk_slot[block_id(S, g0 >> 2, g1 >> 2, g2 >> 2)];
+            if (sl < 0) return;
+            atomicAdd(&S.acc[(size_t)sl * kAccBlockFloats + fld * kBlockNodes + (g0 & 3) + 4 * (g1 & 3) + 16 * (g2 & 3)],
+                      v);
+          });
+        }
       }
     }
     __syncthreads();
+    // ---- bucket offsets and the list of occupied cells (warp 0) -----------
+    if (warp == 0) {
+      constexpr int per = (kCells + 31) / 32;  // 7 cells per lane
+      int cntv[per];
+      int sum = 0, occ = 0;
+#pragma unroll
+      for (int j = 0; j < per; j++) {
+        const int ci = lane * per + j;
+        cntv[j] = ci < kCells ? sh.ccount[ci] : 0;
+        sum += cntv[j];
+        occ += cntv[j] > 0;
+      }
+      int isum = sum, iocc = occ;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int a = __shfl_up_sync(0xffffffffu, isum, o);
+        const int b = __shfl_up_sync(0xffffffffu, iocc, o);
+        if (lane >= o) {
+          isum += a;
+          iocc += b;
+        }
+      }
+      int run = isum - sum, rocc = iocc - occ;
+#pragma unroll
+      for (int j = 0; j < per; j++) {
+        const int ci = lane * per + j;
+        if (ci < kCells) {
+          sh.cstart[ci] = run;
+          if (cntv[j] > 0) sh.cells[rocc++] = (short)ci;
+          run += cntv[j];
+        }
+      }
+      if (lane == 31) {
+        sh.cstart[kCells] = isum;
+        sh.ncells = iocc;
+      }
+    }
+    __syncthreads();
+    if (my_cell >= 0) sh.plist[sh.cstart[my_cell] + my_rank] = (short)i;
+    __syncthreads();
+    // ---- phase 2: one half-warp per occupied cell ---------------------------
+    {
+      const int hw = threadIdx.x >> 4, l16 = threadIdx.x & 15;
+      const int b = l16 & 3, c = l16 >> 2;
+      const int nhw = blockDim.x >> 4;
+      for (int k = hw; k < sh.ncells; k += nhw) {
+        const int ci = sh.cells[k];
+        const int j0 = sh.cstart[ci], j1 = sh.cstart[ci + 1];
+        float acc[4][kAccFields];
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+          for (int f = 0; f < kAccFields; f++) acc[a][f] = 0.0f;
+        for (int j = j0; j < j1; j++) {
+          const float4* d = sh.pd[sh.plist[j]];
+          const float* df = reinterpret_cast<const float*>(d);
+          const float4 w4 = d[4];
+          const float wxa[4] = {w4.x, w4.y, w4.z, w4.w};
+          const float wyb = df[6 * 4 + b], wzc = df[8 * 4 + c];
+          const float t1 = wyb * wzc;
+          const float4 d0 = d[0];
+          const float mw = d0.x * t1;
+          if (MASS_ONLY) {
+#pragma unroll
+            for (int a = 0; a < 4; a++) acc[a][0] += wxa[a] * mw;
+            continue;
+          }
+          const float4 g4 = d[5];
+          const float gxa[4] = {g4.x, g4.y, g4.z, g4.w};
+          const float gyb = df[7 * 4 + b], gzc = df[9 * 4 + c];
+          const float t2 = gyb * wzc, t3 = wyb * gzc;
+          const float4 a1 = d[1], a2 = d[2], a3 = d[3];
+          // A rows: r0 = (a1.x a1.y a1.z), r1 = (a1.w a2.x a2.y), r2 = (a2.z a2.w a3.x)
+          const float pv[3] = {d0.y * t1, d0.z * t1, d0.w * t1};
+          const float kk[3] = {a1.x * t1, a1.w * t1, a2.z * t1};
+          const float hh[3] = {a1.y * t2 + a1.z * t3, a2.x * t2 + a2.y * t3, a2.w * t2 + a3.x * t3};
+#pragma unroll
+          for (int a = 0; a < 4; a++) {
+            acc[a][0] += wxa[a] * mw;
+#pragma unroll
+            for (int r = 0; r < 3; r++) {
+              acc[a][1 + r] += wxa[a] * pv[r];
+              acc[a][4 + r] += gxa[a] * kk[r] + wxa[a] * hh[r];
+            }
+          }
+        }
+        const int lx = ci % kCellsPerAxis, ly = (ci / kCellsPerAxis) % kCellsPerAxis,
+                  lz = ci / (kCellsPerAxis * kCellsPerAxis);
+        const int t0 = lx + kTile * (ly + b) + kTile * kTile * (lz + c);
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+          for (int f = 0; f < nf; f++) atomicAdd(&sh.tile[f * kTile3 + t0 + a], acc[a][f]);
+      }
+    }
+    __syncthreads();
+    // ---- flush the tile's non-empty nodes to the pool -----------------------
     for (int t = threadIdx.x; t < kTile3; t += blockDim.x) {
-      const float m = tile[0][t];
+      const float m = sh.tile[t];
       if (m == 0.0f) continue;
       const int tx = t % kTile, ty = (t / kTile) % kTile, tz = t / (kTile * kTile);
       const int g0 = ox + tx, g1 = oy + ty, g2 = oz + tz;
       if (g0 < 0 || g1 < 0 || g2 < 0 || g0 >= S.dim[0] || g1 >= S.dim[1] || g2 >= S.dim[2]) continue;
       const int k = ((g0 >> 2) - bx + 1) + 3 * ((g1 >> 2) - by + 1) + 9 * ((g2 >> 2) - bz + 1);
-      const int sl = slots[k];
+      const int sl = sh.slots[k];
       if (sl < 0) continue;
       float* dst = S.acc + (size_t)sl * kAccBlockFloats + (g0 & 3) + 4 * (g1 & 3) + 16 * (g2 & 3);
 #pragma unroll
-      for (int f = 0; f < nf; f++) atomicAdd(dst + f * kBlockNodes, tile[f][t]);
+      for (int f = 0; f < nf; f++) atomicAdd(dst + f * kBlockNodes, sh.tile[f * kTile3 + t]);
     }
     __syncthreads();
   }
@@ -710,10 +856,18 @@ void fast_mark(const SceneDev* scenes, const int* chunk_prefix, int nscenes, lon
 
 void fast_p2g(const SceneDev* scenes, const int* item_prefix, int nscenes, int grid_ctas, bool mass_only,
               int threads, cudaStream_t st) {
+  static bool configured = false;
+  const int smem = (int)sizeof(P2GShared);
+  if (!configured) {
+    cudaFuncSetAttribute(k_p2g<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_p2g<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    configured = true;
+  }
+  (void)threads;  // the item layout needs exactly kItemMax threads
   if (mass_only)
-    k_p2g<true><<<grid_ctas, threads, 0, st>>>(scenes, item_prefix, nscenes);
+    k_p2g<true><<<grid_ctas, kItemMax, smem, st>>>(scenes, item_prefix, nscenes);
   else
-    k_p2g<false><<<grid_ctas, threads, 0, st>>>(scenes, item_prefix, nscenes);
+    k_p2g<false><<<grid_ctas, kItemMax, smem, st>>>(scenes, item_prefix, nscenes);
 }
 
 void fast_grid(const SceneDev* scenes, const int* active_prefix, int nscenes, int grid_ctas, bool clear_only,
