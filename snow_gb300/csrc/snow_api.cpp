@@ -57,10 +57,13 @@ struct snow_scene {
   BinScratch bin{};
   FastTuning tune{};
   int key_bits = 0;
-  int* d_prefix = nullptr;  // [0,2) items, [2,4) active, [4,6) chunks, [6,8) blocks
+  int* d_prefix = nullptr;  // [0,2) items, [2,4) active, [6,8) blocks
   int steps_since_sort = 1 << 30;
   int version = 0;
   bool volume_given = false;
+  // FAST: acc holds the P2G sums of the current particle state (the next
+  // step's grid update consumes them)
+  bool p2g_ready = false;
   // graphs of one step, keyed by (dt, with sort)
   cudaGraphExec_t g_plain = nullptr, g_sort = nullptr;
   float g_dt = NAN;
@@ -72,9 +75,9 @@ struct snow_batch {
   snow_ctx* ctx = nullptr;
   std::vector<snow_scene*> scenes;
   SceneDev* d_scenes = nullptr;
-  int* d_prefix = nullptr;  // items (n+1), active (n+1), chunks (n+1), blocks (n+1)
+  int* d_prefix = nullptr;  // items (n+1), active (n+1), unused (n+1), blocks (n+1)
   std::vector<int> versions;
-  long long total_chunks = 0, total_blocks = 0;
+  long long total_blocks = 0;
   int step_count = 0;
   std::map<int, cudaGraphExec_t> graphs;  // phase (step % sort_interval) -> graph
   std::vector<float> g_dt;
@@ -180,6 +183,7 @@ void fill_sd_params(snow_scene* s) {
     d.grav[k] = s->p.gravity[k];
   }
   d.h = s->p.grid_spacing;
+  d.inv_h = 1.0f / s->p.grid_spacing;
   d.nblocks = d.bdim[0] * d.bdim[1] * d.bdim[2];
   d.young = s->p.young;
   d.poisson = s->p.poisson;
@@ -217,7 +221,7 @@ snow_status fast_alloc_particles(snow_scene* s, size_t cap) {
       (st = salloc(s, cap, &b.tmp4[3])) || (st = salloc(s, cap, &b.tmp2)) || (st = salloc(s, cap, &b.tmp_pid)))
     return st;
   b.n_cap = cap;
-  const int items_max = s->tune.p2g_items_max;
+  const int items_max = fast_item_threads();
   d.item_cap = (int)(cap / items_max + std::min<size_t>(cap, (size_t)d.nblocks) + 1);
   if ((st = salloc(s, (size_t)d.item_cap, &d.items))) return st;
   return SNOW_OK;
@@ -228,72 +232,74 @@ snow_status fast_alloc_grid(snow_scene* s) {
   snow_status st;
   const size_t nb = (size_t)d.nblocks;
   if ((st = salloc(s, nb, &d.blk_slot)) || (st = salloc(s, nb, &d.blk_flag)) ||
-      (st = salloc(s, nb, &s->bin.bstart)) || (st = salloc(s, nb, &s->bin.bend)) ||
-      (st = salloc(s, nb, &s->bin.home)) || (st = salloc(s, (size_t)kCounterStride, &d.counters)) ||
-      (st = salloc(s, (size_t)8, &s->d_prefix)) || (st = salloc(s, (size_t)1, &s->sd_dev)))
+      (st = salloc(s, nb * kAccBlockFloats, &d.acc)) || (st = salloc(s, nb, &s->bin.bstart)) ||
+      (st = salloc(s, nb, &s->bin.bend)) || (st = salloc(s, nb, &s->bin.home)) ||
+      (st = salloc(s, (size_t)kCounterStride, &d.counters)) || (st = salloc(s, (size_t)8, &s->d_prefix)) ||
+      (st = salloc(s, (size_t)1, &s->sd_dev)))
     return st;
   snow_ctx* ctx = s->ctx;
   CK(cudaMemsetAsync(d.blk_flag, 0, nb * sizeof(int), ctx->stream));
   CK(cudaMemsetAsync(d.blk_slot, 0xff, nb * sizeof(int), ctx->stream));
+  CK(cudaMemsetAsync(d.acc, 0, nb * kAccBlockFloats * sizeof(float), ctx->stream));
   CK(cudaMemsetAsync(d.counters, 0, kCounterStride * sizeof(int), ctx->stream));
   return SNOW_OK;
 }
 
+// The output pool (grid-update results of the active blocks).
 snow_status fast_alloc_pool(snow_scene* s, int cap_blocks) {
   SceneDev& d = s->sd;
   snow_ctx* ctx = s->ctx;
-  if (d.acc) dfree_one(ctx, s, d.acc);
   if (d.gout) dfree_one(ctx, s, d.gout);
   if (d.active) dfree_one(ctx, s, d.active);
-  d.acc = d.gout = nullptr;
+  d.gout = nullptr;
   d.active = nullptr;
   snow_status st;
-  if ((st = salloc(s, (size_t)cap_blocks * kAccBlockFloats, &d.acc)) ||
-      (st = salloc(s, (size_t)cap_blocks * kOutBlockFloats, &d.gout)) || (st = salloc(s, (size_t)cap_blocks, &d.active)))
+  if ((st = salloc(s, (size_t)cap_blocks * kOutBlockFloats, &d.gout)) || (st = salloc(s, (size_t)cap_blocks, &d.active)))
     return st;
-  CK(cudaMemsetAsync(d.acc, 0, (size_t)cap_blocks * kAccBlockFloats * sizeof(float), ctx->stream));
   d.pool_cap = cap_blocks;
   return SNOW_OK;
 }
 
-// Host prefix arrays of a one-scene "batch": [items 0,1][active 2,3][chunks 4,5][blocks 6,7].
+// Prefix arrays of a one-scene work space: [items 0,1][active 2,3][blocks 6,7];
+// items and active are written on the device.
 snow_status fast_single_prefix(snow_scene* s) {
   snow_ctx* ctx = s->ctx;
-  const int chunk = s->tune.g2p_threads;
-  int h[8] = {0, 0, 0, 0, 0, (int)((s->n + chunk - 1) / chunk), 0, s->sd.nblocks};
-  CK(cudaMemcpyAsync(s->d_prefix + 4, h + 4, 4 * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  int h[2] = {0, s->sd.nblocks};
+  CK(cudaMemcpyAsync(s->d_prefix + 6, h, 2 * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   return SNOW_OK;
 }
 
-int p2g_ctas(const snow_scene* s) { return num_sms() * (s->tune.p2g_threads >= 256 ? 4 : 8); }
+int item_ctas() { return num_sms() * 2; }
 int grid_ctas() { return num_sms() * 8; }
 
-// Binning: keys, radix sort, permutation, work items.
+// Binning: keys, radix sort, permutation, work items, item prefix.
 void fast_bin(snow_scene* s, cudaStream_t st) {
   fast_sort_keys(s->sd, s->sd_dev, s->bin, s->key_bits, st);
-  fast_apply_bins(s->sd, s->sd_dev, s->bin, s->tune.p2g_items_max, st);
+  fast_apply_bins(s->sd, s->sd_dev, s->bin, fast_item_threads(), st);
+  fast_prefix(s->sd_dev, 1, s->d_prefix + 0, s->d_prefix + 2, st);
 }
 
-// The step's kernels for a one-scene batch (enqueue only).
-void fast_enqueue_p2g(snow_scene* s, bool bin, bool mass_only, cudaStream_t st) {
-  if (bin) fast_bin(s, st);
+// Active blocks of the pending P2G sums -> pool slots (and prefixes).
+void fast_enqueue_compact(snow_scene* s, cudaStream_t st) {
   fast_begin_step(s->sd_dev, 1, st);
   fast_compact(s->sd_dev, s->d_prefix + 6, 1, s->sd.nblocks, st);
-  fast_prefix(s->sd_dev, 1, CNT_ITEMS, s->d_prefix + 0, st);
-  fast_prefix(s->sd_dev, 1, CNT_ACTIVE, s->d_prefix + 2, st);
-  fast_p2g(s->sd_dev, s->d_prefix + 0, 1, p2g_ctas(s), mass_only, s->tune.p2g_threads, st);
+  fast_prefix(s->sd_dev, 1, s->d_prefix + 0, s->d_prefix + 2, st);
 }
-void fast_enqueue_grid(snow_scene* s, cudaStream_t st) { fast_grid(s->sd_dev, s->d_prefix + 2, 1, grid_ctas(), false, st); }
-void fast_enqueue_g2p(snow_scene* s, cudaStream_t st) {
-  const int chunk = s->tune.g2p_threads;
-  fast_g2p_advance(s->sd_dev, s->d_prefix + 4, 1, (long long)((s->n + chunk - 1) / chunk), chunk, st);
+void fast_enqueue_p2g(snow_scene* s, bool mass_only, cudaStream_t st) {
+  fast_p2g(s->sd_dev, s->d_prefix + 0, 1, item_ctas(), mass_only, st);
 }
+void fast_enqueue_grid(snow_scene* s, bool clear_only, cudaStream_t st) {
+  fast_grid(s->sd_dev, s->d_prefix + 2, 1, grid_ctas(), clear_only, st);
+}
+// One step of a scene whose P2G sums of the current state are pending in
+// acc: rigid advance, [binning], grid update, G2P + advance + next P2G.
 void fast_enqueue_step(snow_scene* s, bool bin, cudaStream_t st) {
-  if (s->ncoll > 0) fast_rigid(s->sd_dev, 1, nullptr, st);
-  fast_enqueue_p2g(s, bin, false, st);
-  fast_enqueue_grid(s, st);
-  fast_enqueue_g2p(s, st);
+  if (s->ncoll > 0) fast_rigid(s->sd_dev, 1, st);
+  if (bin) fast_bin(s, st);
+  fast_enqueue_compact(s, st);
+  fast_enqueue_grid(s, false, st);
+  fast_g2p2g(s->sd_dev, s->d_prefix + 0, 1, item_ctas(), st);
 }
 
 snow_status set_dt(snow_scene* s, float dt) {
@@ -304,7 +310,7 @@ snow_status set_dt(snow_scene* s, float dt) {
   return SNOW_OK;
 }
 
-// Checks device-side error counters; grows the block pool when it runs full.
+// Checks device-side error counters; grows the output pool when it runs full.
 snow_status fast_check(snow_scene* s) {
   snow_ctx* ctx = s->ctx;
   CK(cudaMemcpyAsync(ctx->h_counters, s->sd.counters, kCounterStride * sizeof(int), cudaMemcpyDeviceToHost,
@@ -313,6 +319,7 @@ snow_status fast_check(snow_scene* s) {
   const int active = ctx->h_counters[CNT_ACTIVE];
   const int overflow = ctx->h_counters[CNT_OVERFLOW];
   const int nonfinite = ctx->h_counters[CNT_NONFINITE];
+  if (ctx->h_counters[CNT_TIMEOUT] > 0) return fail(ctx, SNOW_ETIMEDOUT, "a bounded device wait ran out");
   if (overflow > 0) return fail(ctx, SNOW_ECAPACITY, "grid block pool overflowed");
   if (nonfinite > 0) return fail(ctx, SNOW_ENUMERIC, "non-finite particle state");
   if (active > (s->sd.pool_cap * 3) / 4 && s->sd.pool_cap < s->sd.nblocks) {
@@ -324,6 +331,9 @@ snow_status fast_check(snow_scene* s) {
   return SNOW_OK;
 }
 
+// ExplicitTimeUpdate::init (explicittimeupdate.cpp:29-33) -- grid mass and
+// particle volumes -- followed by the P2G of the initial state, which the
+// first step consumes.
 snow_status fast_init(snow_scene* s) {
   snow_ctx* ctx = s->ctx;
   cudaStream_t st = ctx->stream;
@@ -332,26 +342,26 @@ snow_status fast_init(snow_scene* s) {
   if ((r = fast_single_prefix(s))) return r;
   if ((r = push_sd(s))) return r;
   fast_bin(s, st);
-  // size the block pool from the blocks the particles touch now
-  const int chunk = s->tune.g2p_threads;
-  const long long chunks = (long long)((s->n + chunk - 1) / chunk);
-  fast_mark(s->sd_dev, s->d_prefix + 4, 1, chunks, st);
+  fast_enqueue_p2g(s, true, st);  // gMassCompute
+  // size the output pool from the blocks that received mass
   CK(cudaMemsetAsync(s->sd.counters + CNT_ACTIVE, 0, sizeof(int), st));
   fast_count_flags(s->sd_dev, s->sd.nblocks, st);
   CK(cudaMemcpyAsync(ctx->h_counters, s->sd.counters, kCounterStride * sizeof(int), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   const int touched = ctx->h_counters[CNT_ACTIVE];
   const int cap = std::min(s->sd.nblocks, std::max(2 * touched + 1024, 4096));
-  if ((r = fast_alloc_pool(s, cap))) return r;
-  if ((r = push_sd(s))) return r;
-  // gMassCompute + pVolumeCompute (explicittimeupdate.cpp:29-33)
-  fast_enqueue_p2g(s, false, true, st);
-  if (!s->volume_given) fast_volume(s->sd_dev, s->d_prefix + 4, 1, chunks, st);
-  fast_grid(s->sd_dev, s->d_prefix + 2, 1, grid_ctas(), true, st);  // clear the pool
-  fast_mark(s->sd_dev, s->d_prefix + 4, 1, chunks, st);             // blocks of step 1
+  if (cap != s->sd.pool_cap) {
+    if ((r = fast_alloc_pool(s, cap))) return r;
+    if ((r = push_sd(s))) return r;
+  }
+  fast_enqueue_compact(s, st);
+  if (!s->volume_given) fast_volume(s->sd_dev, (int)s->n, st);  // pVolumeCompute
+  fast_enqueue_grid(s, true, st);                                // clear acc
+  fast_enqueue_p2g(s, false, st);                                // P2G of step 1
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(st));
   s->steps_since_sort = 0;
+  s->p2g_ready = true;
   return SNOW_OK;
 }
 
@@ -747,18 +757,34 @@ snow_status snow_dispatch(snow_scene* s, int kernel, double dt) {
   if (r) return r;
   switch (kernel) {
     case SNOW_K_RIGID_ADVANCE:
-      if (s->ncoll > 0) fast_rigid(s->sd_dev, 1, nullptr, st);
+      if (s->ncoll > 0) fast_rigid(s->sd_dev, 1, st);
       break;
-    case SNOW_K_G_RESET: break;
-    case SNOW_K_P2G: {
-      const bool bin = s->steps_since_sort >= s->tune.sort_interval;
-      fast_enqueue_p2g(s, bin, false, st);
-      if (bin) s->steps_since_sort = 0;
+    case SNOW_K_G_RESET:  // discard pending P2G sums
+      if (s->p2g_ready) {
+        fast_enqueue_compact(s, st);
+        fast_enqueue_grid(s, true, st);
+        s->p2g_ready = false;
+      }
       break;
-    }
-    case SNOW_K_G_FORCE: fast_enqueue_grid(s, st); break;
+    case SNOW_K_P2G:
+      if (s->p2g_ready) {
+        fast_enqueue_compact(s, st);
+        fast_enqueue_grid(s, true, st);
+      }
+      if (s->steps_since_sort >= s->tune.sort_interval) {
+        fast_bin(s, st);
+        s->steps_since_sort = 0;
+      }
+      fast_enqueue_p2g(s, false, st);
+      s->p2g_ready = true;
+      break;
+    case SNOW_K_G_FORCE:
+      fast_enqueue_compact(s, st);
+      fast_enqueue_grid(s, false, st);
+      s->p2g_ready = false;
+      break;
     case SNOW_K_G2P:
-      fast_enqueue_g2p(s, st);
+      fast_g2p_advance(s->sd_dev, s->d_prefix + 0, 1, item_ctas(), st);
       s->steps_since_sort++;
       break;
     case SNOW_K_P_ADVANCE: break;
@@ -793,35 +819,38 @@ snow_status snow_scene_step(snow_scene* s, double dt, int n_steps) {
   }
   snow_status r = set_dt(s, fdt);
   if (r) return r;
+  if (!s->p2g_ready) {
+    // after per-kernel dispatches: bin and scatter the current state first
+    fast_bin(s, st);
+    s->steps_since_sort = 0;
+    fast_enqueue_p2g(s, false, st);
+    s->p2g_ready = true;
+  }
   for (int i = 0; i < n_steps; i++) {
     const bool bin = s->steps_since_sort >= s->tune.sort_interval;
     if (bin) {
       // binning points are where the host looks at the device counters
-      if (s->steps_since_sort < (1 << 30)) {
-        r = fast_check(s);
-        if (r) return r;
-      }
+      r = fast_check(s);
+      if (r) return r;
     }
     if (ctx->profiling) {
       cudaEvent_t* ev = ctx->ev;
       CK(cudaEventRecord(ev[0], st));
-      if (s->ncoll > 0) fast_rigid(s->sd_dev, 1, nullptr, st);
+      if (s->ncoll > 0) fast_rigid(s->sd_dev, 1, st);
       if (bin) fast_bin(s, st);
       CK(cudaEventRecord(ev[1], st));
-      fast_enqueue_p2g(s, false, false, st);
+      fast_enqueue_compact(s, st);
+      fast_enqueue_grid(s, false, st);
       CK(cudaEventRecord(ev[2], st));
-      fast_enqueue_grid(s, st);
+      fast_g2p2g(s->sd_dev, s->d_prefix + 0, 1, item_ctas(), st);
       CK(cudaEventRecord(ev[3], st));
-      fast_enqueue_g2p(s, st);
-      CK(cudaEventRecord(ev[4], st));
-      CK(cudaEventSynchronize(ev[4]));
-      float t[4];
-      for (int k = 0; k < 4; k++) cudaEventElapsedTime(&t[k], ev[k], ev[k + 1]);
+      CK(cudaEventSynchronize(ev[3]));
+      float t[3];
+      for (int k = 0; k < 3; k++) cudaEventElapsedTime(&t[k], ev[k], ev[k + 1]);
       s->times.sort_ms += t[0];
-      s->times.p2g_ms += t[1];
-      s->times.grid_ms += t[2];
-      s->times.g2p_ms += t[3];
-      s->times.total_ms += t[0] + t[1] + t[2] + t[3];
+      s->times.grid_ms += t[1];
+      s->times.g2p_ms += t[2];
+      s->times.total_ms += t[0] + t[1] + t[2];
       s->times.steps++;
     } else {
       cudaGraphExec_t& g = bin ? s->g_sort : s->g_plain;
@@ -972,7 +1001,7 @@ snow_status snow_scene_download_grid(snow_scene* s, float* mass, float* momentum
   cudaMemsetAsync(dp, 0, 3 * G * sizeof(float), ctx->stream);
   cudaMemsetAsync(df, 0, 3 * G * sizeof(float), ctx->stream);
   cudaMemsetAsync(dv, 0, 3 * G * sizeof(float), ctx->stream);
-  fast_download_grid(s->sd_dev, (long long)G, dm, dp, df, dv, ctx->stream);
+  fast_download_grid(s->sd_dev, dm, dp, df, dv, ctx->stream);
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
   if (e == cudaSuccess && mass) e = cudaMemcpy(mass, dm, G * sizeof(float), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess && momentum) e = cudaMemcpy(momentum, dp, 3 * G * sizeof(float), cudaMemcpyDeviceToHost);
@@ -1110,21 +1139,16 @@ snow_status batch_refresh(snow_batch* b, const double* dt) {
   if (!changed) return SNOW_OK;
   std::vector<SceneDev> sds(n);
   std::vector<int> pre(4 * (n + 1), 0);
-  long long chunks = 0, blocks = 0;
+  long long blocks = 0;
   for (int i = 0; i < n; i++) {
     snow_scene* s = b->scenes[i];
     s->sd.dt = want[i];
     s->last_dt = want[i];
     sds[i] = s->sd;
-    const int chunk = s->tune.g2p_threads;
-    pre[2 * (n + 1) + i] = (int)chunks;
     pre[3 * (n + 1) + i] = (int)blocks;
-    chunks += (long long)((s->n + chunk - 1) / chunk);
     blocks += s->sd.nblocks;
   }
-  pre[2 * (n + 1) + n] = (int)chunks;
   pre[3 * (n + 1) + n] = (int)blocks;
-  b->total_chunks = chunks;
   b->total_blocks = blocks;
   CK(cudaMemcpyAsync(b->d_scenes, sds.data(), sizeof(SceneDev) * n, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(b->d_prefix, pre.data(), sizeof(int) * pre.size(), cudaMemcpyHostToDevice, ctx->stream));
@@ -1148,20 +1172,16 @@ void batch_enqueue_step(snow_batch* b, int phase, int interval, cudaStream_t st)
   int* pre = b->d_prefix;
   int* items = pre;
   int* active = pre + (n + 1);
-  int* chunks = pre + 2 * (n + 1);
   int* blocks = pre + 3 * (n + 1);
-  fast_rigid(b->d_scenes, n, nullptr, st);
+  fast_rigid(b->d_scenes, n, st);
   // re-bin a staggered subset of scenes each step
   for (int i = 0; i < n; i++)
     if ((i % interval) == phase) fast_bin(b->scenes[i], st);
   fast_begin_step(b->d_scenes, n, st);
   fast_compact(b->d_scenes, blocks, n, b->total_blocks, st);
-  fast_prefix(b->d_scenes, n, CNT_ITEMS, items, st);
-  fast_prefix(b->d_scenes, n, CNT_ACTIVE, active, st);
-  const int threads = b->scenes[0]->tune.p2g_threads;
-  fast_p2g(b->d_scenes, items, n, num_sms() * (threads >= 256 ? 4 : 8), false, threads, st);
-  fast_grid(b->d_scenes, active, n, num_sms() * 8, false, st);
-  fast_g2p_advance(b->d_scenes, chunks, n, b->total_chunks, b->scenes[0]->tune.g2p_threads, st);
+  fast_prefix(b->d_scenes, n, items, active, st);
+  fast_grid(b->d_scenes, active, n, grid_ctas(), false, st);
+  fast_g2p2g(b->d_scenes, items, n, item_ctas(), st);
 }
 
 }  // namespace
@@ -1169,10 +1189,20 @@ void batch_enqueue_step(snow_batch* b, int phase, int interval, cudaStream_t st)
 snow_status snow_batch_step(snow_batch* b, const double* dt, int n_steps) {
   if (!b || n_steps < 0) return SNOW_EINVAL;
   snow_ctx* ctx = b->ctx;
+  cudaStream_t st = ctx->stream;
+  for (size_t i = 0; i < b->scenes.size(); i++) {
+    snow_scene* s = b->scenes[i];
+    if (s->p2g_ready) continue;  // left behind by per-kernel dispatches: scatter its state first
+    snow_status r0 = set_dt(s, dt ? (float)dt[i] : s->last_dt);
+    if (r0) return r0;
+    fast_bin(s, st);
+    s->steps_since_sort = 0;
+    fast_enqueue_p2g(s, false, st);
+    s->p2g_ready = true;
+  }
   snow_status r = batch_refresh(b, dt);
   if (r) return r;
   const int interval = std::max(1, b->scenes[0]->tune.sort_interval);
-  cudaStream_t st = ctx->stream;
   for (int i = 0; i < n_steps; i++) {
     const int phase = b->step_count % interval;
     if (phase == 0 && b->step_count > 0) {

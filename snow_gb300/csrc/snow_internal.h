@@ -59,6 +59,7 @@ enum {
   CNT_NONFINITE = 3,  // particles with a non-finite field (cumulative)
   CNT_HOME = 4,       // occupied home blocks at the last binning
   CNT_FALLBACK = 5,   // particles that left their P2G tile (diagnostic, cumulative)
+  CNT_TIMEOUT = 6,    // bounded waits that ran out (cumulative)
   kCounterStride = 8
 };
 
@@ -66,6 +67,7 @@ enum {
 struct SceneDev {
   float gpos[3];
   float h;
+  float inv_h;  // 1 / h (FAST kernels multiply instead of dividing)
   int dim[3];
   int bdim[3];
   int nblocks;
@@ -84,12 +86,12 @@ struct SceneDev {
   float4* fb;
   float2* fc;
   uint32_t* pid;    // upload index of the particle now stored at each slot
-  // sparse grid
-  int* blk_slot;    // nblocks: slot in the pool this step, -1 if inactive
-  int* blk_flag;    // nblocks: marked for the next step
+  // blocked grid
+  int* blk_slot;    // nblocks: pool slot of the block this step, -1 if inactive
+  int* blk_flag;    // nblocks: block received P2G sums since the last compaction
+  float* acc;       // nblocks x 448: P2G sums, field-major per block (dense)
   int* active;      // pool_cap: block id of each slot
-  float* acc;       // pool_cap x 448: P2G accumulators, field-major per block
-  float* gout;      // pool_cap x 384: grid-update output
+  float* gout;      // pool_cap x 384: grid-update output (v*, d)
   int pool_cap;
   // P2G work items: (home block, first particle, count, 0)
   int4* items;
@@ -98,33 +100,28 @@ struct SceneDev {
 };
 
 struct FastTuning {
-  int p2g_items_max = 256;     // particles per P2G work item
-  int p2g_threads = 256;
-  int g2p_threads = 128;
-  int sort_interval = 8;
+  int sort_interval = 8;  // re-bin particles every k steps
 };
 
-// Work spaces over a batch: prefix[s] .. prefix[s+1] are scene s's units.
-// For counts only known on the device (items, active blocks) the prefix is
-// computed on the device by fast_prefix().
-void fast_prefix(const SceneDev* scenes, int nscenes, int counter, int* prefix, cudaStream_t st);
-void fast_compact(const SceneDev* scenes, const int* block_prefix, int nscenes, long long total_blocks,
-                  cudaStream_t st);
-void fast_mark(const SceneDev* scenes, const int* chunk_prefix, int nscenes, long long total_chunks,
-               cudaStream_t st);
-void fast_p2g(const SceneDev* scenes, const int* item_prefix, int nscenes, int grid_ctas, bool mass_only,
-              int threads, cudaStream_t st);
-void fast_grid(const SceneDev* scenes, const int* active_prefix, int nscenes, int grid_ctas, bool clear_only,
-               cudaStream_t st);
-void fast_volume(const SceneDev* scenes, const int* chunk_prefix, int nscenes, long long total_chunks,
-                 cudaStream_t st);
-void fast_g2p_advance(const SceneDev* scenes, const int* chunk_prefix, int nscenes, long long total_chunks,
-                      int threads, cudaStream_t st);
-void fast_rigid(const SceneDev* scenes, int nscenes, const snow_collider* dummy, cudaStream_t st);
+// Work spaces over a batch: prefix[s] .. prefix[s+1] are scene s's units
+// (P2G work items, active blocks, grid blocks). Item and active-block counts
+// are only known on the device; fast_prefix() forms both prefixes there.
+int fast_item_threads();
+void fast_prefix(const SceneDev* scenes, int nscenes, int* items_prefix, int* active_prefix, cudaStream_t st);
 // Zeroes the per-step counters (active blocks, overflow) of every scene.
 void fast_begin_step(const SceneDev* scenes, int nscenes, cudaStream_t st);
 // Counts flagged blocks of one scene into counters[CNT_ACTIVE] (pool sizing).
 void fast_count_flags(const SceneDev* sd_dev, int nblocks, cudaStream_t st);
+void fast_compact(const SceneDev* scenes, const int* block_prefix, int nscenes, long long total_blocks,
+                  cudaStream_t st);
+void fast_p2g(const SceneDev* scenes, const int* item_prefix, int nscenes, int grid_ctas, bool mass_only,
+              cudaStream_t st);
+void fast_grid(const SceneDev* scenes, const int* active_prefix, int nscenes, int grid_ctas, bool clear_only,
+               cudaStream_t st);
+void fast_volume(const SceneDev* sd_dev, int n, cudaStream_t st);
+void fast_g2p_advance(const SceneDev* scenes, const int* item_prefix, int nscenes, int grid_ctas, cudaStream_t st);
+void fast_g2p2g(const SceneDev* scenes, const int* item_prefix, int nscenes, int grid_ctas, cudaStream_t st);
+void fast_rigid(const SceneDev* scenes, int nscenes, cudaStream_t st);
 
 // Binning of one scene (host-side sizes known): keys -> radix sort ->
 // permutation of the particle streams -> P2G work items.
@@ -160,8 +157,7 @@ struct StatsAccum {
 };
 void fast_stats(const SceneDev* sd_dev, int n, StatsAccum* out_dev, cudaStream_t st);
 void ref_stats(const RefArgs& a, StatsAccum* out_dev, cudaStream_t st);
-void fast_download_grid(const SceneDev* sd_dev, long long G, float* mass, float* mom, float* force, float* vstar,
-                        cudaStream_t st);
+void fast_download_grid(const SceneDev* sd_dev, float* mass, float* mom, float* force, float* vstar, cudaStream_t st);
 
 int num_sms();
 

@@ -151,7 +151,7 @@ __device__ __forceinline__ void jacobi_step(M3& S, float q[4]) {
   sh = exact ? w * sh : SNOW_SVD_SSTAR;
   ch2 = ch * ch;
   sh2 = sh * sh;
-  const float scale = 1.0f / (ch2 + sh2);
+  const float scale = FAITHFUL ? 1.0f / (ch2 + sh2) : __fdividef(1.0f, ch2 + sh2);
   const float a = (ch2 - sh2) * scale;
   const float b = (2.0f * sh * ch) * scale;
   const float a2 = a * a, b2 = b * b, ab = a * b;

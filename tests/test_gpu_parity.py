@@ -185,9 +185,14 @@ def test_fast_grid_after_p2g_and_grid_update(ctx):
     assert np.abs(gd["force"] - od["force"]).max() <= 1e-4 * fscale, (np.abs(gd["force"] - od["force"]).max(), fscale)
     g.dispatch(N.K_G_FORCE, s2.dt)
     o.phase(O.PH_GRID)
+    # v* = p/m + dt (f/m + g): at the stencil's edge nodes m_i ~ 1e-7 m_p
+    # while f_i is not small, so v* there divides the force's FP32 rounding by
+    # a tiny mass. Those nodes carry ~1e-7 of a particle's weight; v* is
+    # compared where the node holds >= 1e-3 of the peak node mass.
     vs = o.grid()["vstar"]
-    vscale = np.abs(vs).max()
-    assert np.abs(g.grid()["vstar"] - vs).max() <= REL_TOL * vscale
+    heavy = od["mass"] >= 1e-3 * mscale
+    vscale = np.abs(vs[heavy]).max()
+    assert np.abs(g.grid()["vstar"][heavy] - vs[heavy]).max() <= REL_TOL * vscale
 
 
 @gpu
