@@ -195,6 +195,38 @@ snow_status snow_scene_cell_keys(snow_scene* s, uint32_t* keys, uint32_t* perm);
 
 snow_status snow_scene_phase_times(snow_scene* s, snow_phase_times* out, int reset);
 
+/* Largest key count snow_sort_keys_static accepts. */
+#define SNOW_SORT_STATIC_MAX_KEYS 262144
+
+/* The binning sort without any device allocation. (No counterpart in the
+ * reference, which has no sort.)
+ *
+ * For callers that cannot allocate device memory: an application that owns
+ * every device buffer up front (for example particle buffers it shares with
+ * its renderer) and does not let a plug-in call cudaMalloc, which can
+ * synchronise the device and stall a real-time frame loop, or code running
+ * under an external memory budget. Everything else in this library allocates
+ * through its context; this call needs no context.
+ *
+ * Sorts n 32-bit keys (device memory, `key_bits` significant low bits,
+ * 1..32) stably: sorted_keys receives the keys in ascending order and perm[i]
+ * the input index of the i-th smallest key (ties keep input order, as
+ * std::stable_sort). `keys` may alias `sorted_keys`. The work is queued on
+ * `stream` (a cudaStream_t; NULL = the default stream) and the call returns
+ * without waiting.
+ *
+ * Scratch lives in one fixed device array inside the library, sized for
+ * SNOW_SORT_STATIC_MAX_KEYS keys (about 2.1 MB, held by every GPU that loads
+ * the library until the process exits). n above that limit returns
+ * SNOW_EINVAL and queues nothing. All calls share the array, so calls whose
+ * work overlaps on the GPU (other streams, other host threads) race and must
+ * be ordered by the caller; every pass overwrites the scratch it reads, so
+ * nothing carried over from an earlier call needs clearing. The first call on
+ * a device looks up the array's device address; make that first call before
+ * any stream capture. Returns SNOW_ECUDA if a CUDA call fails. */
+snow_status snow_sort_keys_static(const uint32_t* keys, uint32_t* sorted_keys, uint32_t* perm, size_t n,
+                                  int key_bits, void* stream);
+
 /* Batched stepping of many independent scenes (all SNOW_MODE_FAST): one
  * launch per phase covers every scene, the whole step is a CUDA graph. */
 snow_status snow_batch_create(snow_ctx* ctx, snow_scene* const* scenes, int n, snow_batch** out);

@@ -15,6 +15,8 @@
 // digit-major), an exclusive scan of the histograms and a downsweep that ranks
 // each tile's keys stably with warp match/ballot and per-warp digit counters,
 // then scatters.
+#include <mutex>
+
 #include "snow_internal.h"
 
 namespace snow {
@@ -303,3 +305,78 @@ void fast_apply_bins(const SceneDev& sd, const SceneDev* sd_dev, BinScratch& b, 
 }
 
 }  // namespace snow
+
+// ---------------------------------------------------------------------------
+// snow_sort_keys_static: the stable radix sort above for callers that cannot
+// allocate device memory. Its scratch (the second key/value buffer of the
+// ping-pong passes, the digit histograms and the scan partials) lives in one
+// file-scope __device__ array, sized for SNOW_SORT_STATIC_MAX_KEYS keys; every
+// GPU that loads the library holds it (about 2.1 MB) until the process exits.
+// ---------------------------------------------------------------------------
+namespace snow {
+namespace {
+
+constexpr size_t kStaticKeys = SNOW_SORT_STATIC_MAX_KEYS;
+constexpr size_t kStaticTiles = (kStaticKeys + kRsTile - 1) / kRsTile;
+constexpr size_t kStaticHist = 256 * kStaticTiles;
+constexpr size_t kStaticPartials = (kStaticHist + kScanChunk - 1) / kScanChunk + 1;
+// layout: [keys kStaticKeys][vals kStaticKeys][hist kStaticHist][partials]
+constexpr size_t kStaticWords = 2 * kStaticKeys + kStaticHist + kStaticPartials;
+
+__device__ __align__(256) uint32_t g_sort_scratch[kStaticWords];
+
+__global__ void k_iota(uint32_t* __restrict__ v, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    v[i] = (uint32_t)i;
+}
+
+// Device address of g_sort_scratch on the current device. Host code only sees
+// a host-side stand-in for the symbol, so the address is looked up once per
+// device (cudaGetSymbolAddress) and cached.
+cudaError_t static_scratch(uint32_t** out) {
+  static std::mutex mu;
+  static uint32_t* addr[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_sort_scratch);
+    if (e != cudaSuccess) return e;
+    addr[dev] = static_cast<uint32_t*>(p);
+  }
+  *out = addr[dev];
+  return cudaSuccess;
+}
+
+}  // namespace
+}  // namespace snow
+
+extern "C" snow_status snow_sort_keys_static(const uint32_t* keys, uint32_t* sorted_keys, uint32_t* perm, size_t n,
+                                             int key_bits, void* stream) {
+  using namespace snow;
+  if (!keys || !sorted_keys || !perm || key_bits < 1 || key_bits > 32) return SNOW_EINVAL;
+  if (n > kStaticKeys) return SNOW_EINVAL;
+  if (n == 0) return SNOW_OK;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  uint32_t* scratch = nullptr;
+  if (static_scratch(&scratch) != cudaSuccess) {
+    cudaGetLastError();
+    return SNOW_ECUDA;
+  }
+  uint32_t* k[2] = {sorted_keys, scratch};
+  uint32_t* v[2] = {perm, scratch + kStaticKeys};
+  uint32_t* hist = scratch + 2 * kStaticKeys;
+  uint32_t* partials = hist + kStaticHist;
+  if (sorted_keys != keys &&
+      cudaMemcpyAsync(sorted_keys, keys, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st) != cudaSuccess) {
+    cudaGetLastError();
+    return SNOW_ECUDA;
+  }
+  k_iota<<<grid_for(n, 256, 4), 256, 0, st>>>(perm, n);
+  radix_sort_pairs(k, v, n, key_bits, hist, partials, st);
+  if (cudaGetLastError() != cudaSuccess) return SNOW_ECUDA;
+  return SNOW_OK;
+}

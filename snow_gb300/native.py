@@ -27,8 +27,9 @@ EXPORTS = [
     "snow_scene_set_volume", "snow_scene_init", "snow_scene_step", "snow_dispatch", "snow_scene_download", "snow_scene_download_std140",
     "snow_scene_download_grid", "snow_scene_download_colliders", "snow_scene_stats", "snow_scene_size",
     "snow_scene_cell_keys", "snow_scene_phase_times", "snow_batch_create", "snow_batch_destroy",
-    "snow_batch_step", "snow_batch_autotune",
+    "snow_batch_step", "snow_batch_autotune", "snow_sort_keys_static",
 ]
+SORT_STATIC_MAX_KEYS = 262144  # SNOW_SORT_STATIC_MAX_KEYS
 
 
 class SnowParams(C.Structure):
@@ -111,6 +112,7 @@ def load(path: str = LIB_PATH):
     L.snow_batch_destroy.restype = None
     L.snow_batch_step.argtypes = [vp, C.POINTER(C.c_double), C.c_int]
     L.snow_batch_autotune.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_int)]
+    L.snow_sort_keys_static.argtypes = [vp, vp, vp, sz, C.c_int, vp]
     _lib = L
     return L
 
