@@ -323,7 +323,7 @@ def main():
         line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * args.particles / r["value"], "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32+i32", "data": "synthetic",
-                "config": workload_config(args), "impl": "reference",
+                "config": dict(workload_config(args), mode="the reference compute shaders compiled as C++ (FP32 + int32 fixed point)", l2="n/a (host)"), "impl": "reference",
                 "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": r["cores"], "kind": r["kind"],
                                  "sample": r["sample"]},
                 "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
