@@ -146,7 +146,8 @@ snow_status snow_scene_create(snow_ctx* ctx, const snow_params* p, const snow_co
                               int n_colliders, size_t capacity, snow_scene** out);
 /* Also destroys the batches that hold this scene. */
 void snow_scene_destroy(snow_scene* s);
-/* Device bytes a scene with these parameters and n particles will hold. */
+/* Device bytes a scene with these parameters and n particles will hold at
+ * most (in SNOW_MODE_FAST the output pool counted at its largest). */
 size_t snow_scene_footprint(const snow_params* p, size_t n);
 
 /* x, v: N x 3; m: N; FE, FP: N x 9 row-major or NULL for identity. */
@@ -194,6 +195,72 @@ size_t snow_scene_size(const snow_scene* s);
 snow_status snow_scene_cell_keys(snow_scene* s, uint32_t* keys, uint32_t* perm);
 
 snow_status snow_scene_phase_times(snow_scene* s, snow_phase_times* out, int reset);
+
+/* ---- Serving ---------------------------------------------------------------
+ * A worker thread that owns one context and runs simulation jobs: it admits
+ * queued jobs in arrival order while their device footprint fits the HBM
+ * budget, keeps every admitted job's state resident, and advances all
+ * admitted jobs together as one batch (snow_batch_step) in chunks of steps;
+ * jobs that arrive meanwhile join at the next chunk boundary and finished jobs
+ * leave, freeing their memory. (No counterpart in the reference, which runs
+ * one scene per process.) */
+typedef struct snow_server snow_server;
+
+typedef struct snow_server_config {
+  int device;
+  size_t hbm_budget_bytes;  /* admission limit for resident jobs (0 = no limit) */
+  int max_active;           /* most jobs advanced together (0 = 256) */
+  int chunk_steps;          /* steps per batch launch between admissions (0 = 16) */
+} snow_server_config;
+
+typedef struct snow_job_desc {
+  const snow_params* params;  /* mode is forced to SNOW_MODE_FAST */
+  const snow_collider* colliders;
+  int n_colliders;
+  const float* x; /* N x 3 */
+  const float* v; /* N x 3 */
+  const float* m; /* N */
+  size_t n;
+  int steps;
+  double dt;
+  int keep_state; /* keep the final state for snow_server_fetch */
+} snow_job_desc;
+
+typedef struct snow_job_result {
+  uint64_t id;
+  int status;          /* snow_status of the job */
+  size_t n;
+  int steps;
+  double queue_s;      /* arrival -> admission */
+  double service_s;    /* admission -> completion */
+  double latency_s;    /* arrival -> completion */
+  snow_stats stats;    /* bulk statistics of the final state */
+} snow_job_result;
+
+typedef struct snow_server_report {
+  uint64_t submitted, admitted, completed, failed;
+  uint64_t pending, active;
+  double particle_steps;  /* completed particle-steps of all jobs */
+  double busy_s;          /* time with at least one admitted job */
+  double uptime_s;
+  size_t resident_bytes;
+} snow_server_report;
+
+snow_status snow_server_create(const snow_server_config* cfg, snow_server** out);
+/* Stops the worker after the jobs already admitted finish; pending jobs are
+ * dropped. */
+void snow_server_destroy(snow_server* srv);
+/* Copies the job's host arrays; returns at once with the job id. */
+snow_status snow_server_submit(snow_server* srv, const snow_job_desc* job, uint64_t* id);
+/* Moves up to max finished jobs into out; *n_out = how many. */
+snow_status snow_server_poll(snow_server* srv, snow_job_result* out, int max, int* n_out);
+/* Final state of a finished job submitted with keep_state (x, v: N x 3, FE:
+ * N x 9 row-major, Jp: N; any may be NULL); releases it. */
+snow_status snow_server_fetch(snow_server* srv, uint64_t id, float* x, float* v, float* FE, float* Jp);
+snow_status snow_server_stats(snow_server* srv, snow_server_report* out);
+/* Blocks until no job is pending or active, or timeout_s passes
+ * (SNOW_ETIMEDOUT). */
+snow_status snow_server_drain(snow_server* srv, double timeout_s);
 
 /* Largest key count snow_sort_keys_static accepts. */
 #define SNOW_SORT_STATIC_MAX_KEYS 262144

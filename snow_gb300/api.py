@@ -195,9 +195,7 @@ class SimScene:
     def stats(self) -> dict:
         s = N.SnowStats()
         self.ctx.check(self.L.snow_scene_stats(self.h, C.byref(s)))
-        return dict(mass=s.mass, momentum=np.array(s.momentum[:]), kinetic_energy=s.kinetic_energy,
-                    center_of_mass=np.array(s.center_of_mass[:]), bbox_min=np.array(s.bbox_min[:]),
-                    bbox_max=np.array(s.bbox_max[:]), mean_jp=s.mean_jp, nonfinite=int(s.nonfinite), n=int(s.n))
+        return _stats_dict(s)
 
     def cell_keys(self):
         n = self.n
@@ -236,6 +234,89 @@ class Batch:
         if getattr(self, "h", None) and alive:
             self.L.snow_batch_destroy(self.h)
         self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _stats_dict(s: N.SnowStats) -> dict:
+    return dict(mass=s.mass, momentum=np.array(s.momentum[:]), kinetic_energy=s.kinetic_energy,
+                center_of_mass=np.array(s.center_of_mass[:]), bbox_min=np.array(s.bbox_min[:]),
+                bbox_max=np.array(s.bbox_max[:]), mean_jp=s.mean_jp, nonfinite=int(s.nonfinite), n=int(s.n))
+
+
+class Server:
+    """Continuous-batching simulation server (snow_server_* in the C ABI): a
+    native worker thread admits submitted jobs while their device footprint
+    fits the HBM budget and advances all admitted jobs together, chunk by
+    chunk; jobs join and leave at chunk boundaries."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0, max_active: int = 0, chunk_steps: int = 0):
+        self.L = N.load()
+        cfg = N.SnowServerConfig(int(device), int(hbm_budget), int(max_active), int(chunk_steps))
+        h = C.c_void_p()
+        st = self.L.snow_server_create(C.byref(cfg), C.byref(h))
+        if st != N.SNOW_OK:
+            raise N.SnowError(st, "snow_server_create failed")
+        self.h = h
+
+    def submit(self, scene: Scene, steps: Optional[int] = None, dt: Optional[float] = None,
+               keep_state: bool = False, sort_interval: int = 0) -> int:
+        """Queues a job (FAST mode); returns its id. The arrays are copied."""
+        p = params_for(scene, N.MODE_FAST, sort_interval)
+        coll, nc = colliders_for(scene)
+        x = np.ascontiguousarray(scene.x, dtype=np.float32)
+        v = np.ascontiguousarray(scene.v, dtype=np.float32)
+        m = np.ascontiguousarray(scene.m, dtype=np.float32)
+        d = N.SnowJobDesc(C.pointer(p), C.cast(coll, C.POINTER(N.SnowCollider)), nc, N.ptr(x), N.ptr(v), N.ptr(m), len(m),
+                          int(steps if steps is not None else scene.steps),
+                          float(dt if dt is not None else scene.dt), int(bool(keep_state)))
+        jid = C.c_uint64()
+        st = self.L.snow_server_submit(self.h, C.byref(d), C.byref(jid))
+        if st != N.SNOW_OK:
+            raise N.SnowError(st, "snow_server_submit failed")
+        return int(jid.value)
+
+    def poll(self, max_results: int = 256) -> List[dict]:
+        out = (N.SnowJobResult * max_results)()
+        n = C.c_int()
+        st = self.L.snow_server_poll(self.h, out, max_results, C.byref(n))
+        if st != N.SNOW_OK:
+            raise N.SnowError(st, "snow_server_poll failed")
+        return [dict(id=int(r.id), status=int(r.status), n=int(r.n), steps=int(r.steps), queue_s=r.queue_s,
+                     service_s=r.service_s, latency_s=r.latency_s, stats=_stats_dict(r.stats))
+                for r in out[:n.value]]
+
+    def fetch(self, job_id: int, n: int) -> dict:
+        """Final state of a finished job submitted with keep_state."""
+        x = np.empty((n, 3), np.float32)
+        v = np.empty((n, 3), np.float32)
+        fe = np.empty((n, 3, 3), np.float32)
+        jp = np.empty(n, np.float32)
+        st = self.L.snow_server_fetch(self.h, int(job_id), N.ptr(x), N.ptr(v), N.ptr(fe), N.ptr(jp))
+        if st != N.SNOW_OK:
+            raise N.SnowError(st, "snow_server_fetch failed")
+        return dict(x=x, v=v, FE=fe, Jp=jp)
+
+    def stats(self) -> dict:
+        r = N.SnowServerStats()
+        st = self.L.snow_server_stats(self.h, C.byref(r))
+        if st != N.SNOW_OK:
+            raise N.SnowError(st, "snow_server_stats failed")
+        return {k: getattr(r, k) for k, _ in N.SnowServerStats._fields_}
+
+    def drain(self, timeout_s: float = 600.0):
+        st = self.L.snow_server_drain(self.h, float(timeout_s))
+        if st != N.SNOW_OK:
+            raise N.SnowError(st, "snow_server_drain: jobs still running")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.snow_server_destroy(self.h)
+            self.h = None
 
     def __del__(self):
         try:

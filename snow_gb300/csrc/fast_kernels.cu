@@ -26,6 +26,7 @@
 // per-kernel dispatch entry point.
 #include "snow_internal.h"
 #include "snow_math.cuh"
+#include "snow_stats.cuh"
 #include "snow_tma.cuh"
 
 namespace snow {
@@ -895,68 +896,40 @@ __global__ void k_rigid(const SceneDev* __restrict__ scenes, int nscenes) {  // 
     for (int k = 0; k < 3; k++) S.coll[i].pos[k] = S.coll[i].pos[k] + S.dt * S.coll[i].vel[k];
 }
 
-// Monotone map float -> int: a < b  <=>  key(a) < key(b) (finite values).
-__device__ __forceinline__ int float_order_key(float f) {
-  const int i = __float_as_int(f);
-  return i >= 0 ? i : i ^ 0x7fffffff;
-}
-
-// Bulk statistics (double accumulation).
+// Bulk statistics: per-thread sums in FP32 over a dozen particles, then FP64
+// across threads (FP64 arithmetic is slow on this part: the per-particle work
+// stays in FP32).
 __global__ void __launch_bounds__(256) k_stats(const SceneDev* __restrict__ sd, int n, StatsAccum* out) {
   const SceneDev& S = *sd;
-  double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-  float bmin[3] = {3.4e38f, 3.4e38f, 3.4e38f}, bmax[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
-  unsigned long long bad = 0;
+  float acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  StatsPartial t;
+  stats_init(t);
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
     const float4 xm = S.xm[p];
     const float4 vv = S.vv[p];
     const float jp = S.fc[p].y;
-    const double m = xm.w;
+    const float m = xm.w;
     const bool ok = isfinite(xm.x) && isfinite(xm.y) && isfinite(xm.z) && isfinite(vv.x) && isfinite(vv.y) &&
                     isfinite(vv.z) && isfinite(jp);
     if (!ok) {
-      bad++;
+      t.bad++;
       continue;
     }
     acc[0] += m;
     acc[1] += m * vv.x;
     acc[2] += m * vv.y;
     acc[3] += m * vv.z;
-    acc[4] += 0.5 * m * ((double)vv.x * vv.x + (double)vv.y * vv.y + (double)vv.z * vv.z);
+    acc[4] += 0.5f * m * (vv.x * vv.x + vv.y * vv.y + vv.z * vv.z);
     acc[5] += m * xm.x;
     acc[6] += m * xm.y;
     acc[7] += m * xm.z;
     acc[8] += jp;
-    bmin[0] = fminf(bmin[0], xm.x); bmin[1] = fminf(bmin[1], xm.y); bmin[2] = fminf(bmin[2], xm.z);
-    bmax[0] = fmaxf(bmax[0], xm.x); bmax[1] = fmaxf(bmax[1], xm.y); bmax[2] = fmaxf(bmax[2], xm.z);
+    t.bmin[0] = fminf(t.bmin[0], xm.x); t.bmin[1] = fminf(t.bmin[1], xm.y); t.bmin[2] = fminf(t.bmin[2], xm.z);
+    t.bmax[0] = fmaxf(t.bmax[0], xm.x); t.bmax[1] = fmaxf(t.bmax[1], xm.y); t.bmax[2] = fmaxf(t.bmax[2], xm.z);
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-#pragma unroll
-    for (int k = 0; k < 9; k++) acc[k] += __shfl_down_sync(0xffffffffu, acc[k], o);
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      bmin[k] = fminf(bmin[k], __shfl_down_sync(0xffffffffu, bmin[k], o));
-      bmax[k] = fmaxf(bmax[k], __shfl_down_sync(0xffffffffu, bmax[k], o));
-    }
-    bad += __shfl_down_sync(0xffffffffu, bad, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    atomicAdd(&out->mass, acc[0]);
-    atomicAdd(&out->mom[0], acc[1]);
-    atomicAdd(&out->mom[1], acc[2]);
-    atomicAdd(&out->mom[2], acc[3]);
-    atomicAdd(&out->ke, acc[4]);
-    atomicAdd(&out->com[0], acc[5]);
-    atomicAdd(&out->com[1], acc[6]);
-    atomicAdd(&out->com[2], acc[7]);
-    atomicAdd(&out->jp, acc[8]);
-    atomicAdd(&out->nonfinite, bad);
-    for (int k = 0; k < 3; k++) {
-      atomicMin(&out->bmin_key[k], float_order_key(bmin[k]));
-      atomicMax(&out->bmax_key[k], float_order_key(bmax[k]));
-    }
-  }
+  for (int k = 0; k < 9; k++) t.acc[k] = acc[k];
+  stats_commit(t, out);
 }
 
 // Dense copies of the P2G sums (acc) and of v* (pool) of the active blocks.
@@ -1082,7 +1055,7 @@ void fast_rigid(const SceneDev* scenes, int nscenes, cudaStream_t st) {
 void fast_stats(const SceneDev* sd_dev, int n, StatsAccum* out_dev, cudaStream_t st) {
   if (n <= 0) return;
   int g = (n + 255) / 256;
-  if (g > num_sms() * 8) g = num_sms() * 8;
+  if (g > num_sms() * 2) g = num_sms() * 2;
   k_stats<<<g, 256, 0, st>>>(sd_dev, n, out_dev);
 }
 

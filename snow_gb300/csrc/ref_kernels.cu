@@ -14,6 +14,7 @@
 //     have no bounds check and run past the grid's end).
 #include "snow_internal.h"
 #include "snow_math.cuh"
+#include "snow_stats.cuh"
 
 namespace snow {
 namespace {
@@ -314,57 +315,32 @@ __global__ void __launch_bounds__(kThreads) k_advance(RefArgs a, float dt) {
   }
 }
 
-__device__ __forceinline__ int order_key(float f) {
-  const int i = __float_as_int(f);
-  return i >= 0 ? i : i ^ 0x7fffffff;
-}
-
 __global__ void __launch_bounds__(kThreads) k_stats(RefArgs a, StatsAccum* out) {
-  double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-  float bmin[3] = {3.4e38f, 3.4e38f, 3.4e38f}, bmax[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
-  unsigned long long bad = 0;
+  StatsPartial t;
+  stats_init(t);
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += gridDim.x * blockDim.x) {
     const float4 xm = a.pxm[p];
     const int4 pv = a.pv[p];
     const double v[3] = {pv.x * 1e-8, pv.y * 1e-8, pv.z * 1e-8};
     const float jp = m3_det(load_mat4(a.pfp + 4 * (size_t)p));
     if (!(isfinite(xm.x) && isfinite(xm.y) && isfinite(xm.z) && isfinite(jp))) {
-      bad++;
+      t.bad++;
       continue;
     }
     const double m = xm.w;
-    acc[0] += m;
-    acc[1] += m * v[0];
-    acc[2] += m * v[1];
-    acc[3] += m * v[2];
-    acc[4] += 0.5 * m * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
-    acc[5] += m * xm.x;
-    acc[6] += m * xm.y;
-    acc[7] += m * xm.z;
-    acc[8] += jp;
-    bmin[0] = fminf(bmin[0], xm.x); bmin[1] = fminf(bmin[1], xm.y); bmin[2] = fminf(bmin[2], xm.z);
-    bmax[0] = fmaxf(bmax[0], xm.x); bmax[1] = fmaxf(bmax[1], xm.y); bmax[2] = fmaxf(bmax[2], xm.z);
+    t.acc[0] += m;
+    t.acc[1] += m * v[0];
+    t.acc[2] += m * v[1];
+    t.acc[3] += m * v[2];
+    t.acc[4] += 0.5 * m * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    t.acc[5] += m * xm.x;
+    t.acc[6] += m * xm.y;
+    t.acc[7] += m * xm.z;
+    t.acc[8] += jp;
+    t.bmin[0] = fminf(t.bmin[0], xm.x); t.bmin[1] = fminf(t.bmin[1], xm.y); t.bmin[2] = fminf(t.bmin[2], xm.z);
+    t.bmax[0] = fmaxf(t.bmax[0], xm.x); t.bmax[1] = fmaxf(t.bmax[1], xm.y); t.bmax[2] = fmaxf(t.bmax[2], xm.z);
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    for (int k = 0; k < 9; k++) acc[k] += __shfl_down_sync(0xffffffffu, acc[k], o);
-    for (int k = 0; k < 3; k++) {
-      bmin[k] = fminf(bmin[k], __shfl_down_sync(0xffffffffu, bmin[k], o));
-      bmax[k] = fmaxf(bmax[k], __shfl_down_sync(0xffffffffu, bmax[k], o));
-    }
-    bad += __shfl_down_sync(0xffffffffu, bad, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    atomicAdd(&out->mass, acc[0]);
-    for (int k = 0; k < 3; k++) atomicAdd(&out->mom[k], acc[1 + k]);
-    atomicAdd(&out->ke, acc[4]);
-    for (int k = 0; k < 3; k++) atomicAdd(&out->com[k], acc[5 + k]);
-    atomicAdd(&out->jp, acc[8]);
-    atomicAdd(&out->nonfinite, bad);
-    for (int k = 0; k < 3; k++) {
-      atomicMin(&out->bmin_key[k], order_key(bmin[k]));
-      atomicMax(&out->bmax_key[k], order_key(bmax[k]));
-    }
-  }
+  stats_commit(t, out);
 }
 
 int grid_for(long long n) {

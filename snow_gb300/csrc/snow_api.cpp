@@ -533,9 +533,15 @@ size_t snow_scene_footprint(const snow_params* p, size_t n) {
   const double G = (double)p->grid_dim[0] * p->grid_dim[1] * p->grid_dim[2];
   if (p->mode == SNOW_MODE_REFERENCE) return (size_t)(n * (16.0 * 6 + 128.0) + G * 48.0);
   const double nb = (double)((p->grid_dim[0] + 3) / 4) * ((p->grid_dim[1] + 3) / 4) * ((p->grid_dim[2] + 3) / 4);
-  // particle streams + binning scratch + block tables + an initial pool estimate
-  const double pool = std::min(nb, 2.0 * (double)n / 64.0 * 4.0 + 4096.0);
-  return (size_t)(n * (76.0 + 4.0 * 4 + 76.0 + 4.0 / 256 * 256 + 24) + nb * 20.0 + pool * (448 + 384 + 4) * 4.0);
+  // An upper bound: particle streams (xm, vv, fa, fb: 16 B, fc: 8 B, pid: 4 B)
+  // + binning scratch (2 key + 2 value words, 4 x 16 B + 8 B + 4 B permutation
+  // targets, radix histograms) + work items (16 B each) + per block the dense
+  // P2G sums (448 floats), flags, slot and bin tables (5 ints) + the output
+  // pool at its largest (every block: 384 floats + 1 int).
+  const double tiles = (double)radix_tiles(n);
+  const double items = (double)n / fast_item_threads() + std::min((double)n, nb) + 1;
+  return (size_t)(n * (76.0 + 92.0) + tiles * 256 * 4.0 + 4096.0 + items * 16.0 + nb * (448 * 4.0 + 5 * 4.0) +
+                  nb * (384 * 4.0 + 4.0) + 1024.0);
 }
 
 snow_status snow_scene_create(snow_ctx* ctx, const snow_params* p, const snow_collider* colliders, int n_colliders,

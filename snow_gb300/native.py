@@ -27,7 +27,8 @@ EXPORTS = [
     "snow_scene_set_volume", "snow_scene_init", "snow_scene_step", "snow_dispatch", "snow_scene_download", "snow_scene_download_std140",
     "snow_scene_download_grid", "snow_scene_download_colliders", "snow_scene_stats", "snow_scene_size",
     "snow_scene_cell_keys", "snow_scene_phase_times", "snow_batch_create", "snow_batch_destroy",
-    "snow_batch_step", "snow_batch_autotune", "snow_sort_keys_static",
+    "snow_batch_step", "snow_batch_autotune", "snow_sort_keys_static", "snow_server_create", "snow_server_destroy",
+    "snow_server_submit", "snow_server_poll", "snow_server_fetch", "snow_server_stats", "snow_server_drain",
 ]
 SORT_STATIC_MAX_KEYS = 262144  # SNOW_SORT_STATIC_MAX_KEYS
 
@@ -53,6 +54,31 @@ class SnowStats(C.Structure):
 class SnowPhaseTimes(C.Structure):
     _fields_ = [("sort_ms", C.c_double), ("p2g_ms", C.c_double), ("grid_ms", C.c_double), ("g2p_ms", C.c_double),
                 ("other_ms", C.c_double), ("total_ms", C.c_double), ("steps", C.c_uint64)]
+
+
+class SnowServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int), ("hbm_budget_bytes", C.c_size_t), ("max_active", C.c_int),
+                ("chunk_steps", C.c_int)]
+
+
+class SnowJobDesc(C.Structure):
+    _fields_ = [("params", C.POINTER(SnowParams)), ("colliders", C.POINTER(SnowCollider)),
+                ("n_colliders", C.c_int), ("x", C.POINTER(C.c_float)), ("v", C.POINTER(C.c_float)),
+                ("m", C.POINTER(C.c_float)), ("n", C.c_size_t), ("steps", C.c_int), ("dt", C.c_double),
+                ("keep_state", C.c_int)]
+
+
+class SnowJobResult(C.Structure):
+    _fields_ = [("id", C.c_uint64), ("status", C.c_int), ("n", C.c_size_t), ("steps", C.c_int),
+                ("queue_s", C.c_double), ("service_s", C.c_double), ("latency_s", C.c_double),
+                ("stats", SnowStats)]
+
+
+class SnowServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("admitted", C.c_uint64), ("completed", C.c_uint64),
+                ("failed", C.c_uint64), ("pending", C.c_uint64), ("active", C.c_uint64),
+                ("particle_steps", C.c_double), ("busy_s", C.c_double), ("uptime_s", C.c_double),
+                ("resident_bytes", C.c_size_t)]
 
 
 class SnowError(RuntimeError):
@@ -113,6 +139,14 @@ def load(path: str = LIB_PATH):
     L.snow_batch_step.argtypes = [vp, C.POINTER(C.c_double), C.c_int]
     L.snow_batch_autotune.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_int)]
     L.snow_sort_keys_static.argtypes = [vp, vp, vp, sz, C.c_int, vp]
+    L.snow_server_create.argtypes = [C.POINTER(SnowServerConfig), C.POINTER(vp)]
+    L.snow_server_destroy.argtypes = [vp]
+    L.snow_server_destroy.restype = None
+    L.snow_server_submit.argtypes = [vp, C.POINTER(SnowJobDesc), C.POINTER(C.c_uint64)]
+    L.snow_server_poll.argtypes = [vp, C.POINTER(SnowJobResult), C.c_int, C.POINTER(C.c_int)]
+    L.snow_server_fetch.argtypes = [vp, C.c_uint64, fp, fp, fp, fp]
+    L.snow_server_stats.argtypes = [vp, C.POINTER(SnowServerStats)]
+    L.snow_server_drain.argtypes = [vp, C.c_double]
     _lib = L
     return L
 

@@ -142,11 +142,16 @@ def sample_shape(kind, center, n, h, rng, aspect=(1.0, 1.0, 1.0)):
         key = np.sqrt((d ** 2).sum(1))
     else:
         key = np.abs(d).max(1)
-    # ties broken by a random secondary key so the selection stays isotropic
-    order = np.lexsort((rng.random(len(key)), key))
-    if len(order) < n:
+    # the n smallest keys, ties broken by a random secondary key so the
+    # selection stays isotropic (the same set a full lexsort would give)
+    tie = rng.random(len(key))
+    if len(key) < n:
         raise ValueError("sampling box too small")
-    sel = pts[np.sort(order[:n])]
+    kv = np.partition(key, n - 1)[n - 1]
+    less = np.flatnonzero(key < kv)
+    eq = np.flatnonzero(key == kv)
+    picked = eq[np.argsort(tie[eq], kind="stable")[:n - len(less)]]
+    sel = pts[np.sort(np.concatenate([less, picked]))]
     return sel.astype(np.float32)
 
 
