@@ -10,7 +10,7 @@
 //   compact  turns the flags into the active-block list and gives each
 //            active block a slot in the output pool.
 //   gout     the pool: per slot the grid update's output v* and
-//            d = v* - alpha p/m (6 x 64 floats, 1536 bytes).
+//            d = v* - alpha p/m, one 6-float record per node (1536 bytes).
 //
 // Kernels of one step (every scene of a batch in one launch each):
 //   compact      flags -> slots, active list             (thread per block)
@@ -265,72 +265,109 @@ __device__ __forceinline__ void scatter_global(const SceneDev& S, const P2GParti
 
 // ---- shared memory of one work item --------------------------------------
 struct ItemShared {
-  union {
-    float stage[27][kOutBlockFloats];  // G2P: the pool blocks around the home block
-    float4 pd[kItemMax][kPd];          // P2G: per-particle data, after the gather
-  } u;
-  float tile[kAccFields * kTile3];  // P2G sums of the tile's nodes
-  short plist[kItemMax];            // item particles ordered by tile cell
-  short cells[kCells];              // occupied tile cells
-  int cstart[kCells + 1];
-  int ccount[kCells];
-  int slots[27];                    // pool slot of each tile block (-1: none)
-  int touched[27];                  // tile blocks that received P2G sums
+  float stage[27][kOutBlockFloats];  // G2P: the pool blocks around the home block
+  float4 pd[kItemMax][kPd];          // P2G: per-particle data
+  short plist[kItemMax];             // the item's particles in tile-cell order
+  float tile[kAccFields * kTile3];   // P2G sums of the tile's nodes
+  int cstart[kCells + 1];            // first pd slot of each tile cell
+  int ccount[kCells];                // particles per tile cell (zero between items)
+  int wsum[kItemMax / 32];
+  int wocc[kItemMax / 32];
+  short rows[kTile * kTile];         // flush: tile rows holding mass ...
+  uint32_t rowmask[kTile * kTile];   // ... and which of their nodes do
+  int nrows;
+  short cells[kCells];               // occupied tile cells
   int ncells;
+  int touched[27];                   // tile blocks that received P2G sums
+  int4 item_q[2];                    // this and the next work item of the CTA
+  int scene_q[2];                    // ... and their scenes
+  int next_slots[27];                // pool slots of the next item's tile blocks
+  int coll_scene;                    // scene whose colliders sit in coll
   uint64_t bar;
   snow_collider coll[kShColliders];
 };
 
-// Item set-up shared by the kernels: the home block's coordinates, zeroed
-// P2G tile and buckets, the pool slots of the 27 tile blocks, the scene's
-// colliders. Ends with __syncthreads.
-__device__ __forceinline__ void item_begin(ItemShared& sh, const SceneDev& S, int blk, bool p2g, int nf, int& bx,
-                                           int& by, int& bz) {
+// Tile block k (0..26) around home block (bx, by, bz), or -1 outside the grid.
+__device__ __forceinline__ int tile_block(const SceneDev& S, int bx, int by, int bz, int k) {
+  const int cx = bx - 1 + k % 3, cy = by - 1 + (k / 3) % 3, cz = bz - 1 + k / 9;
+  const bool in = cx >= 0 && cy >= 0 && cz >= 0 && cx < S.bdim[0] && cy < S.bdim[1] && cz < S.bdim[2];
+  return in ? block_id(S, cx, cy, cz) : -1;
+}
+
+__device__ __forceinline__ void home_coords(const SceneDev& S, int blk, int& bx, int& by, int& bz) {
   bx = blk % S.bdim[0];
   by = (blk / S.bdim[0]) % S.bdim[1];
   bz = blk / (S.bdim[0] * S.bdim[1]);
-  if (p2g) {
-    for (int i = threadIdx.x; i < nf * kTile3; i += blockDim.x) sh.tile[i] = 0.0f;
-    for (int i = threadIdx.x; i < kCells; i += blockDim.x) sh.ccount[i] = 0;
-  }
-  if (threadIdx.x < 27) {
-    const int k = threadIdx.x;
-    const int cx = bx - 1 + k % 3, cy = by - 1 + (k / 3) % 3, cz = bz - 1 + k / 9;
-    const bool in = cx >= 0 && cy >= 0 && cz >= 0 && cx < S.bdim[0] && cy < S.bdim[1] && cz < S.bdim[2];
-    sh.slots[k] = in ? S.blk_slot[block_id(S, cx, cy, cz)] : -1;
-    sh.touched[k] = 0;
-  }
-  if (S.ncoll <= kShColliders && threadIdx.x >= 32 && threadIdx.x < 32 + S.ncoll)
-    sh.coll[threadIdx.x - 32] = S.coll[threadIdx.x - 32];
-  __syncthreads();
 }
 
-// Stages the grid-update output of the tile's 27 blocks with bulk copies.
-// Blocks outside the grid or without a slot read as zero. Ends with
-// __syncthreads.
-__device__ __forceinline__ void stage_tile(ItemShared& sh, const SceneDev& S, uint32_t& phase) {
-  // warp 0: lane 0 posts the phase's byte count, then lanes 0..26 each issue
-  // their block's copy
-  if (threadIdx.x < 32) {
-    const int k = threadIdx.x;
-    const bool mine = k < 27 && sh.slots[k] >= 0;
-    const uint32_t nvalid = __popc(__ballot_sync(0xffffffffu, mine));
-    if (k == 0) mbar_arrive_expect_tx(&sh.bar, nvalid * (uint32_t)(kOutBlockFloats * sizeof(float)));
-    __syncwarp();
-    if (mine) {
-      fence_proxy_async_smem();
-      bulk_g2s(sh.u.stage[k], S.gout + (size_t)sh.slots[k] * kOutBlockFloats,
-               (uint32_t)(kOutBlockFloats * sizeof(float)), &sh.bar);
-    }
+// Pool slot of tile block k of item `it`; -1: no block.
+__device__ __forceinline__ int tile_slot(const SceneDev& S, int4 it, int k) {
+  if (k >= 27) return -1;
+  int bx, by, bz;
+  home_coords(S, it.x, bx, by, bz);
+  const int b = tile_block(S, bx, by, bz, k);
+  return b < 0 ? -1 : __ldg(&S.blk_slot[b]);
+}
+
+// One full warp issues the bulk copies (TMA) of the tile's pool blocks into
+// `stage` (lane k < 27 copies block k from pool slot `slot`) and zero-fills
+// the blocks without a slot; completion lands on sh.bar. The caller
+// guarantees nobody reads `stage` until the barrier's phase completes and
+// that all earlier reads of `stage` are done.
+__device__ __forceinline__ void stage_issue(ItemShared& sh, const SceneDev& S, int slot) {
+  const int k = threadIdx.x & 31;
+  const bool mine = k < 27 && slot >= 0;
+  const uint32_t valid = __ballot_sync(0xffffffffu, mine);
+  if (k == 0) mbar_arrive_expect_tx(&sh.bar, __popc(valid) * (uint32_t)(kOutBlockFloats * sizeof(float)));
+  __syncwarp();
+  if (mine) {
+    fence_proxy_async_smem();
+    bulk_g2s(sh.stage[k], S.gout + (size_t)slot * kOutBlockFloats, (uint32_t)(kOutBlockFloats * sizeof(float)),
+             &sh.bar);
   }
-  for (int k = 0; k < 27; k++)
-    if (sh.slots[k] < 0)
-      for (int i = threadIdx.x; i < kOutBlockFloats; i += blockDim.x) sh.u.stage[k][i] = 0.0f;
+  uint32_t missing = __ballot_sync(0xffffffffu, k < 27 && slot < 0);
+  while (missing) {
+    const int m = __ffs(missing) - 1;
+    missing &= missing - 1;
+    float4* dst = reinterpret_cast<float4*>(sh.stage[m]);
+    for (int i = k; i < kOutBlockFloats / 4; i += 32) dst[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  }
+}
+
+// Every thread waits for the stage copies of the current phase (bounded; a
+// copy that never lands is counted and the kernel carries on).
+__device__ __forceinline__ void stage_wait(ItemShared& sh, const SceneDev& S, uint32_t& phase) {
   if (!mbar_wait(&sh.bar, phase, kWaitPolls)) {
-    atomicAdd(&S.counters[CNT_TIMEOUT], 1);
+    if (threadIdx.x == 0) atomicAdd(&S.counters[CNT_TIMEOUT], 1);
     mbar_wait(&sh.bar, phase, kWaitPolls);
   }
   phase ^= 1u;
+}
+
+// Colliders of scene S into shared memory (when they fit). Ends with
+// __syncthreads.
+__device__ __forceinline__ void load_colliders(ItemShared& sh, const SceneDev& S) {
+  if (S.ncoll <= kShColliders && threadIdx.x < S.ncoll) sh.coll[threadIdx.x] = S.coll[threadIdx.x];
+  __syncthreads();
+}
+
+// Zeroes the first nf fields of the P2G tile (at the start of each item,
+// after the previous item's flush has read it).
+__device__ __forceinline__ void tile_zero(ItemShared& sh, int nf) {
+  static_assert(offsetof(ItemShared, tile) % 16 == 0, "tile must be 16-byte aligned");
+  float4* t4 = reinterpret_cast<float4*>(sh.tile);
+  const int n4 = nf * kTile3 / 4;
+  for (int i = threadIdx.x; i < n4; i += blockDim.x) t4[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  for (int i = 4 * n4 + threadIdx.x; i < nf * kTile3; i += blockDim.x) sh.tile[i] = 0.0f;
+}
+
+// Kernel start: cell counts, flags and the bulk-copy barrier. Ends with
+// __syncthreads.
+__device__ __forceinline__ void tile_init(ItemShared& sh) {
+  for (int i = threadIdx.x; i < kCells; i += blockDim.x) sh.ccount[i] = 0;
+  if (threadIdx.x == 32) sh.nrows = 0;
+  if (threadIdx.x < 27) sh.touched[threadIdx.x] = 0;
+  if (threadIdx.x == 0) mbar_init(&sh.bar, 1);
   __syncthreads();
 }
 
@@ -376,7 +413,7 @@ __device__ __forceinline__ void g2p_sums(const AxisW& w, Node node, float dv[3],
 
 // Gather for particle at base cell `base` of the item at home block
 // (bx, by, bz): from the staged tile when the stencil lies in it, else from
-// the pool in global memory.
+// the pool in global memory. Pool nodes are 6-float records (v*, d).
 __device__ __forceinline__ void g2p_gather(const ItemShared& sh, const SceneDev& S, int bx, int by, int bz,
                                            const int base[3], const AxisW& w, float dv[3], float L[3][3]) {
   const int tx = base[0] - 1 - (4 * bx - 2), ty = base[1] - 1 - (4 * by - 2), tz = base[2] - 1 - (4 * bz - 2);
@@ -386,16 +423,17 @@ __device__ __forceinline__ void g2p_gather(const ItemShared& sh, const SceneDev&
 #pragma unroll
     for (int a = 0; a < 4; a++) {
       const int t = tx + a, q = ty + a, r = tz + a;
-      X[a] = ((t + 2) >> 2) * kOutBlockFloats + ((t + 2) & 3);
-      Y[a] = ((q + 2) >> 2) * 3 * kOutBlockFloats + 4 * ((q + 2) & 3);
-      Z[a] = ((r + 2) >> 2) * 9 * kOutBlockFloats + 16 * ((r + 2) & 3);
+      X[a] = ((t + 2) >> 2) * kOutBlockFloats + kOutFields * ((t + 2) & 3);
+      Y[a] = ((q + 2) >> 2) * 3 * kOutBlockFloats + kOutFields * 4 * ((q + 2) & 3);
+      Z[a] = ((r + 2) >> 2) * 9 * kOutBlockFloats + kOutFields * 16 * ((r + 2) & 3);
     }
-    const float* st = &sh.u.stage[0][0];
+    const float* st = &sh.stage[0][0];
     g2p_sums(w,
              [&](int a, int b, int c, float v6[6]) {
-               const float* o = st + X[a] + Y[b] + Z[c];
-#pragma unroll
-               for (int f = 0; f < 6; f++) v6[f] = o[f * kBlockNodes];
+               const float2* o = reinterpret_cast<const float2*>(st + X[a] + Y[b] + Z[c]);
+               const float2 p0 = o[0], p1 = o[1], p2 = o[2];
+               v6[0] = p0.x; v6[1] = p0.y; v6[2] = p1.x;
+               v6[3] = p1.y; v6[4] = p2.x; v6[5] = p2.y;
                return true;
              },
              dv, L);
@@ -406,13 +444,26 @@ __device__ __forceinline__ void g2p_gather(const ItemShared& sh, const SceneDev&
                if (!node_in_grid(S, g0, g1, g2)) return false;
                const int sl = __ldg(&S.blk_slot[block_id(S, g0 >> 2, g1 >> 2, g2 >> 2)]);
                if (sl < 0) return false;
-               const float* o = S.gout + (size_t)sl * kOutBlockFloats + (g0 & 3) + 4 * (g1 & 3) + 16 * (g2 & 3);
+               const float* o = S.gout + (size_t)sl * kOutBlockFloats +
+                                kOutFields * ((g0 & 3) + 4 * (g1 & 3) + 16 * (g2 & 3));
 #pragma unroll
-               for (int f = 0; f < 6; f++) v6[f] = __ldg(o + f * kBlockNodes);
+               for (int f = 0; f < 6; f++) v6[f] = __ldg(o + f);
                return true;
              },
              dv, L);
   }
+}
+
+// Position and velocity of one particle, loaded ahead of the gather.
+struct PState {
+  float4 xm, vv;
+};
+
+__device__ __forceinline__ PState load_state(const SceneDev& S, int p) {
+  PState t;
+  t.xm = S.xm[p];
+  t.vv = S.vv[p];
+  return t;
 }
 
 // particleAdvance.glsl:87-210 for particle p given its G2P sums; stores the
@@ -423,11 +474,12 @@ struct Advanced {
   float jp;
 };
 
-__device__ __forceinline__ void advance_particle(const SceneDev& S, int p, float4 xm, float4 vv, const float dv[3],
+__device__ __forceinline__ void advance_particle(const SceneDev& S, int p, const PState& ps, const float dv[3],
                                                  const float L[3][3], const snow_collider* coll, Advanced& out) {
   M3 FE;
   float jp;
   load_fe(S, p, FE, jp);
+  float4 xm = ps.xm, vv = ps.vv;
   M3 step;
 #pragma unroll
   for (int c = 0; c < 3; c++)
@@ -473,21 +525,79 @@ __device__ __forceinline__ void advance_particle(const SceneDev& S, int p, float
   if (!finite) atomicAdd(&S.counters[CNT_NONFINITE], 1);
 }
 
+// Sums of the particles of one tile cell (list slots j0..j1) for the x-row
+// (b, c) of the cell's 4x4x4 stencil that this lane owns (sixteen lanes cover
+// a stencil), added to the shared tile at the end.
+template <bool MASS_ONLY>
+__device__ __forceinline__ void cell_run(ItemShared& sh, int ci, int j0, int j1, int b, int c) {
+  constexpr int nf = MASS_ONLY ? 1 : kAccFields;
+  float acc[4][kAccFields];
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int f = 0; f < kAccFields; f++) acc[a][f] = 0.0f;
+  for (int j = j0; j < j1; j++) {
+    const float4* d = sh.pd[sh.plist[j]];
+    const float* df = reinterpret_cast<const float*>(d);
+    const float4 w4 = d[4];
+    const float wxa[4] = {w4.x, w4.y, w4.z, w4.w};
+    const float wyb = df[6 * 4 + b], wzc = df[8 * 4 + c];
+    const float t1 = wyb * wzc;
+    const float4 d0 = d[0];
+    const float mw = d0.x * t1;
+    if (MASS_ONLY) {
+#pragma unroll
+      for (int a = 0; a < 4; a++) acc[a][0] += wxa[a] * mw;
+      continue;
+    }
+    const float4 g4 = d[5];
+    const float gxa[4] = {g4.x, g4.y, g4.z, g4.w};
+    const float gyb = df[7 * 4 + b], gzc = df[9 * 4 + c];
+    const float t2 = gyb * wzc, t3 = wyb * gzc;
+    const float4 a1 = d[1], a2 = d[2];
+    const float a22 = df[3 * 4];
+    // A rows: r0 = (a1.x a1.y a1.z), r1 = (a1.w a2.x a2.y), r2 = (a2.z a2.w a22)
+    const float pv[3] = {d0.y * t1, d0.z * t1, d0.w * t1};
+    const float kk[3] = {a1.x * t1, a1.w * t1, a2.z * t1};
+    const float hh[3] = {a1.y * t2 + a1.z * t3, a2.x * t2 + a2.y * t3, a2.w * t2 + a22 * t3};
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+      acc[a][0] += wxa[a] * mw;
+#pragma unroll
+      for (int r = 0; r < 3; r++) {
+        acc[a][1 + r] += wxa[a] * pv[r];
+        acc[a][4 + r] += gxa[a] * kk[r] + wxa[a] * hh[r];
+      }
+    }
+  }
+  const int lx = ci % kCellsPerAxis, ly = (ci / kCellsPerAxis) % kCellsPerAxis, lz = ci / (kCellsPerAxis * kCellsPerAxis);
+  const int t0 = lx + kTile * (ly + b) + kTile * kTile * (lz + c);
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int f = 0; f < nf; f++) atomicAdd(&sh.tile[f * kTile3 + t0 + a], acc[a][f]);
+}
+
 // P2G of the item's particles into acc (every thread of the CTA calls it;
 // thread i holds particle i of the item when `have`):
-//   1. each particle inside the tile takes a bucket slot of its base cell
-//      (the others scatter straight to acc);
-//   2. its mass, momentum, A and axis weights go to shared memory;
-//   3. each half-warp owns one occupied cell's 4x4x4 stencil -- lane l sums
-//      the x-row (b, c) = (l & 3, l >> 2) over the cell's particles in
-//      registers -- and adds the row to the shared tile;
-//   4. the tile's non-empty nodes are added to acc and their blocks flagged.
-template <bool MASS_ONLY>
+//   1. each particle inside the tile counts itself in its base cell and
+//      stores its mass, momentum, A and axis weights (the others scatter
+//      straight to acc);
+//   2. a scan of the cell counts lists the particles in tile-cell order and
+//      the occupied cells;
+//   3. each half-warp owns one occupied cell at a time: lane l sums the
+//      x-row (b, c) = (l & 3, l >> 2) of the cell's stencil over the cell's
+//      particles in registers and adds the row to the shared tile;
+//   4. the tile's non-empty nodes are added to acc (row by row, vector
+//      atomics) and their blocks flagged.
+// `between` runs between steps 3 and 4, long after the staged G2P tile was
+// last read (the fused kernel issues the next item's copies there).
+template <bool MASS_ONLY, class Between>
 __device__ __forceinline__ void p2g_tile_pass(ItemShared& sh, const SceneDev& S, int bx, int by, int bz, bool have,
-                                              const P2GParticle& q, const AxisW& w, const int base[3]) {
+                                              const P2GParticle& q, const AxisW& w, const int base[3],
+                                              Between between) {
   constexpr int nf = MASS_ONLY ? 1 : kAccFields;
   const int ox = 4 * bx - 2, oy = 4 * by - 2, oz = 4 * bz - 2;
-  const int i = threadIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int my_cell = -1, my_rank = 0;
   if (have) {
@@ -501,14 +611,13 @@ __device__ __forceinline__ void p2g_tile_pass(ItemShared& sh, const SceneDev& S,
       scatter_global<MASS_ONLY>(S, q, w, base);
     }
   }
-  __syncthreads();  // buckets counted; the staged G2P tile is no longer read
   if (my_cell >= 0) {
-    float4* d = sh.u.pd[i];
+    float4* d = sh.pd[threadIdx.x];
     const bool f = !MASS_ONLY && q.force;
     d[0] = MASS_ONLY ? make_float4(q.m, 0.0f, 0.0f, 0.0f) : make_float4(q.m, q.mv[0], q.mv[1], q.mv[2]);
     d[1] = f ? make_float4(q.A[0][0], q.A[0][1], q.A[0][2], q.A[1][0]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     d[2] = f ? make_float4(q.A[1][1], q.A[1][2], q.A[2][0], q.A[2][1]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    d[3] = make_float4(f ? q.A[2][2] : 0.0f, 0.0f, 0.0f, 0.0f);
+    d[3] = make_float4(f ? q.A[2][2] : 0.0f, __int_as_float(my_cell), 0.0f, 0.0f);
     d[4] = make_float4(w.wx[0], w.wx[1], w.wx[2], w.wx[3]);
     d[5] = make_float4(w.gx[0], w.gx[1], w.gx[2], w.gx[3]);
     d[6] = make_float4(w.wy[0], w.wy[1], w.wy[2], w.wy[3]);
@@ -516,118 +625,107 @@ __device__ __forceinline__ void p2g_tile_pass(ItemShared& sh, const SceneDev& S,
     d[8] = make_float4(w.wz[0], w.wz[1], w.wz[2], w.wz[3]);
     d[9] = make_float4(w.gz[0], w.gz[1], w.gz[2], w.gz[3]);
   }
-  if (warp == 0) {  // bucket offsets and the list of occupied cells
-    constexpr int per = (kCells + 31) / 32;
-    int cntv[per];
-    int sum = 0, occ = 0;
+  __syncthreads();  // counts and P2G data done
+  // exclusive scan of the cell counts and list of the occupied cells, one
+  // cell per thread
+  const int t = threadIdx.x;
+  const int cnt = t < kCells ? sh.ccount[t] : 0;
+  int incl = cnt;
 #pragma unroll
-    for (int j = 0; j < per; j++) {
-      const int ci = lane * per + j;
-      cntv[j] = ci < kCells ? sh.ccount[ci] : 0;
-      sum += cntv[j];
-      occ += cntv[j] > 0;
-    }
-    int isum = sum, iocc = occ;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int a = __shfl_up_sync(0xffffffffu, isum, o);
-      const int b = __shfl_up_sync(0xffffffffu, iocc, o);
-      if (lane >= o) {
-        isum += a;
-        iocc += b;
-      }
-    }
-    int run = isum - sum, rocc = iocc - occ;
-#pragma unroll
-    for (int j = 0; j < per; j++) {
-      const int ci = lane * per + j;
-      if (ci < kCells) {
-        sh.cstart[ci] = run;
-        if (cntv[j] > 0) sh.cells[rocc++] = (short)ci;
-        run += cntv[j];
-      }
-    }
-    if (lane == 31) {
-      sh.cstart[kCells] = isum;
-      sh.ncells = iocc;
-    }
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const uint32_t occ = __ballot_sync(0xffffffffu, cnt > 0);
+  if (lane == 31) {
+    sh.wsum[warp] = incl;
+    sh.wocc[warp] = __popc(occ);
   }
   __syncthreads();
-  if (my_cell >= 0) sh.plist[sh.cstart[my_cell] + my_rank] = (short)i;
+  int off = 0, ooff = 0;
+  for (int k = 0; k < warp; k++) {
+    off += sh.wsum[k];
+    ooff += sh.wocc[k];
+  }
+  if (t < kCells) {
+    sh.cstart[t] = off + incl - cnt;
+    sh.ccount[t] = 0;
+    if (cnt > 0) sh.cells[ooff + __popc(occ & ((1u << lane) - 1u))] = (short)t;
+  }
+  if (t == kCells - 1) sh.cstart[kCells] = off + incl;
+  if (t == blockDim.x - 1) sh.ncells = ooff + __popc(occ);
+  __syncthreads();
+  if (my_cell >= 0) sh.plist[sh.cstart[my_cell] + my_rank] = (short)threadIdx.x;
   __syncthreads();
   {
+    // half-warp h takes occupied cells h, h + 16, ...: the two halves of a
+    // warp get neighbouring cells, whose particle counts are alike
     const int hw = threadIdx.x >> 4, l16 = threadIdx.x & 15;
-    const int b = l16 & 3, c = l16 >> 2;
     const int nhw = blockDim.x >> 4;
-    for (int k = hw; k < sh.ncells; k += nhw) {
+    const int ncells = sh.ncells;
+    for (int k = hw; k < ncells; k += nhw) {
       const int ci = sh.cells[k];
-      const int j0 = sh.cstart[ci], j1 = sh.cstart[ci + 1];
-      float acc[4][kAccFields];
-#pragma unroll
-      for (int a = 0; a < 4; a++)
-#pragma unroll
-        for (int f = 0; f < kAccFields; f++) acc[a][f] = 0.0f;
-      for (int j = j0; j < j1; j++) {
-        const float4* d = sh.u.pd[sh.plist[j]];
-        const float* df = reinterpret_cast<const float*>(d);
-        const float4 w4 = d[4];
-        const float wxa[4] = {w4.x, w4.y, w4.z, w4.w};
-        const float wyb = df[6 * 4 + b], wzc = df[8 * 4 + c];
-        const float t1 = wyb * wzc;
-        const float4 d0 = d[0];
-        const float mw = d0.x * t1;
-        if (MASS_ONLY) {
-#pragma unroll
-          for (int a = 0; a < 4; a++) acc[a][0] += wxa[a] * mw;
-          continue;
-        }
-        const float4 g4 = d[5];
-        const float gxa[4] = {g4.x, g4.y, g4.z, g4.w};
-        const float gyb = df[7 * 4 + b], gzc = df[9 * 4 + c];
-        const float t2 = gyb * wzc, t3 = wyb * gzc;
-        const float4 a1 = d[1], a2 = d[2], a3 = d[3];
-        // A rows: r0 = (a1.x a1.y a1.z), r1 = (a1.w a2.x a2.y), r2 = (a2.z a2.w a3.x)
-        const float pv[3] = {d0.y * t1, d0.z * t1, d0.w * t1};
-        const float kk[3] = {a1.x * t1, a1.w * t1, a2.z * t1};
-        const float hh[3] = {a1.y * t2 + a1.z * t3, a2.x * t2 + a2.y * t3, a2.w * t2 + a3.x * t3};
-#pragma unroll
-        for (int a = 0; a < 4; a++) {
-          acc[a][0] += wxa[a] * mw;
-#pragma unroll
-          for (int r = 0; r < 3; r++) {
-            acc[a][1 + r] += wxa[a] * pv[r];
-            acc[a][4 + r] += gxa[a] * kk[r] + wxa[a] * hh[r];
-          }
-        }
-      }
-      const int lx = ci % kCellsPerAxis, ly = (ci / kCellsPerAxis) % kCellsPerAxis,
-                lz = ci / (kCellsPerAxis * kCellsPerAxis);
-      const int t0 = lx + kTile * (ly + b) + kTile * kTile * (lz + c);
-#pragma unroll
-      for (int a = 0; a < 4; a++)
-#pragma unroll
-        for (int f = 0; f < nf; f++) atomicAdd(&sh.tile[f * kTile3 + t0 + a], acc[a][f]);
+      cell_run<MASS_ONLY>(sh, ci, sh.cstart[ci], sh.cstart[ci + 1], l16 & 3, l16 >> 2);
     }
   }
   __syncthreads();
-  for (int t = threadIdx.x; t < kTile3; t += blockDim.x) {
-    const float m = sh.tile[t];
-    if (m == 0.0f) continue;
-    const int tx = t % kTile, ty = (t / kTile) % kTile, tz = t / (kTile * kTile);
-    const int g0 = ox + tx, g1 = oy + ty, g2 = oz + tz;
-    if (!node_in_grid(S, g0, g1, g2)) continue;
-    const int k = ((g0 >> 2) - bx + 1) + 3 * ((g1 >> 2) - by + 1) + 9 * ((g2 >> 2) - bz + 1);
-    sh.touched[k] = 1;
-    const int blk = block_id(S, g0 >> 2, g1 >> 2, g2 >> 2);
-    float* dst = S.acc + (size_t)blk * kAccBlockFloats + (g0 & 3) + 4 * (g1 & 3) + 16 * (g2 & 3);
+  between();
+  // 4a. the tile rows (ty, tz) with nodes that hold mass and lie in the grid
+  for (int r = threadIdx.x; r < kTile * kTile; r += blockDim.x) {
+    const int g1 = oy + r % kTile, g2 = oz + r / kTile;
+    uint32_t mask = 0;
+    if (g1 >= 0 && g2 >= 0 && g1 < S.dim[1] && g2 < S.dim[2]) {
+      const float* row = &sh.tile[r * kTile];
 #pragma unroll
-    for (int f = 0; f < nf; f++) atomicAdd(dst + f * kBlockNodes, sh.tile[f * kTile3 + t]);
+      for (int x = 0; x < kTile; x++)
+        if (row[x] != 0.0f && ox + x >= 0 && ox + x < S.dim[0]) mask |= 1u << x;
+    }
+    if (mask) {
+      const int k = atomicAdd(&sh.nrows, 1);
+      sh.rows[k] = r;
+      sh.rowmask[k] = mask;
+    }
+  }
+  __syncthreads();
+  // 4b. one (field, row) per thread: the row's nodes x = 4bx-2 .. 4bx+6 lie
+  // in blocks bx-1 (local x 2, 3), bx (0..3) and bx+1 (0..2); each part is one
+  // vector atomic into acc (nodes without mass or outside the grid add 0, as
+  // does the unused fourth lane of the last part).
+  const int nrows = sh.nrows;
+  for (int task = threadIdx.x; task < nf * nrows; task += blockDim.x) {
+    const int f = task / nrows, k = task % nrows;
+    const int r = sh.rows[k];
+    const uint32_t mask = sh.rowmask[k];
+    const float* row = &sh.tile[f * kTile3 + r * kTile];
+    float v[kTile];
+#pragma unroll
+    for (int x = 0; x < kTile; x++) v[x] = ((mask >> x) & 1u) ? row[x] : 0.0f;
+    const int g1 = oy + r % kTile, g2 = oz + r / kTile;
+    const int kyz = 3 * ((g1 >> 2) - by + 1) + 9 * ((g2 >> 2) - bz + 1);
+    float* base = S.acc + f * kBlockNodes + 4 * (g1 & 3) + 16 * (g2 & 3);
+    if (mask & 0x3u) {
+      const int blk = block_id(S, bx - 1, g1 >> 2, g2 >> 2);
+      atomicAdd(reinterpret_cast<float2*>(base + (size_t)blk * kAccBlockFloats + 2), make_float2(v[0], v[1]));
+      if (f == 0) sh.touched[kyz] = 1;
+    }
+    if (mask & 0x3cu) {
+      const int blk = block_id(S, bx, g1 >> 2, g2 >> 2);
+      atomicAdd(reinterpret_cast<float4*>(base + (size_t)blk * kAccBlockFloats), make_float4(v[2], v[3], v[4], v[5]));
+      if (f == 0) sh.touched[kyz + 1] = 1;
+    }
+    if (mask & 0x1c0u) {
+      const int blk = block_id(S, bx + 1, g1 >> 2, g2 >> 2);
+      atomicAdd(reinterpret_cast<float4*>(base + (size_t)blk * kAccBlockFloats), make_float4(v[6], v[7], v[8], 0.0f));
+      if (f == 0) sh.touched[kyz + 2] = 1;
+    }
   }
   __syncthreads();
   if (threadIdx.x < 27 && sh.touched[threadIdx.x]) {
     const int k = threadIdx.x;
+    sh.touched[k] = 0;
     S.blk_flag[block_id(S, bx - 1 + k % 3, by - 1 + (k / 3) % 3, bz - 1 + k / 9)] = 1;
   }
+  if (threadIdx.x == 32) sh.nrows = 0;
 }
 
 // ===========================================================================
@@ -687,17 +785,19 @@ __global__ void k_compact(const SceneDev* __restrict__ scenes, const int* __rest
 // P2G of the stored particle state (p2gTransfer.glsl:44-151, or
 // gMassCompute.glsl:33-84 when MASS_ONLY).
 template <bool MASS_ONLY>
-__global__ void __launch_bounds__(kItemMax) k_p2g(const SceneDev* __restrict__ scenes,
+__global__ void __launch_bounds__(kItemMax, 2) k_p2g(const SceneDev* __restrict__ scenes,
                                                   const int* __restrict__ item_prefix, int nscenes) {
   extern __shared__ float4 smem_raw[];
   ItemShared& sh = *reinterpret_cast<ItemShared*>(smem_raw);
+  tile_init(sh);
   const int total = item_prefix[nscenes];
   for (int u = blockIdx.x; u < total; u += gridDim.x) {
     const int s = find_scene(item_prefix, nscenes, u);
     const SceneDev& S = scenes[s];
     const int4 it = S.items[u - item_prefix[s]];
+    tile_zero(sh, MASS_ONLY ? 1 : kAccFields);
     int bx, by, bz;
-    item_begin(sh, S, it.x, true, MASS_ONLY ? 1 : kAccFields, bx, by, bz);
+    home_coords(S, it.x, bx, by, bz);
     const int i = threadIdx.x;
     bool have = false;
     P2GParticle q;
@@ -714,7 +814,7 @@ __global__ void __launch_bounds__(kItemMax) k_p2g(const SceneDev* __restrict__ s
         have = true;
       }
     }
-    p2g_tile_pass<MASS_ONLY>(sh, S, bx, by, bz, have, q, w, base);
+    p2g_tile_pass<MASS_ONLY>(sh, S, bx, by, bz, have, q, w, base, [] {});
     __syncthreads();
   }
 }
@@ -740,7 +840,7 @@ __global__ void __launch_bounds__(256) k_grid(const SceneDev* __restrict__ scene
       acc[f * kBlockNodes] = 0.0f;
     }
     if (clear_only) continue;
-    float* out = S.gout + (size_t)slot * kOutBlockFloats + node;
+    float2* out = reinterpret_cast<float2*>(S.gout + (size_t)slot * kOutBlockFloats + kOutFields * node);
     const float mi = v[0];
     float vs[3] = {0.0f, 0.0f, 0.0f}, d[3] = {0.0f, 0.0f, 0.0f};
     if (mi > 0.0f) {
@@ -758,11 +858,9 @@ __global__ void __launch_bounds__(256) k_grid(const SceneDev* __restrict__ scene
 #pragma unroll
       for (int k = 0; k < 3; k++) d[k] = vs[k] - S.alpha * vold[k];
     }
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      out[k * kBlockNodes] = vs[k];
-      out[(3 + k) * kBlockNodes] = d[k];
-    }
+    out[0] = make_float2(vs[0], vs[1]);
+    out[1] = make_float2(vs[2], d[0]);
+    out[2] = make_float2(d[1], d[2]);
   }
 }
 
@@ -801,8 +899,7 @@ __global__ void __launch_bounds__(kItemMax) k_g2p_advance(const SceneDev* __rest
                                                           const int* __restrict__ item_prefix, int nscenes) {
   extern __shared__ float4 smem_raw[];
   ItemShared& sh = *reinterpret_cast<ItemShared*>(smem_raw);
-  if (threadIdx.x == 0) mbar_init(&sh.bar, 1);
-  __syncthreads();
+  tile_init(sh);
   const int total = item_prefix[nscenes];
   uint32_t phase = 0;
   for (int u = blockIdx.x; u < total; u += gridDim.x) {
@@ -810,22 +907,23 @@ __global__ void __launch_bounds__(kItemMax) k_g2p_advance(const SceneDev* __rest
     const SceneDev& S = scenes[s];
     const int4 it = S.items[u - item_prefix[s]];
     int bx, by, bz;
-    item_begin(sh, S, it.x, false, 0, bx, by, bz);
-    stage_tile(sh, S, phase);
+    home_coords(S, it.x, bx, by, bz);
+    if (threadIdx.x < 32) stage_issue(sh, S, tile_slot(S, it, threadIdx.x));
+    load_colliders(sh, S);
+    stage_wait(sh, S, phase);
     const snow_collider* coll = S.ncoll <= kShColliders ? sh.coll : S.coll;
     for (int i = threadIdx.x; i < it.z; i += blockDim.x) {
       const int p = it.y + i;
-      const float4 xm = S.xm[p];
-      const float4 vv = S.vv[p];
+      const PState ps = load_state(S, p);
       float pg[3];
       int base[3];
-      grid_coords(S, xm, pg, base);
+      grid_coords(S, ps.xm, pg, base);
       AxisW w;
       all_weights(pg, base, w);
       float dv[3], L[3][3];
       g2p_gather(sh, S, bx, by, bz, base, w, dv, L);
       Advanced adv;
-      advance_particle(S, p, xm, vv, dv, L, coll, adv);
+      advance_particle(S, p, ps, dv, L, coll, adv);
     }
     __syncthreads();
   }
@@ -835,40 +933,75 @@ __global__ void __launch_bounds__(kItemMax) k_g2p_advance(const SceneDev* __rest
 // P2G of the next, in one pass over the item's particles. The P2G stress uses
 // the rotation R = W V^T of the advance's SVD: F_E' = W S' V^T with S'
 // diagonal up to the Jacobi residual, whose polar rotation is W V^T.
-__global__ void __launch_bounds__(kItemMax) k_g2p2g(const SceneDev* __restrict__ scenes,
-                                                    const int* __restrict__ item_prefix, int nscenes) {
+// The pool blocks of the CTA's next item are copied into shared memory while
+// this item's P2G runs.
+__global__ void __launch_bounds__(kItemMax, 2) k_g2p2g(const SceneDev* __restrict__ scenes,
+                                                       const int* __restrict__ item_prefix, int nscenes) {
   extern __shared__ float4 smem_raw[];
   ItemShared& sh = *reinterpret_cast<ItemShared*>(smem_raw);
-  if (threadIdx.x == 0) mbar_init(&sh.bar, 1);
-  __syncthreads();
+  tile_init(sh);
   const int total = item_prefix[nscenes];
+  if ((int)blockIdx.x >= total) return;
+  // The last warp, which holds the fewest particles of an item (items are
+  // filled from thread 0), looks up the next item and its pool slots.
+  const int lane = threadIdx.x & 31;
+  const bool lastw = (threadIdx.x >> 5) == (blockDim.x >> 5) - 1;
+  if (lastw) {
+    const int s0 = find_scene(item_prefix, nscenes, blockIdx.x);
+    const int4 it0 = scenes[s0].items[blockIdx.x - item_prefix[s0]];
+    stage_issue(sh, scenes[s0], tile_slot(scenes[s0], it0, lane));
+    if (lane == 0) {
+      sh.item_q[0] = it0;
+      sh.scene_q[0] = s0;
+      sh.coll_scene = -1;
+    }
+  }
   uint32_t phase = 0;
-  for (int u = blockIdx.x; u < total; u += gridDim.x) {
-    const int s = find_scene(item_prefix, nscenes, u);
+  int par = 0;
+  for (int u = blockIdx.x; u < total; u += gridDim.x, par ^= 1) {
+    __syncthreads();  // this item's queue entry is written; the last flush is done
+    tile_zero(sh, kAccFields);
+    const int s = sh.scene_q[par];
     const SceneDev& S = scenes[s];
-    const int4 it = S.items[u - item_prefix[s]];
+    if (s != sh.coll_scene) {  // uniform across the CTA
+      load_colliders(sh, S);
+      if (threadIdx.x == 0) sh.coll_scene = s;
+    }
+    const int4 it = sh.item_q[par];
+    const int un = u + gridDim.x;
+    if (lastw && un < total) {
+      const int sn = find_scene(item_prefix, nscenes, un);
+      const int4 itn = scenes[sn].items[un - item_prefix[sn]];
+      const int slot = tile_slot(scenes[sn], itn, lane);
+      if (lane < 27) sh.next_slots[lane] = slot;
+      if (lane == 0) {
+        sh.item_q[par ^ 1] = itn;
+        sh.scene_q[par ^ 1] = sn;
+      }
+    }
     int bx, by, bz;
-    item_begin(sh, S, it.x, true, kAccFields, bx, by, bz);
-    stage_tile(sh, S, phase);
+    home_coords(S, it.x, bx, by, bz);
     const snow_collider* coll = S.ncoll <= kShColliders ? sh.coll : S.coll;
     const int i = threadIdx.x;
+    const bool mine = i < min(it.z, kItemMax);
+    const int p = it.y + i;
+    PState ps;
+    if (mine) ps = load_state(S, p);
+    stage_wait(sh, S, phase);
     bool have = false;
     P2GParticle q;
     AxisW wn;
     int nbase[3] = {0, 0, 0};
-    if (i < min(it.z, kItemMax)) {
-      const int p = it.y + i;
-      const float4 xm = S.xm[p];
-      const float4 vv = S.vv[p];
+    if (mine) {
       float pg[3];
       int base[3];
-      grid_coords(S, xm, pg, base);
+      grid_coords(S, ps.xm, pg, base);
       AxisW w;
       all_weights(pg, base, w);
       float dv[3], L[3][3];
       g2p_gather(sh, S, bx, by, bz, base, w, dv, L);
       Advanced adv;
-      advance_particle(S, p, xm, vv, dv, L, coll, adv);
+      advance_particle(S, p, ps, dv, L, coll, adv);
       // P2G quantities of the advanced particle
       q.m = adv.xm.w;
       if (fabsf(q.m) <= 100.0f) {  // p2gTransfer.glsl:64-66
@@ -883,8 +1016,9 @@ __global__ void __launch_bounds__(kItemMax) k_g2p2g(const SceneDev* __restrict__
         all_weights(npg, nbase, wn);
       }
     }
-    p2g_tile_pass<false>(sh, S, bx, by, bz, have, q, wn, nbase);
-    __syncthreads();
+    p2g_tile_pass<false>(sh, S, bx, by, bz, have, q, wn, nbase, [&] {
+      if (lastw && un < total) stage_issue(sh, scenes[sh.scene_q[par ^ 1]], lane < 27 ? sh.next_slots[lane] : -1);
+    });
   }
 }
 
@@ -944,9 +1078,9 @@ __global__ void k_download_grid(const SceneDev* __restrict__ sd, float* mass, fl
     const int gi = 4 * bx + (node & 3), gj = 4 * by + ((node >> 2) & 3), gk = 4 * bz + (node >> 4);
     if (gi >= S.dim[0] || gj >= S.dim[1] || gk >= S.dim[2]) continue;
     const long long g = gi + (long long)S.dim[0] * (gj + (long long)S.dim[1] * gk);
-    const float* out = S.gout + (size_t)slot * kOutBlockFloats + node;
+    const float* out = S.gout + (size_t)slot * kOutBlockFloats + kOutFields * node;
     if (vstar)
-      for (int k = 0; k < 3; k++) vstar[3 * g + k] = out[k * kBlockNodes];
+      for (int k = 0; k < 3; k++) vstar[3 * g + k] = out[k];
   }
   // acc is dense: every block, every node
   for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;

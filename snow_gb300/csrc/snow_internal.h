@@ -91,7 +91,7 @@ struct SceneDev {
   int* blk_flag;    // nblocks: block received P2G sums since the last compaction
   float* acc;       // nblocks x 448: P2G sums, field-major per block (dense)
   int* active;      // pool_cap: block id of each slot
-  float* gout;      // pool_cap x 384: grid-update output (v*, d)
+  float* gout;      // pool_cap x 384: grid-update output, per node (v*, d) as 6 floats
   int pool_cap;
   // P2G work items: (home block, first particle, count, 0)
   int4* items;
