@@ -284,6 +284,7 @@ def bench_batched(args, local_rank):
 
     sims = [api.SimScene(ctx, s).upload().init() for s in scs]
     batch = api.Batch(ctx, sims)
+    tuning = batch.autotune(dts)  # times candidate work splits on real steps
     for _ in range(W):
         batch.step(1, dts)
     batch_ms = timed(lambda: batch.step(K, dts))
@@ -295,7 +296,7 @@ def bench_batched(args, local_rank):
     # copies of the check scenes to the same step count
     for i in check:
         p = api.SimScene(ctx, scs[i]).upload().init()
-        p.step(dts[i], W + K + 3)
+        p.step(dts[i], tuning["steps_taken"] + W + K + 3)
         a, b = p.download(), sims[i].download()
         diff = max(diff, float(np.abs(a["x"] - b["x"]).max()))
         p.close()
@@ -312,6 +313,8 @@ def bench_batched(args, local_rank):
             "plain_per_scene": {"value": v_plain, "unit": UNIT, "ms_per_step": plain_ms / K},
             "batched": {"value": v_batch, "unit": UNIT, "ms_per_step": batch_ms / K},
             "speedup": v_batch / v_plain,
+            "tuning": {k: tuning[k] for k in ("sort_interval", "items_max", "ctas_per_sm", "ms_per_step",
+                                              "steps_taken")},
             "max_abs_dx_plain_vs_batched": diff,
             "l2": "inputs larger than L2 (no flush)", "scene_generation_s": gen_s}
 

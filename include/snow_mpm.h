@@ -300,9 +300,24 @@ snow_status snow_batch_create(snow_ctx* ctx, snow_scene* const* scenes, int n, s
 void snow_batch_destroy(snow_batch* b);
 /* dt: one per scene (NULL = each scene's last dt or 1e-3). */
 snow_status snow_batch_step(snow_batch* b, const double* dt, int n_steps);
-/* Tunes tile/block/sort parameters on the batch by timing a few steps; the
- * choice is kept in the batch (and reported in *choice_out if non-NULL). */
-snow_status snow_batch_autotune(snow_batch* b, const double* dt, int* choice_out);
+/* Work decomposition of the FAST step (no counterpart in the reference). */
+typedef struct snow_tuning {
+  int sort_interval;   /* steps between re-binnings of each scene's particles (1..64) */
+  int items_max;       /* most particles per work item (64..256) */
+  int ctas_per_sm;     /* work-item CTAs per SM (1 or 2) */
+  int steps_taken;     /* autotune: steps the batch advanced while timing */
+  double ms_per_step;  /* autotune: measured time per step of the choice */
+} snow_tuning;
+/* Applies a tuning to one FAST scene; takes effect at its next re-binning. */
+snow_status snow_scene_set_tuning(snow_scene* s, const snow_tuning* t);
+/* Applies a tuning to every scene of the batch (e.g. one kept from an
+ * earlier autotune); takes effect at each scene's next re-binning. */
+snow_status snow_batch_set_tuning(snow_batch* b, const snow_tuning* t);
+/* Times candidate tunings (sort interval 4/8/16 x 128/256 particles per work
+ * item x 1/2 CTAs per SM) on real steps of the batch and keeps the fastest.
+ * The steps advance the scenes like snow_batch_step (out->steps_taken says
+ * how many); dt as for snow_batch_step. */
+snow_status snow_batch_autotune(snow_batch* b, const double* dt, snow_tuning* out);
 
 #ifdef __cplusplus
 }

@@ -197,6 +197,11 @@ class SimScene:
         self.ctx.check(self.L.snow_scene_stats(self.h, C.byref(s)))
         return _stats_dict(s)
 
+    def set_tuning(self, sort_interval: int, items_max: int = 256, ctas_per_sm: int = 2):
+        t = N.SnowTuning(int(sort_interval), int(items_max), int(ctas_per_sm), 0, 0.0)
+        self.ctx.check(self.L.snow_scene_set_tuning(self.h, C.byref(t)))
+        return self
+
     def cell_keys(self):
         n = self.n
         keys, perm = np.zeros(n, np.uint32), np.zeros(n, np.uint32)
@@ -227,6 +232,48 @@ class Batch:
             dts = (C.c_double * len(self.sims))(*[float(d) for d in dt])
         self.ctx.check(self.L.snow_batch_step(self.h, dts, int(n)))
         return self
+
+    def set_tuning(self, sort_interval: int, items_max: int, ctas_per_sm: int):
+        t = N.SnowTuning(int(sort_interval), int(items_max), int(ctas_per_sm), 0, 0.0)
+        self.ctx.check(self.L.snow_batch_set_tuning(self.h, C.byref(t)))
+        return self
+
+    def signature(self) -> str:
+        """Key of the tuning cache: scene count, particle total (2 significant
+        digits) and the set of grid sizes."""
+        n = sum(s.n for s in self.sims)
+        grids = sorted({tuple(int(g) for g in s.scene.grid_dim) for s in self.sims})
+        return f"{len(self.sims)}|{float(f'{n:.2g}'):.0f}|" + ",".join("x".join(map(str, g)) for g in grids)
+
+    def autotune(self, dt: Optional[Sequence[float]] = None, cache: Optional[str] = None) -> dict:
+        """Chooses sort interval, particles per work item and CTAs per SM by
+        timing real steps of the batch (they advance the scenes), or applies
+        the choice kept in the JSON file `cache` for this batch's signature."""
+        import json
+        import os
+        key = self.signature()
+        table = {}
+        if cache and os.path.exists(cache):
+            with open(cache) as f:
+                table = json.load(f)
+            if key in table:
+                c = table[key]
+                self.set_tuning(c["sort_interval"], c["items_max"], c["ctas_per_sm"])
+                return dict(c, steps_taken=0, cached=True)
+        dts = None
+        if dt is not None:
+            dts = (C.c_double * len(self.sims))(*[float(d) for d in dt])
+        t = N.SnowTuning()
+        self.ctx.check(self.L.snow_batch_autotune(self.h, dts, C.byref(t)))
+        out = dict(sort_interval=t.sort_interval, items_max=t.items_max, ctas_per_sm=t.ctas_per_sm,
+                   ms_per_step=t.ms_per_step)
+        if cache:
+            table[key] = out
+            tmp = cache + ".tmp"
+            with open(tmp, "w") as f:
+                json.dump(table, f, indent=1, sort_keys=True)
+            os.replace(tmp, cache)
+        return dict(out, steps_taken=t.steps_taken, cached=False)
 
     def close(self):
         # Destroying the context or any member scene releases the batch too.

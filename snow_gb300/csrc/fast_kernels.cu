@@ -1128,7 +1128,6 @@ int num_sms() {
   return n;
 }
 
-int fast_item_threads() { return kItemMax; }
 
 void fast_prefix(const SceneDev* scenes, int nscenes, int* items_prefix, int* active_prefix, cudaStream_t st) {
   k_prefix<<<1, 32, 0, st>>>(scenes, nscenes, items_prefix, active_prefix);

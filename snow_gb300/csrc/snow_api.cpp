@@ -221,8 +221,7 @@ snow_status fast_alloc_particles(snow_scene* s, size_t cap) {
       (st = salloc(s, cap, &b.tmp4[3])) || (st = salloc(s, cap, &b.tmp2)) || (st = salloc(s, cap, &b.tmp_pid)))
     return st;
   b.n_cap = cap;
-  const int items_max = fast_item_threads();
-  d.item_cap = (int)(cap / items_max + std::min<size_t>(cap, (size_t)d.nblocks) + 1);
+  d.item_cap = (int)(cap / kMinItemMax + std::min<size_t>(cap, (size_t)d.nblocks) + 1);
   if ((st = salloc(s, (size_t)d.item_cap, &d.items))) return st;
   return SNOW_OK;
 }
@@ -270,13 +269,13 @@ snow_status fast_single_prefix(snow_scene* s) {
   return SNOW_OK;
 }
 
-int item_ctas() { return num_sms() * 2; }
+int item_ctas(const FastTuning& t) { return num_sms() * t.ctas_per_sm; }
 int grid_ctas() { return num_sms() * 8; }
 
 // Binning: keys, radix sort, permutation, work items, item prefix.
 void fast_bin(snow_scene* s, cudaStream_t st) {
   fast_sort_keys(s->sd, s->sd_dev, s->bin, s->key_bits, st);
-  fast_apply_bins(s->sd, s->sd_dev, s->bin, fast_item_threads(), st);
+  fast_apply_bins(s->sd, s->sd_dev, s->bin, s->tune.items_max, st);
   fast_prefix(s->sd_dev, 1, s->d_prefix + 0, s->d_prefix + 2, st);
 }
 
@@ -287,7 +286,7 @@ void fast_enqueue_compact(snow_scene* s, cudaStream_t st) {
   fast_prefix(s->sd_dev, 1, s->d_prefix + 0, s->d_prefix + 2, st);
 }
 void fast_enqueue_p2g(snow_scene* s, bool mass_only, cudaStream_t st) {
-  fast_p2g(s->sd_dev, s->d_prefix + 0, 1, item_ctas(), mass_only, st);
+  fast_p2g(s->sd_dev, s->d_prefix + 0, 1, item_ctas(s->tune), mass_only, st);
 }
 void fast_enqueue_grid(snow_scene* s, bool clear_only, cudaStream_t st) {
   fast_grid(s->sd_dev, s->d_prefix + 2, 1, grid_ctas(), clear_only, st);
@@ -299,7 +298,7 @@ void fast_enqueue_step(snow_scene* s, bool bin, cudaStream_t st) {
   if (bin) fast_bin(s, st);
   fast_enqueue_compact(s, st);
   fast_enqueue_grid(s, false, st);
-  fast_g2p2g(s->sd_dev, s->d_prefix + 0, 1, item_ctas(), st);
+  fast_g2p2g(s->sd_dev, s->d_prefix + 0, 1, item_ctas(s->tune), st);
 }
 
 snow_status set_dt(snow_scene* s, float dt) {
@@ -539,7 +538,7 @@ size_t snow_scene_footprint(const snow_params* p, size_t n) {
   // P2G sums (448 floats), flags, slot and bin tables (5 ints) + the output
   // pool at its largest (every block: 384 floats + 1 int).
   const double tiles = (double)radix_tiles(n);
-  const double items = (double)n / fast_item_threads() + std::min((double)n, nb) + 1;
+  const double items = (double)n / kMinItemMax + std::min((double)n, nb) + 1;
   return (size_t)(n * (76.0 + 92.0) + tiles * 256 * 4.0 + 4096.0 + items * 16.0 + nb * (448 * 4.0 + 5 * 4.0) +
                   nb * (384 * 4.0 + 4.0) + 1024.0);
 }
@@ -790,7 +789,7 @@ snow_status snow_dispatch(snow_scene* s, int kernel, double dt) {
       s->p2g_ready = false;
       break;
     case SNOW_K_G2P:
-      fast_g2p_advance(s->sd_dev, s->d_prefix + 0, 1, item_ctas(), st);
+      fast_g2p_advance(s->sd_dev, s->d_prefix + 0, 1, item_ctas(s->tune), st);
       s->steps_since_sort++;
       break;
     case SNOW_K_P_ADVANCE: break;
@@ -848,7 +847,7 @@ snow_status snow_scene_step(snow_scene* s, double dt, int n_steps) {
       fast_enqueue_compact(s, st);
       fast_enqueue_grid(s, false, st);
       CK(cudaEventRecord(ev[2], st));
-      fast_g2p2g(s->sd_dev, s->d_prefix + 0, 1, item_ctas(), st);
+      fast_g2p2g(s->sd_dev, s->d_prefix + 0, 1, item_ctas(s->tune), st);
       CK(cudaEventRecord(ev[3], st));
       CK(cudaEventSynchronize(ev[3]));
       float t[3];
@@ -1187,7 +1186,7 @@ void batch_enqueue_step(snow_batch* b, int phase, int interval, cudaStream_t st)
   fast_compact(b->d_scenes, blocks, n, b->total_blocks, st);
   fast_prefix(b->d_scenes, n, items, active, st);
   fast_grid(b->d_scenes, active, n, grid_ctas(), false, st);
-  fast_g2p2g(b->d_scenes, items, n, item_ctas(), st);
+  fast_g2p2g(b->d_scenes, items, n, item_ctas(b->scenes[0]->tune), st);
 }
 
 }  // namespace
@@ -1238,10 +1237,86 @@ snow_status snow_batch_step(snow_batch* b, const double* dt, int n_steps) {
   return SNOW_OK;
 }
 
-snow_status snow_batch_autotune(snow_batch* b, const double* dt, int* choice_out) {
+static bool valid_tuning(const snow_tuning* t) {
+  return t && t->sort_interval >= 1 && t->sort_interval <= 64 && t->items_max >= kMinItemMax && t->items_max <= 256 &&
+         (t->ctas_per_sm == 1 || t->ctas_per_sm == 2);
+}
+
+snow_status snow_scene_set_tuning(snow_scene* s, const snow_tuning* t) {
+  if (!s || !valid_tuning(t)) return fail(s ? s->ctx : nullptr, SNOW_EINVAL, "snow_scene_set_tuning: invalid tuning");
+  if (s->mode != SNOW_MODE_FAST) return fail(s->ctx, SNOW_EUNSUPPORTED, "tuning applies to SNOW_MODE_FAST scenes");
+  snow_ctx* ctx = s->ctx;
+  CK(cudaStreamSynchronize(ctx->stream));
+  s->tune.sort_interval = t->sort_interval;
+  s->tune.items_max = t->items_max;
+  s->tune.ctas_per_sm = t->ctas_per_sm;
+  drop_graphs(s);
+  return SNOW_OK;
+}
+
+snow_status snow_batch_set_tuning(snow_batch* b, const snow_tuning* t) {
+  if (!b || !valid_tuning(t)) return fail(b ? b->ctx : nullptr, SNOW_EINVAL, "snow_batch_set_tuning: invalid tuning");
+  snow_ctx* ctx = b->ctx;
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (snow_scene* s : b->scenes) {
+    s->tune.sort_interval = t->sort_interval;
+    s->tune.items_max = t->items_max;
+    s->tune.ctas_per_sm = t->ctas_per_sm;
+    drop_graphs(s);
+  }
+  for (auto& g : b->graphs) cudaGraphExecDestroy(g.second);
+  b->graphs.clear();
+  b->step_count = 0;
+  return SNOW_OK;
+}
+
+// Times each candidate (sort interval x particles per work item x CTAs per
+// SM) over real steps of the batch -- one sort interval to re-bin every scene
+// with the candidate's work items and capture its graphs, then two intervals
+// (at least 8 steps) timed with events -- and keeps the fastest.
+snow_status snow_batch_autotune(snow_batch* b, const double* dt, snow_tuning* out) {
   if (!b) return SNOW_EINVAL;
-  (void)dt;
-  if (choice_out) *choice_out = b->scenes[0]->tune.sort_interval;
+  snow_ctx* ctx = b->ctx;
+  static const int kIntervals[] = {4, 8, 16};
+  static const int kItems[] = {128, 256};
+  static const int kCtas[] = {1, 2};
+  snow_tuning best{};
+  best.ms_per_step = 1e30;
+  int steps = 0;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  snow_status r = SNOW_OK;
+  for (int si : kIntervals)
+    for (int im : kItems)
+      for (int cp : kCtas) {
+        snow_tuning t{si, im, cp, 0, 0.0};
+        if ((r = snow_batch_set_tuning(b, &t))) goto done;
+        if ((r = snow_batch_step(b, dt, si))) goto done;
+        const int k = std::max(8, 2 * si);
+        if (cudaEventRecord(e0, ctx->stream) != cudaSuccess) { r = cuda_fail(ctx, cudaGetLastError(), "event"); goto done; }
+        if ((r = snow_batch_step(b, dt, k))) goto done;
+        if (cudaEventRecord(e1, ctx->stream) != cudaSuccess) { r = cuda_fail(ctx, cudaGetLastError(), "event"); goto done; }
+        if (cudaEventSynchronize(e1) != cudaSuccess) { r = cuda_fail(ctx, cudaGetLastError(), "event"); goto done; }
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        steps += si + k;
+        if (ms / k < best.ms_per_step) {
+          best = t;
+          best.ms_per_step = ms / k;
+        }
+      }
+  r = snow_batch_set_tuning(b, &best);
+done:
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (r) return r;
+  for (snow_scene* s : b->scenes) {
+    r = fast_check(s);
+    if (r) return r;
+  }
+  best.steps_taken = steps;
+  if (out) *out = best;
   return SNOW_OK;
 }
 

@@ -101,12 +101,14 @@ struct SceneDev {
 
 struct FastTuning {
   int sort_interval = 8;  // re-bin particles every k steps
+  int items_max = 256;    // most particles per work item (kMinItemMax .. 256)
+  int ctas_per_sm = 2;    // work-item CTAs launched per SM (1 or 2)
 };
+constexpr int kMinItemMax = 64;
 
 // Work spaces over a batch: prefix[s] .. prefix[s+1] are scene s's units
 // (P2G work items, active blocks, grid blocks). Item and active-block counts
 // are only known on the device; fast_prefix() forms both prefixes there.
-int fast_item_threads();
 void fast_prefix(const SceneDev* scenes, int nscenes, int* items_prefix, int* active_prefix, cudaStream_t st);
 // Zeroes the per-step counters (active blocks, overflow) of every scene.
 void fast_begin_step(const SceneDev* scenes, int nscenes, cudaStream_t st);

@@ -239,12 +239,15 @@ __global__ void k_items(const SceneDev* __restrict__ sd, const int* __restrict__
   for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += gridDim.x * blockDim.x) {
     const int b = home[h];
     const int s = bstart[b], e = bend[b];
-    const int nit = (e - s + items_max - 1) / items_max;
+    // split the block's particles into nit near-equal items of <= items_max
+    const int cnt = e - s;
+    const int nit = (cnt + items_max - 1) / items_max;
     const int at = atomicAdd(&S.counters[CNT_ITEMS], nit);
     for (int j = 0; j < nit; j++) {
       if (at + j >= S.item_cap) break;  // cannot happen: item_cap covers the bound
-      const int first = s + j * items_max;
-      S.items[at + j] = make_int4(b, first, min(items_max, e - first), 0);
+      const int first = s + (int)(((long long)j * cnt) / nit);
+      const int last = s + (int)(((long long)(j + 1) * cnt) / nit);
+      S.items[at + j] = make_int4(b, first, last - first, 0);
     }
   }
 }

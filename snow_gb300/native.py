@@ -29,6 +29,7 @@ EXPORTS = [
     "snow_scene_cell_keys", "snow_scene_phase_times", "snow_batch_create", "snow_batch_destroy",
     "snow_batch_step", "snow_batch_autotune", "snow_sort_keys_static", "snow_server_create", "snow_server_destroy",
     "snow_server_submit", "snow_server_poll", "snow_server_fetch", "snow_server_stats", "snow_server_drain",
+    "snow_scene_set_tuning", "snow_batch_set_tuning",
 ]
 SORT_STATIC_MAX_KEYS = 262144  # SNOW_SORT_STATIC_MAX_KEYS
 
@@ -54,6 +55,11 @@ class SnowStats(C.Structure):
 class SnowPhaseTimes(C.Structure):
     _fields_ = [("sort_ms", C.c_double), ("p2g_ms", C.c_double), ("grid_ms", C.c_double), ("g2p_ms", C.c_double),
                 ("other_ms", C.c_double), ("total_ms", C.c_double), ("steps", C.c_uint64)]
+
+
+class SnowTuning(C.Structure):
+    _fields_ = [("sort_interval", C.c_int), ("items_max", C.c_int), ("ctas_per_sm", C.c_int),
+                ("steps_taken", C.c_int), ("ms_per_step", C.c_double)]
 
 
 class SnowServerConfig(C.Structure):
@@ -137,7 +143,9 @@ def load(path: str = LIB_PATH):
     L.snow_batch_destroy.argtypes = [vp]
     L.snow_batch_destroy.restype = None
     L.snow_batch_step.argtypes = [vp, C.POINTER(C.c_double), C.c_int]
-    L.snow_batch_autotune.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_int)]
+    L.snow_batch_autotune.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(SnowTuning)]
+    L.snow_batch_set_tuning.argtypes = [vp, C.POINTER(SnowTuning)]
+    L.snow_scene_set_tuning.argtypes = [vp, C.POINTER(SnowTuning)]
     L.snow_sort_keys_static.argtypes = [vp, vp, vp, sz, C.c_int, vp]
     L.snow_server_create.argtypes = [C.POINTER(SnowServerConfig), C.POINTER(vp)]
     L.snow_server_destroy.argtypes = [vp]

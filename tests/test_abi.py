@@ -49,3 +49,34 @@ def test_struct_layouts_match_the_header():
     # snow_collider is the reference's cx, cv, cn vec4 triple: 48 bytes
     assert ctypes.sizeof(native.SnowCollider) == 48
     assert ctypes.sizeof(native.SnowParams) == 4 * (3 + 3 + 1 + 6 + 3 + 2)
+
+
+def test_ctypes_structs_match_the_c_compiler_layout(tmp_path):
+    """Every struct of the header, laid out by gcc, against its ctypes twin:
+    size and each field's offset."""
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc unavailable")
+    import subprocess
+    from snow_gb300 import native as N
+    pairs = {"snow_params": N.SnowParams, "snow_collider": N.SnowCollider, "snow_stats": N.SnowStats,
+             "snow_phase_times": N.SnowPhaseTimes, "snow_tuning": N.SnowTuning,
+             "snow_server_config": N.SnowServerConfig, "snow_job_desc": N.SnowJobDesc,
+             "snow_job_result": N.SnowJobResult, "snow_server_report": N.SnowServerStats}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "snow_mpm.h"', "int main(void) {"]
+    for cname, ct in pairs.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in ct._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines.append("  return 0;\n}")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.check_call(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    got = {}
+    for line in subprocess.check_output([str(exe)], text=True).splitlines():
+        a, b, v = line.split()
+        got[(a, b)] = int(v)
+    for cname, ct in pairs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(ct), cname
+        for fname, _ in ct._fields_:
+            assert got[(cname, fname)] == getattr(ct, fname).offset, (cname, fname)

@@ -1,5 +1,7 @@
 """GPU tests of the host API: batching, the reference-shaped engine classes,
 error statuses, and that results are the same alone and in a batch."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -84,3 +86,48 @@ def test_rigid_advance_moves_colliders(ctx):
     sim = api.SimScene(ctx, s).upload().init().step(1e-3, 10)
     c = sim.colliders()
     assert abs(c[-1][1] - (0.1 + 10 * 1e-3)) < 1e-6
+
+
+@gpu
+def test_tunings_change_the_work_split_not_the_physics(ctx):
+    """Sort interval, particles per work item and CTAs per SM only change how
+    the step is cut into launches; states agree with the default within the
+    batch-vs-alone tolerance."""
+    from snow_gb300 import api
+    scs = _three_scenes()
+    steps = 12
+    alone = [api.SimScene(ctx, s).upload().init().step(s.dt, steps).download() for s in scs]
+    for si, im, cp in [(4, 128, 1), (16, 64, 2), (1, 256, 1)]:
+        sims = [api.SimScene(ctx, s).upload().init() for s in scs]
+        b = api.Batch(ctx, sims).set_tuning(si, im, cp)
+        b.step(steps, dt=[s.dt for s in scs])
+        for a, sim in zip(alone, sims):
+            got = sim.download()
+            assert np.abs(a["x"] - got["x"]).max() <= 1e-4
+            assert np.abs(a["FE"] - got["FE"]).max() <= 1e-4
+        b.close()
+        for sim in sims:
+            sim.close()
+    single = api.SimScene(ctx, scs[0]).upload().init().set_tuning(2, 96, 1).step(scs[0].dt, steps).download()
+    assert np.abs(alone[0]["x"] - single["x"]).max() <= 1e-4
+
+
+@gpu
+def test_autotune_picks_a_candidate_and_reuses_the_cache(ctx, tmp_path):
+    from snow_gb300 import api, native as N
+    scs = _three_scenes()
+    sims = [api.SimScene(ctx, s).upload().init() for s in scs]
+    b = api.Batch(ctx, sims)
+    cache = str(tmp_path / "tuning.json")
+    c = b.autotune(dt=[s.dt for s in scs], cache=cache)
+    assert not c["cached"] and c["steps_taken"] > 0 and c["ms_per_step"] > 0
+    assert c["sort_interval"] in (4, 8, 16) and c["items_max"] in (128, 256) and c["ctas_per_sm"] in (1, 2)
+    again = b.autotune(dt=[s.dt for s in scs], cache=cache)
+    assert again["cached"] and again["steps_taken"] == 0
+    assert {k: again[k] for k in ("sort_interval", "items_max", "ctas_per_sm")} == \
+        {k: c[k] for k in ("sort_interval", "items_max", "ctas_per_sm")}
+    b.step(3, dt=[s.dt for s in scs])
+    for sim in sims:
+        assert sim.stats()["nonfinite"] == 0
+    bad = N.SnowTuning(0, 256, 2, 0, 0.0)
+    assert N.load().snow_batch_set_tuning(b.h, ctypes.byref(bad)) == -1
