@@ -144,6 +144,10 @@ def bench_ours(args, local_rank):
     sim.upload().init()
     n = s.n
     dt = s.dt
+    # work split chosen by the autotuner (on real steps of this scene)
+    tb = api.Batch(ctx, [sim])
+    tuning = tb.autotune([dt])
+    tb.close()
     # active grid nodes (nodes with mass) after one step, for the roofline
     sim.step(dt, 1)
     ctx.synchronize()
@@ -201,7 +205,7 @@ def bench_ours(args, local_rank):
     e2e_steps = args.steps
     t1 = time.perf_counter()
     sim2 = api.SimScene(ctx, s, mode=N.MODE_FAST)
-    sim2.upload().init()
+    sim2.upload().init().set_tuning(tuning["sort_interval"], tuning["items_max"], tuning["ctas_per_sm"])
     for _ in range(e2e_steps):
         sim2.step(dt, 1)
         sim2.stats()
@@ -213,7 +217,7 @@ def bench_ours(args, local_rank):
     sim2.close()
     del out
 
-    sort_every = sim.params.sort_interval or 8
+    sort_every = tuning["sort_interval"]
     key_bits = math.ceil(math.log2(((args.grid + 3) // 4) ** 3 * 64))
     launches = 0
     for i in range(args.steps):
@@ -223,7 +227,7 @@ def bench_ours(args, local_rank):
     res = dict(total_ms=total_ms, step_ms=step_ms, n=n, A=A, per=per, dominant=dominant, alg_bytes=alg_bytes,
                achieved=achieved, peak=peak, peak_kind=peak_kind, clocks=clocks.summary(), e2e_s=e2e_s,
                e2e_steps=e2e_steps, h2d=h2d, d2h=d2h_stats + d2h_final / e2e_steps, launches=launches,
-               gen_s=gen_s, stats=st, scene=s)
+               gen_s=gen_s, stats=st, scene=s, tuning=tuning)
     ctx.close()
     return res
 
@@ -233,20 +237,23 @@ def _events(stream, n):
     return [torch.cuda.Event(enable_timing=True) for _ in range(n)]
 
 
-def bench_batched(args, local_rank):
-    """Many independent scenes of uneven size (64 scenes, 10k-500k particles
-    log-uniform, 64^3-192^3 grids, per-scene E0 and xi): the plain per-scene
-    loop (each scene's own step, scenes one after another) against the batched
-    step (one launch per phase for all scenes, CUDA graph). Both advance the
-    same scenes by the same steps; the inputs (~10M particles, ~1.7 GB of
-    state) are far larger than L2, so no flush is needed."""
+def bench_batched(args, local_rank, at_scale=False):
+    """Many independent scenes of uneven size: the plain per-scene loop (each
+    scene's own step, scenes one after another) against the batched step (one
+    launch per phase for all scenes, CUDA graph, autotuned work split). Both
+    advance the same scenes by the same steps; the inputs are far larger than
+    L2, so no flush is needed.
+      default:   64 scenes, 10k-500k particles log-uniform, 64^3-192^3 grids,
+                 per-scene E0 and xi (~10M particles, ~1.7 GB of state);
+      at_scale:  16 snow blocks of 2M-8M particles dropped onto a sphere
+                 collider, 384^3-512^3 grids (~80M particles)."""
     import torch
 
     from snow_gb300 import api, scenes
 
     torch.cuda.set_device(local_rank)
     t0 = time.time()
-    scs = scenes.cfg3_batch(n_scenes=args.batch_scenes)
+    scs = scenes.cfg4_batch(n_scenes=args.batch_scenes) if at_scale else scenes.cfg3_batch(n_scenes=args.batch_scenes)
     gen_s = time.time() - t0
     ntot = sum(s.n for s in scs)
     dts = [s.dt for s in scs]
@@ -276,8 +283,11 @@ def bench_batched(args, local_rank):
                 sim.step(dt, 1)
 
     plain_ms = timed(plain_loop)
+    # the same loop launching each step's kernels one by one (no CUDA graph)
+    ctx.set_graphs(False)
+    eager_ms = timed(plain_loop)
+    ctx.set_graphs(True)
     check = sorted(range(len(scs)), key=lambda i: scs[i].n)[:4]
-    ref_states = {i: plain[i].download() for i in check}
     for sim in plain:
         sim.close()
     del plain
@@ -305,12 +315,22 @@ def bench_batched(args, local_rank):
         sim.close()
     ctx.close()
     v_plain = ntot * K / (plain_ms * 1e-3)
+    v_eager = ntot * K / (eager_ms * 1e-3)
     v_batch = ntot * K / (batch_ms * 1e-3)
-    return {"workload": f"{len(scs)} independent scenes, {ntot} particles in total (10k-500k log-uniform), "
-                        f"grids {min(s.grid_dim[0] for s in scs)}^3-{max(s.grid_dim[0] for s in scs)}^3, "
-                        f"E0 ~ U[4.8e4, 1.4e5], xi ~ U[5, 10], dt=1e-4",
+    grids = f"grids {min(s.grid_dim[0] for s in scs)}^3-{max(s.grid_dim[0] for s in scs)}^3"
+    if at_scale:
+        wl = (f"{len(scs)} snow blocks dropped onto a sphere collider, {ntot} particles in total (2M-8M each), "
+              f"{grids}, dt=2e-5")
+    else:
+        wl = (f"{len(scs)} independent scenes, {ntot} particles in total (10k-500k log-uniform), {grids}, "
+              f"E0 ~ U[4.8e4, 1.4e5], xi ~ U[5, 10], dt=1e-4")
+    return {"workload": wl,
             "steps": K, "warmup": W, "particles": ntot,
-            "plain_per_scene": {"value": v_plain, "unit": UNIT, "ms_per_step": plain_ms / K},
+            "plain_per_scene": {"value": v_plain, "unit": UNIT, "ms_per_step": plain_ms / K,
+                                "launch": "each scene's step replayed as its own CUDA graph"},
+            "plain_per_scene_eager": {"value": v_eager, "unit": UNIT, "ms_per_step": eager_ms / K,
+                                      "launch": "each scene's kernels launched one by one"},
+            "speedup_vs_eager": v_batch / v_eager,
             "batched": {"value": v_batch, "unit": UNIT, "ms_per_step": batch_ms / K},
             "speedup": v_batch / v_plain,
             "tuning": {k: tuning[k] for k in ("sort_interval", "items_max", "ctas_per_sm", "ms_per_step",
@@ -473,6 +493,8 @@ def main():
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
     ap.add_argument("--serve-drain-s", type=float, default=180.0)
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--workload", default="default", choices=["default", "batch16"],
+                    help="batch16: only the 16-scene batch at scale (2M-8M particles each), one JSON line")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local_rank = rank_info()
@@ -488,6 +510,27 @@ def main():
                 "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": r["cores"], "kind": r["kind"],
                                  "sample": r["sample"]},
                 "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    if args.workload == "batch16":
+        if rank != 0:
+            return 0
+        if "--batch-scenes" not in sys.argv:
+            args.batch_scenes = 16
+        if "--batch-steps" not in sys.argv:
+            args.batch_steps = 8
+        r = bench_batched(args, local_rank, at_scale=True)
+        b = r["batched"]
+        line = {"metric": METRIC, "value": b["value"], "unit": UNIT, "n_gpus": 1, "steps": r["steps"],
+                "warmup": r["warmup"], "ms_per_step": b["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered lattice)",
+                "config": {"workload": r["workload"], "particles": r["particles"], "mode": "fast (FP32)",
+                           "l2": r["l2"], "parallelism": "replicas", "tuning": r["tuning"]},
+                "plain_per_scene": r["plain_per_scene"], "speedup": r["speedup"],
+                "plain_per_scene_eager": r["plain_per_scene_eager"], "speedup_vs_eager": r["speedup_vs_eager"],
+                "max_abs_dx_plain_vs_batched": r["max_abs_dx_plain_vs_batched"],
+                "scene_generation_s": r["scene_generation_s"]}
         print(json.dumps(line))
         return 0
 
@@ -515,7 +558,8 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered lattice)",
-        "config": workload_config(args),
+        "config": dict(workload_config(args), tuning={k: res["tuning"][k] for k in
+                                                       ("sort_interval", "items_max", "ctas_per_sm")}),
         "roofline": {"bound": "hbm", "kernel": res["dominant"], "achieved": res["achieved"],
                      "peak": res["peak"], "unit": "GB/s", "frac": res["achieved"] / res["peak"],
                      "peak_source": res["peak_kind"],

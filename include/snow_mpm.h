@@ -136,6 +136,10 @@ void snow_ctx_destroy(snow_ctx* ctx);
 const char* snow_last_error(const snow_ctx* ctx);
 size_t snow_ctx_bytes_in_use(const snow_ctx* ctx);
 snow_status snow_ctx_set_profiling(snow_ctx* ctx, int on);
+/* on = 0: snow_scene_step launches each step's kernels one by one instead of
+ * replaying the step's captured CUDA graph (default on). Batches always
+ * replay graphs. */
+snow_status snow_ctx_set_graphs(snow_ctx* ctx, int on);
 /* The cudaStream_t every call of this context launches on, for callers that
  * order or time their own GPU work against it. */
 void* snow_ctx_stream(const snow_ctx* ctx);

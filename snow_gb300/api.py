@@ -44,6 +44,10 @@ class Context:
     def set_profiling(self, on: bool):
         self.check(self.L.snow_ctx_set_profiling(self.h, int(bool(on))))
 
+    def set_graphs(self, on: bool):
+        """False: single-scene steps launch kernels one by one (no CUDA graph)."""
+        self.check(self.L.snow_ctx_set_graphs(self.h, int(bool(on))))
+
     @property
     def stream(self) -> int:
         """The context's cudaStream_t as an integer handle."""

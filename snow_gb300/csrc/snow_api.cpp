@@ -26,6 +26,7 @@ struct snow_ctx {
   size_t used = 0;
   std::string err;
   bool profiling = false;
+  bool graphs = true;  // replay each step as a captured CUDA graph
   StatsAccum* d_stats = nullptr;
   StatsAccum* h_stats = nullptr;  // pinned
   int* h_counters = nullptr;      // pinned, kCounterStride ints
@@ -515,6 +516,12 @@ void snow_ctx_destroy(snow_ctx* ctx) {
 
 const char* snow_last_error(const snow_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
 size_t snow_ctx_bytes_in_use(const snow_ctx* ctx) { return ctx ? ctx->used : 0; }
+snow_status snow_ctx_set_graphs(snow_ctx* ctx, int on) {
+  if (!ctx) return SNOW_EINVAL;
+  ctx->graphs = on != 0;
+  return SNOW_OK;
+}
+
 snow_status snow_ctx_set_profiling(snow_ctx* ctx, int on) {
   if (!ctx) return SNOW_EINVAL;
   ctx->profiling = on != 0;
@@ -857,6 +864,8 @@ snow_status snow_scene_step(snow_scene* s, double dt, int n_steps) {
       s->times.g2p_ms += t[2];
       s->times.total_ms += t[0] + t[1] + t[2];
       s->times.steps++;
+    } else if (!ctx->graphs) {
+      fast_enqueue_step(s, bin, st);
     } else {
       cudaGraphExec_t& g = bin ? s->g_sort : s->g_plain;
       if (!g || s->g_dt != fdt) {

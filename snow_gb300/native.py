@@ -29,7 +29,7 @@ EXPORTS = [
     "snow_scene_cell_keys", "snow_scene_phase_times", "snow_batch_create", "snow_batch_destroy",
     "snow_batch_step", "snow_batch_autotune", "snow_sort_keys_static", "snow_server_create", "snow_server_destroy",
     "snow_server_submit", "snow_server_poll", "snow_server_fetch", "snow_server_stats", "snow_server_drain",
-    "snow_scene_set_tuning", "snow_batch_set_tuning",
+    "snow_scene_set_tuning", "snow_batch_set_tuning", "snow_ctx_set_graphs",
 ]
 SORT_STATIC_MAX_KEYS = 262144  # SNOW_SORT_STATIC_MAX_KEYS
 
@@ -116,6 +116,7 @@ def load(path: str = LIB_PATH):
     L.snow_ctx_bytes_in_use.argtypes = [vp]
     L.snow_ctx_bytes_in_use.restype = sz
     L.snow_ctx_set_profiling.argtypes = [vp, C.c_int]
+    L.snow_ctx_set_graphs.argtypes = [vp, C.c_int]
     L.snow_ctx_synchronize.argtypes = [vp]
     L.snow_ctx_stream.argtypes = [vp]
     L.snow_ctx_stream.restype = vp
