@@ -357,7 +357,8 @@ def bench_serving(args, local_rank):
         if t > args.serve_seconds:
             break
         arrivals.append((t, int(rng.integers(len(pool))), int(rng.integers(50, 2001))))
-    srv = api.Server(local_rank, hbm_budget=int(args.serve_budget_gb * (1 << 30)), chunk_steps=16)
+    srv = api.Server(local_rank, hbm_budget=int(args.serve_budget_gb * (1 << 30)), chunk_steps=16,
+                     max_active_particles=args.serve_cap, policy=args.serve_policy)
     t0 = time.perf_counter()
     ids = {}
     for at, j, steps in arrivals:
@@ -386,7 +387,8 @@ def bench_serving(args, local_rank):
     offered = sum(pool[j].n * st for j, st in ids.values()) / args.serve_seconds
     return {"workload": f"Poisson arrivals at {args.serve_rate}/s for {args.serve_seconds} s, jobs of 20k-2M "
                         f"particles (log-uniform, pool of {len(pool)} scenes) x 50-2000 steps, HBM budget "
-                        f"{args.serve_budget_gb} GB, chunks of 16 steps",
+                        f"{args.serve_budget_gb} GB, chunks of 16 steps, {args.serve_policy} under a cap of "
+                        f"{args.serve_cap} particles stepped together",
             "jobs": len(ids), "completed": len(ok), "failed": len(res) - len(ok), "drained": drained,
             "value": psteps / wall, "unit": UNIT, "wall_s": wall, "busy_s": stats["busy_s"],
             "offered_particle_steps_per_s": offered,
@@ -493,6 +495,8 @@ def main():
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
     ap.add_argument("--serve-drain-s", type=float, default=180.0)
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serve-policy", default="srpt", choices=["fifo", "srpt"])
+    ap.add_argument("--serve-cap", type=int, default=4 << 20, help="particles stepped together (0 = all)")
     ap.add_argument("--workload", default="default", choices=["default", "batch16"],
                     help="batch16: only the 16-scene batch at scale (2M-8M particles each), one JSON line")
     args = ap.parse_args()

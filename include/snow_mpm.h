@@ -206,15 +206,21 @@ snow_status snow_scene_phase_times(snow_scene* s, snow_phase_times* out, int res
  * budget, keeps every admitted job's state resident, and advances all
  * admitted jobs together as one batch (snow_batch_step) in chunks of steps;
  * jobs that arrive meanwhile join at the next chunk boundary and finished jobs
- * leave, freeing their memory. (No counterpart in the reference, which runs
- * one scene per process.) */
+ * leave, freeing their memory. With a particle cap, only the first resident
+ * jobs (arrival order, or least remaining work) step in a chunk; the others
+ * keep their state on the device and wait. (No counterpart in the reference,
+ * which runs one scene per process.) */
 typedef struct snow_server snow_server;
+
+enum { SNOW_SERVE_FIFO = 0, SNOW_SERVE_SRPT = 1 };
 
 typedef struct snow_server_config {
   int device;
-  size_t hbm_budget_bytes;  /* admission limit for resident jobs (0 = no limit) */
-  int max_active;           /* most jobs advanced together (0 = 256) */
-  int chunk_steps;          /* steps per batch launch between admissions (0 = 16) */
+  size_t hbm_budget_bytes;      /* admission limit for resident jobs (0 = no limit) */
+  int max_active;               /* most jobs resident at once (0 = 256) */
+  int chunk_steps;              /* steps per batch launch between admissions (0 = 16) */
+  size_t max_active_particles;  /* particles stepped together per chunk (0 = all resident jobs) */
+  int policy;                   /* which resident jobs step first under the cap: SNOW_SERVE_* */
 } snow_server_config;
 
 typedef struct snow_job_desc {

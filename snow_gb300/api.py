@@ -302,12 +302,17 @@ def _stats_dict(s: N.SnowStats) -> dict:
 class Server:
     """Continuous-batching simulation server (snow_server_* in the C ABI): a
     native worker thread admits submitted jobs while their device footprint
-    fits the HBM budget and advances all admitted jobs together, chunk by
-    chunk; jobs join and leave at chunk boundaries."""
+    fits the HBM budget and advances admitted jobs together, chunk by chunk;
+    jobs join and leave at chunk boundaries. With `max_active_particles`,
+    only that many particles step per chunk, chosen in arrival order
+    ("fifo") or least remaining work first ("srpt")."""
 
-    def __init__(self, device: int = 0, hbm_budget: int = 0, max_active: int = 0, chunk_steps: int = 0):
+    def __init__(self, device: int = 0, hbm_budget: int = 0, max_active: int = 0, chunk_steps: int = 0,
+                 max_active_particles: int = 0, policy: str = "fifo"):
         self.L = N.load()
-        cfg = N.SnowServerConfig(int(device), int(hbm_budget), int(max_active), int(chunk_steps))
+        pol = {"fifo": N.SERVE_FIFO, "srpt": N.SERVE_SRPT}[policy]
+        cfg = N.SnowServerConfig(int(device), int(hbm_budget), int(max_active), int(chunk_steps),
+                                 int(max_active_particles), pol)
         h = C.c_void_p()
         st = self.L.snow_server_create(C.byref(cfg), C.byref(h))
         if st != N.SNOW_OK:

@@ -6,9 +6,12 @@
 //      fit waits; nothing behind it overtakes it);
 //   2. creates, uploads and initialises the admitted jobs' scenes (their state
 //      stays resident until they finish);
-//   3. advances every admitted job together with snow_batch_step by
-//      k = min(chunk, fewest remaining steps) steps -- one launch per phase
-//      for all jobs, a CUDA graph per batch composition;
+//   3. picks the admitted jobs that step in this chunk (all of them, or --
+//      with a particle cap -- the first ones in arrival order or by least
+//      remaining work, SRPT) and advances them together with snow_batch_step
+//      by k = min(chunk, fewest remaining steps) steps -- one launch per
+//      phase for all of them, CUDA graphs per batch composition; jobs left
+//      out keep their state resident and wait;
 //   4. retires finished jobs (bulk statistics, optional final state), which
 //      frees their memory for the next admissions.
 // Jobs that arrive while others run join at the next chunk boundary, so their
@@ -55,7 +58,6 @@ struct snow_server {
   std::mutex mu;
   std::condition_variable cv;
   std::deque<Job*> pending;
-  std::vector<Job*> active;
   std::deque<Job*> done;
   std::map<uint64_t, Job*> kept;
   std::thread worker;
@@ -99,29 +101,31 @@ void run(snow_server* srv) {
   }
   srv->cv.notify_all();
   if (s0 != SNOW_OK) return;
-  const int max_active = srv->cfg.max_active > 0 ? srv->cfg.max_active : 256;
+  const int max_resident = srv->cfg.max_active > 0 ? srv->cfg.max_active : 256;
   const int chunk = srv->cfg.chunk_steps > 0 ? srv->cfg.chunk_steps : 16;
   const size_t budget = srv->cfg.hbm_budget_bytes;
-  std::vector<Job*> active;
+  const size_t cap = srv->cfg.max_active_particles;
+  const bool srpt = srv->cfg.policy == SNOW_SERVE_SRPT;
+  std::vector<Job*> resident;  // admitted, state on the device
+  std::vector<Job*> running;   // the members of `batch`
   snow_batch* batch = nullptr;
-  bool dirty = true;
   double busy_since = -1.0;
   for (;;) {
-    // ---- admission -------------------------------------------------------
+    // ---- admission (arrival order, HBM budget) ---------------------------
     std::vector<Job*> admit;
     {
       std::unique_lock<std::mutex> lock(srv->mu);
-      if (active.empty() && srv->pending.empty()) {
+      if (resident.empty() && srv->pending.empty()) {
         if (srv->stop) break;
         srv->cv.wait_for(lock, std::chrono::milliseconds(2));
         continue;
       }
-      size_t resident = snow_ctx_bytes_in_use(ctx);
-      while (!srv->pending.empty() && (int)(active.size() + admit.size()) < max_active) {
+      size_t used = snow_ctx_bytes_in_use(ctx);
+      while (!srv->pending.empty() && (int)(resident.size() + admit.size()) < max_resident) {
         Job* j = srv->pending.front();
-        if (budget && resident + j->footprint > budget) {
-          if (!active.empty() || !admit.empty()) break;  // wait for memory to free up
-          if (j->footprint > budget) {                    // can never fit
+        if (budget && used + j->footprint > budget) {
+          if (!resident.empty() || !admit.empty()) break;  // wait for memory to free up
+          if (j->footprint > budget) {                      // can never fit
             srv->pending.pop_front();
             srv->st.pending = srv->pending.size();
             lock.unlock();
@@ -131,7 +135,7 @@ void run(snow_server* srv) {
           }
         }
         srv->pending.pop_front();
-        resident += j->footprint;
+        used += j->footprint;
         admit.push_back(j);
       }
       srv->st.pending = srv->pending.size();
@@ -150,51 +154,66 @@ void run(snow_server* srv) {
       std::vector<float>().swap(j->x);  // the device holds the state now
       std::vector<float>().swap(j->v);
       std::vector<float>().swap(j->m);
-      active.push_back(j);
-      dirty = true;
+      resident.push_back(j);
       std::lock_guard<std::mutex> lock(srv->mu);
       srv->st.admitted++;
     }
     {
       std::lock_guard<std::mutex> lock(srv->mu);
-      srv->st.active = active.size();
+      srv->st.active = resident.size();
       srv->st.resident_bytes = snow_ctx_bytes_in_use(ctx);
     }
-    if (active.empty()) continue;
+    if (resident.empty()) continue;
     if (busy_since < 0) busy_since = now_s();
-    // ---- one chunk of batched steps -------------------------------------
-    if (dirty) {
+    // ---- which resident jobs step in this chunk --------------------------
+    // FIFO: arrival order; SRPT: least remaining particle-steps first. Jobs
+    // are added until the particle cap is reached (at least one job).
+    std::vector<Job*> order = resident;
+    if (srpt)
+      std::stable_sort(order.begin(), order.end(), [](const Job* a, const Job* b) {
+        return (double)a->left * a->n < (double)b->left * b->n;
+      });
+    std::vector<Job*> pick;
+    size_t parts = 0;
+    for (Job* j : order) {
+      if (cap && !pick.empty() && parts + j->n > cap) continue;
+      pick.push_back(j);
+      parts += j->n;
+    }
+    if (pick != running || !batch) {
       if (batch) snow_batch_destroy(batch);
       batch = nullptr;
       std::vector<snow_scene*> sc;
-      for (Job* j : active) sc.push_back(j->scene);
+      for (Job* j : pick) sc.push_back(j->scene);
       snow_status s = snow_batch_create(ctx, sc.data(), (int)sc.size(), &batch);
       if (s != SNOW_OK) {
-        for (Job* j : active) {
+        for (Job* j : pick) {
           snow_scene_destroy(j->scene);
           j->scene = nullptr;
           finish(srv, j, s);
         }
-        active.clear();
+        std::vector<Job*> keep;
+        for (Job* j : resident)
+          if (j->scene) keep.push_back(j);
+        resident.swap(keep);
+        running.clear();
         continue;
       }
-      dirty = false;
+      running = pick;
     }
+    // ---- one chunk of batched steps -------------------------------------
     int k = chunk;
     std::vector<double> dts;
-    for (Job* j : active) {
+    for (Job* j : running) {
       k = std::min(k, j->left);
       dts.push_back(j->dt);
     }
     snow_status s = snow_batch_step(batch, dts.data(), k);
     if (s == SNOW_OK) s = snow_ctx_synchronize(ctx);
-    std::vector<Job*> still;
-    for (Job* j : active) {
+    bool retired = false;
+    for (Job* j : running) {
       j->left -= (s == SNOW_OK) ? k : j->left;
-      if (j->left > 0) {
-        still.push_back(j);
-        continue;
-      }
+      if (j->left > 0) continue;
       snow_status js = s;
       if (js == SNOW_OK) js = snow_scene_stats(j->scene, &j->result.stats);
       if (js == SNOW_OK && j->result.stats.nonfinite) js = SNOW_ENUMERIC;
@@ -212,11 +231,17 @@ void run(snow_server* srv) {
       }
       snow_scene_destroy(j->scene);
       j->scene = nullptr;
-      dirty = true;
+      retired = true;
       finish(srv, j, js);
     }
-    active.swap(still);
-    if (active.empty() && busy_since >= 0) {
+    if (retired) {
+      std::vector<Job*> keep;
+      for (Job* j : resident)
+        if (j->scene) keep.push_back(j);
+      resident.swap(keep);
+      running.clear();
+    }
+    if (resident.empty() && busy_since >= 0) {
       std::lock_guard<std::mutex> lock(srv->mu);
       srv->st.busy_s += now_s() - busy_since;
       busy_since = -1.0;

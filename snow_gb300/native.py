@@ -62,9 +62,12 @@ class SnowTuning(C.Structure):
                 ("steps_taken", C.c_int), ("ms_per_step", C.c_double)]
 
 
+SERVE_FIFO, SERVE_SRPT = 0, 1
+
+
 class SnowServerConfig(C.Structure):
     _fields_ = [("device", C.c_int), ("hbm_budget_bytes", C.c_size_t), ("max_active", C.c_int),
-                ("chunk_steps", C.c_int)]
+                ("chunk_steps", C.c_int), ("max_active_particles", C.c_size_t), ("policy", C.c_int)]
 
 
 class SnowJobDesc(C.Structure):

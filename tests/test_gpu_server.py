@@ -103,3 +103,31 @@ def test_admission_keeps_resident_state_within_the_budget():
         assert srv.stats()["resident_bytes"] <= budget
     finally:
         srv.close()
+
+
+@gpu
+@pytest.mark.parametrize("policy", ["fifo", "srpt"])
+def test_particle_cap_and_policy_order_the_jobs(policy):
+    """Under a particle cap that fits one job at a time, SRPT runs a short job
+    that arrives behind a long one first; FIFO finishes the long one first.
+    Both give the same results as the jobs alone."""
+    import time
+    from snow_gb300 import api
+    long_job = scenes.small_scene(n=12000, grid_edge=48, seed=221)
+    short_job = scenes.small_scene(n=3000, grid_edge=32, seed=222)
+    srv = api.Server(0, chunk_steps=8, max_active_particles=12000, policy=policy)
+    try:
+        a = srv.submit(long_job, steps=200, keep_state=True)
+        time.sleep(0.02)
+        b = srv.submit(short_job, steps=16, keep_state=True)
+        srv.drain(120.0)
+        res = {r["id"]: r for r in srv.poll()}
+        assert res[a]["status"] == 0 and res[b]["status"] == 0
+        if policy == "srpt":
+            assert res[b]["latency_s"] < res[a]["latency_s"]
+        else:
+            assert res[b]["latency_s"] > res[a]["latency_s"] - 0.02
+        _close(_alone(short_job, 16), srv.fetch(b, short_job.n))
+        _close(_alone(long_job, 200), srv.fetch(a, long_job.n), tol=5e-4)
+    finally:
+        srv.close()
