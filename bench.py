@@ -129,7 +129,21 @@ def kernels_per_step(n_colliders, sort_step, key_bits):
     return plain + 1 + passes * 5 + 4
 
 
-def bench_ours(args, local_rank):
+def reduce_max_ms(total_ms, dist_mod, device):
+    """Slowest rank's timed total (all ranks get it)."""
+    import torch
+    t = torch.tensor([float(total_ms)], dtype=torch.float64, device=device)
+    dist_mod.all_reduce(t, op=dist_mod.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(world, particles, steps, total_ms):
+    """Whole-job particle-steps/s of `world` replicas that each advance
+    `particles` particles by `steps` steps, timed by the slowest rank."""
+    return world * particles * steps / (total_ms * 1e-3)
+
+
+def bench_ours(args, local_rank, barrier=lambda: None):
     import torch
 
     from snow_gb300 import api, native as N, scenes
@@ -158,6 +172,7 @@ def bench_ours(args, local_rank):
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     with ClockSampler(local_rank) as clocks:
+        barrier()
         torch.cuda.synchronize()
         for i in range(args.steps):
             with torch.cuda.stream(stream):
@@ -167,6 +182,7 @@ def bench_ours(args, local_rank):
             with torch.cuda.stream(stream):
                 ends[i].record(stream)
         torch.cuda.synchronize()
+        barrier()
     step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
     total_ms = sum(step_ms)
     st = sim.stats()
@@ -544,20 +560,17 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(local_rank)
         dist.init_process_group("nccl")
-    res = bench_ours(args, local_rank)
+    res = bench_ours(args, local_rank, barrier=dist.barrier if dist is not None else (lambda: None))
     total_ms = res["total_ms"]
     if dist is not None:
-        import torch
-        t = torch.tensor([total_ms], device=f"cuda:{local_rank}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+        total_ms = reduce_max_ms(total_ms, dist, f"cuda:{local_rank}")
         dist.barrier()
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
         return 0
     n = res["n"]
-    value = world * n * args.steps / (total_ms * 1e-3)
+    value = replica_value(world, n, args.steps, total_ms)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,

@@ -299,3 +299,68 @@ def reference_scene(x, v=None, m=None) -> Scene:
     s.v = np.zeros((n, 3), np.float32) if v is None else np.asarray(v, np.float32).reshape(-1, 3)
     s.m = np.full(n, 1.25e-3, np.float32) if m is None else np.asarray(m, np.float32).reshape(-1)
     return s
+
+
+# ---- particles from files ---------------------------------------------------
+_FLOAT_PREFIX = None
+
+
+def _stof(text: str) -> float:
+    """std::stof: skip leading white space, convert the longest prefix that
+    reads as a float, raise ValueError when nothing converts."""
+    import re
+    global _FLOAT_PREFIX
+    if _FLOAT_PREFIX is None:
+        _FLOAT_PREFIX = re.compile(r"[+-]?(?:(?:\d+\.?\d*|\.\d+)(?:[eE][+-]?\d+)?|inf(?:inity)?|nan)",
+                                   re.IGNORECASE)
+    t = text.lstrip(" \t\n\v\f\r")
+    mt = _FLOAT_PREFIX.match(t)
+    if not mt:
+        raise ValueError(f"stof: no conversion of {text!r}")
+    return float(np.float32(float(mt.group(0))))
+
+
+def particles_from_xyz(path: str, pos=(0.0, 0.0, 0.0), scale=(1.0, 1.0, 1.0), mass: float = 6.25e-3):
+    """Particles from a text file with one `x,y,z` line per particle, as
+    ParticleSystem::initParticlesFromFile reads it (particlesystem.cpp:14-38):
+    position = scale * (x, y, z) + pos, velocity 0, mass 6.25e-3 each. Each
+    field converts like std::stof (a malformed line raises ValueError, where
+    the reference's stof throws); a line without a comma yields its one
+    number for x, y and z, as the reference's substr/erase arithmetic does.
+    A missing file is reported and yields no particles, like the reference.
+    Returns (x N x 3, v N x 3, m N) as float32."""
+    import os
+    import sys
+    if not os.path.exists(path):
+        print(f"Error: File {path} not found.", file=sys.stderr)
+        return np.zeros((0, 3), np.float32), np.zeros((0, 3), np.float32), np.zeros(0, np.float32)
+    pts = []
+    with open(path) as f:
+        for line in f:
+            line = line.rstrip("\n")
+            c = line.find(",")
+            x = _stof(line if c < 0 else line[:c])
+            line = line if c < 0 else line[c + 1:]
+            c = line.find(",")
+            y = _stof(line if c < 0 else line[:c])
+            line = line if c < 0 else line[c + 1:]
+            z = _stof(line)
+            pts.append((x, y, z))
+    xyz = np.asarray(pts, np.float32).reshape(-1, 3)
+    sc = np.asarray(scale, np.float32)
+    off = np.asarray(pos, np.float32)
+    x = (sc * xyz + off).astype(np.float32)
+    n = len(x)
+    return x, np.zeros((n, 3), np.float32), np.full(n, mass, np.float32)
+
+
+def add_particles(scene: Scene, x, v, m) -> Scene:
+    """Appends particles to a scene (the reference's ParticleSystem holds the
+    particles of every init call in one list)."""
+    def cat(a, b, shape):
+        b = np.asarray(b, np.float32).reshape(shape)
+        return b if a is None else np.concatenate([a, b])
+    scene.x = cat(scene.x, x, (-1, 3))
+    scene.v = cat(scene.v, v, (-1, 3))
+    scene.m = cat(scene.m, m, (-1,))
+    return scene
