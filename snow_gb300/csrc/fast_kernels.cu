@@ -525,17 +525,11 @@ __device__ __forceinline__ void advance_particle(const SceneDev& S, int p, const
   if (!finite) atomicAdd(&S.counters[CNT_NONFINITE], 1);
 }
 
-// Sums of the particles of one tile cell (list slots j0..j1) for the x-row
-// (b, c) of the cell's 4x4x4 stencil that this lane owns (sixteen lanes cover
-// a stencil), added to the shared tile at the end.
+// Adds the particles of one tile cell (list slots j0..j1) to this lane's
+// x-row (b, c) of the cell's 4x4x4 stencil: acc[a] holds node x = lx + a.
 template <bool MASS_ONLY>
-__device__ __forceinline__ void cell_run(ItemShared& sh, int ci, int j0, int j1, int b, int c) {
-  constexpr int nf = MASS_ONLY ? 1 : kAccFields;
-  float acc[4][kAccFields];
-#pragma unroll
-  for (int a = 0; a < 4; a++)
-#pragma unroll
-    for (int f = 0; f < kAccFields; f++) acc[a][f] = 0.0f;
+__device__ __forceinline__ void cell_sums(const ItemShared& sh, int j0, int j1, int b, int c,
+                                          float (&acc)[4][kAccFields]) {
   for (int j = j0; j < j1; j++) {
     const float4* d = sh.pd[sh.plist[j]];
     const float* df = reinterpret_cast<const float*>(d);
@@ -570,12 +564,25 @@ __device__ __forceinline__ void cell_run(ItemShared& sh, int ci, int j0, int j1,
       }
     }
   }
+}
+
+// Adds the 4 nodes of this lane's row (tile nodes t0 .. t0 + 3) to the
+// shared tile and clears them.
+template <int NF>
+__device__ __forceinline__ void row_flush(ItemShared& sh, int t0, float (&acc)[4][kAccFields]) {
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+#pragma unroll
+    for (int f = 0; f < NF; f++) {
+      atomicAdd(&sh.tile[f * kTile3 + t0 + a], acc[a][f]);
+      acc[a][f] = 0.0f;
+    }
+  }
+}
+
+__device__ __forceinline__ int cell_row_node(int ci, int b, int c) {
   const int lx = ci % kCellsPerAxis, ly = (ci / kCellsPerAxis) % kCellsPerAxis, lz = ci / (kCellsPerAxis * kCellsPerAxis);
-  const int t0 = lx + kTile * (ly + b) + kTile * kTile * (lz + c);
-#pragma unroll
-  for (int a = 0; a < 4; a++)
-#pragma unroll
-    for (int f = 0; f < nf; f++) atomicAdd(&sh.tile[f * kTile3 + t0 + a], acc[a][f]);
+  return lx + kTile * (ly + b) + kTile * kTile * (lz + c);
 }
 
 // P2G of the item's particles into acc (every thread of the CTA calls it;
@@ -658,15 +665,44 @@ __device__ __forceinline__ void p2g_tile_pass(ItemShared& sh, const SceneDev& S,
   if (my_cell >= 0) sh.plist[sh.cstart[my_cell] + my_rank] = (short)threadIdx.x;
   __syncthreads();
   {
-    // half-warp h takes occupied cells h, h + 16, ...: the two halves of a
-    // warp get neighbouring cells, whose particle counts are alike
+    // half-warp h takes a contiguous slice of the occupied-cell list (the
+    // two halves of a warp get neighbouring slices, whose particle counts
+    // are alike). Cells of a slice often follow each other along x: the
+    // row's sums then slide one node instead of being flushed, so only the
+    // node that leaves the window goes to the shared tile.
+    constexpr int NF = MASS_ONLY ? 1 : kAccFields;
     const int hw = threadIdx.x >> 4, l16 = threadIdx.x & 15;
+    const int b = l16 & 3, c = l16 >> 2;
     const int nhw = blockDim.x >> 4;
     const int ncells = sh.ncells;
-    for (int k = hw; k < ncells; k += nhw) {
+    const int k0 = (ncells * hw) / nhw, k1 = (ncells * (hw + 1)) / nhw;
+    float acc[4][kAccFields];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+      for (int f = 0; f < kAccFields; f++) acc[a][f] = 0.0f;
+    int cur = -1;
+    for (int k = k0; k < k1; k++) {
       const int ci = sh.cells[k];
-      cell_run<MASS_ONLY>(sh, ci, sh.cstart[ci], sh.cstart[ci + 1], l16 & 3, l16 >> 2);
+      if (cur >= 0) {
+        if (ci == cur + 1 && ci % kCellsPerAxis != 0) {
+          // only node 0 leaves the window: flush it, slide the rest
+#pragma unroll
+          for (int f = 0; f < NF; f++) {
+            atomicAdd(&sh.tile[f * kTile3 + cell_row_node(cur, b, c)], acc[0][f]);
+            acc[0][f] = acc[1][f];
+            acc[1][f] = acc[2][f];
+            acc[2][f] = acc[3][f];
+            acc[3][f] = 0.0f;
+          }
+        } else {
+          row_flush<NF>(sh, cell_row_node(cur, b, c), acc);
+        }
+      }
+      cell_sums<MASS_ONLY>(sh, sh.cstart[ci], sh.cstart[ci + 1], b, c, acc);
+      cur = ci;
     }
+    if (cur >= 0) row_flush<NF>(sh, cell_row_node(cur, b, c), acc);
   }
   __syncthreads();
   between();
