@@ -158,10 +158,16 @@ def bench_ours(args, local_rank, barrier=lambda: None):
     sim.upload().init()
     n = s.n
     dt = s.dt
-    # work split chosen by the autotuner (on real steps of this scene)
-    tb = api.Batch(ctx, [sim])
-    tuning = tb.autotune([dt])
-    tb.close()
+    # work split chosen by the autotuner (on real steps of this scene), or
+    # given with --tuning
+    if args.tuning:
+        si, im, cp = (int(v) for v in args.tuning.split(","))
+        sim.set_tuning(si, im, cp)
+        tuning = dict(sort_interval=si, items_max=im, ctas_per_sm=cp, steps_taken=0)
+    else:
+        tb = api.Batch(ctx, [sim])
+        tuning = tb.autotune([dt])
+        tb.close()
     # active grid nodes (nodes with mass) after one step, for the roofline
     sim.step(dt, 1)
     ctx.synchronize()
@@ -218,15 +224,33 @@ def bench_ours(args, local_rank, barrier=lambda: None):
 
     # end to end through the C ABI: upload from host arrays, init, per step
     # one step + a device->host read of the step's bulk statistics, download.
+    # inputs and outputs in pinned host memory, filled before the clock starts
     e2e_steps = args.steps
+
+    def pinned(*shape):
+        return torch.empty(shape, dtype=torch.float32, pin_memory=True).numpy()
+
+    hx, hv, hm = pinned(n, 3), pinned(n, 3), pinned(n)
+    hx[:], hv[:], hm[:] = s.x, s.v, s.m
+    hout = dict(x=pinned(n, 3), v=pinned(n, 3), FE=pinned(n, 3, 3), Jp=pinned(n), volume=pinned(n))
+    split = {}
     t1 = time.perf_counter()
     sim2 = api.SimScene(ctx, s, mode=N.MODE_FAST)
-    sim2.upload().init().set_tuning(tuning["sort_interval"], tuning["items_max"], tuning["ctas_per_sm"])
+    sim2.set_tuning(tuning["sort_interval"], tuning["items_max"], tuning["ctas_per_sm"])
+    t = time.perf_counter()
+    split["create_ms"] = 1e3 * (t - t1)
+    sim2.upload(hx, hv, hm).init()
+    ctx.synchronize()
+    t2 = time.perf_counter()
+    split["upload_init_ms"] = 1e3 * (t2 - t)
     for _ in range(e2e_steps):
         sim2.step(dt, 1)
         sim2.stats()
-    out = sim2.download()
+    t3 = time.perf_counter()
+    split["steps_ms"] = 1e3 * (t3 - t2)
+    out = sim2.download(out=hout)
     e2e_s = time.perf_counter() - t1
+    split["download_ms"] = 1e3 * (time.perf_counter() - t3)
     h2d = n * (12 + 12 + 4)
     d2h_stats = 8 * 20
     d2h_final = n * (12 + 12 + 36 + 4 + 4)
@@ -242,7 +266,7 @@ def bench_ours(args, local_rank, barrier=lambda: None):
                                                kernels_per_step(len(s.colliders), False, key_bits))
     res = dict(total_ms=total_ms, step_ms=step_ms, n=n, A=A, per=per, dominant=dominant, alg_bytes=alg_bytes,
                achieved=achieved, peak=peak, peak_kind=peak_kind, clocks=clocks.summary(), e2e_s=e2e_s,
-               e2e_steps=e2e_steps, h2d=h2d, d2h=d2h_stats + d2h_final / e2e_steps, launches=launches,
+               e2e_steps=e2e_steps, e2e_split=split, h2d=h2d, d2h=d2h_stats + d2h_final / e2e_steps, launches=launches,
                gen_s=gen_s, stats=st, scene=s, tuning=tuning)
     ctx.close()
     return res
@@ -502,6 +526,7 @@ def main():
     ap.add_argument("--grid", type=int, default=256)
     ap.add_argument("--ref-sample", type=int, default=32768)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--tuning", default="", help="SORT_INTERVAL,ITEMS_MAX,CTAS_PER_SM instead of autotuning")
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=16)
     ap.add_argument("--no-batched", action="store_true")
@@ -587,7 +612,9 @@ def main():
         "clocks": res["clocks"],
         "e2e": {"value": n * res["e2e_steps"] / res["e2e_s"], "unit": UNIT,
                 "h2d_bytes_per_step": res["h2d"] / res["e2e_steps"], "d2h_bytes_per_step": res["d2h"],
-                "note": "upload + init + per-step (step + stats read) + download through the C ABI"},
+                "note": "scene create + upload from pinned host memory + init + per step (step + statistics "
+                        "read) + download into pinned host memory, through the C ABI",
+                "split_ms": res["e2e_split"]},
         "gpu_launches": res["launches"],
         "step_ms_p50": statistics.median(res["step_ms"]), "step_ms_max": max(res["step_ms"]),
     }

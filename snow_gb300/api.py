@@ -163,10 +163,19 @@ class SimScene:
         return self
 
     # -- data out ----------------------------------------------------------
-    def download(self, fp: bool = False):
+    def download(self, fp: bool = False, out: Optional[dict] = None):
+        """Particle state in upload order. `out` may hold preallocated
+        float32 arrays x, v (N x 3), FE (N x 3 x 3), Jp, volume (N) -- e.g.
+        views of pinned host memory -- which are filled and returned."""
         n = self.n
-        x, v = np.zeros((n, 3), np.float32), np.zeros((n, 3), np.float32)
-        fe, jp, vol = np.zeros((n, 3, 3), np.float32), np.zeros(n, np.float32), np.zeros(n, np.float32)
+        if out is not None:
+            x, v, fe, jp, vol = out["x"], out["v"], out["FE"], out["Jp"], out["volume"]
+            for a in (x, v, fe, jp, vol):
+                if a.dtype != np.float32 or not a.flags.c_contiguous or a.size * 4 != a.nbytes or len(a) != n:
+                    raise ValueError("download: out arrays must be C-contiguous float32 with N rows")
+        else:
+            x, v = np.zeros((n, 3), np.float32), np.zeros((n, 3), np.float32)
+            fe, jp, vol = np.zeros((n, 3, 3), np.float32), np.zeros(n, np.float32), np.zeros(n, np.float32)
         fpa = np.zeros((n, 3, 3), np.float32) if fp else None
         self.ctx.check(self.L.snow_scene_download(self.h, N.ptr(x), N.ptr(v), N.ptr(fe), N.ptr(fpa), N.ptr(jp),
                                                   N.ptr(vol)))

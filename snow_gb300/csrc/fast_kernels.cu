@@ -1102,6 +1102,71 @@ __global__ void __launch_bounds__(256) k_stats(const SceneDev* __restrict__ sd, 
   stats_commit(t, out);
 }
 
+// Upload: the caller's arrays (x, v: N x 3; m: N; FE, FP: N x 9 row-major or
+// null for identity), copied to the device as they are, packed into the
+// particle streams. J_p = det F_P in double without contraction, as the
+// host formerly computed it.
+__global__ void __launch_bounds__(256) k_pack(const float* __restrict__ x, const float* __restrict__ v,
+                                              const float* __restrict__ m, const float* __restrict__ FE,
+                                              const float* __restrict__ FP, size_t n, float4* xm, float4* vv,
+                                              float4* fa, float4* fb, float2* fc, uint32_t* pid) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    xm[i] = make_float4(x[3 * i], x[3 * i + 1], x[3 * i + 2], m[i]);
+    vv[i] = make_float4(v[3 * i], v[3 * i + 1], v[3 * i + 2], 0.0f);
+    float F[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    if (FE)
+#pragma unroll
+      for (int k = 0; k < 9; k++) F[k] = FE[9 * i + k];
+    fa[i] = make_float4(F[0], F[3], F[6], F[1]);
+    fb[i] = make_float4(F[4], F[7], F[2], F[5]);
+    float jp = 1.0f;
+    if (FP) {
+      const float* f = FP + 9 * i;
+      const double a = f[0], b = f[1], c = f[2], d = f[3], e = f[4], g = f[5], h = f[6], ii = f[7], j = f[8];
+      const double t0 = __dsub_rn(__dmul_rn(e, j), __dmul_rn(g, ii));
+      const double t1 = __dsub_rn(__dmul_rn(d, j), __dmul_rn(g, h));
+      const double t2 = __dsub_rn(__dmul_rn(d, ii), __dmul_rn(e, h));
+      jp = (float)__dadd_rn(__dsub_rn(__dmul_rn(a, t0), __dmul_rn(b, t1)), __dmul_rn(c, t2));
+    }
+    fc[i] = make_float2(F[8], jp);
+    pid[i] = (uint32_t)i;
+  }
+}
+
+// Download: the particle streams back to the caller's layout and order
+// (slot i holds upload index pid[i]); any output may be null.
+__global__ void __launch_bounds__(256) k_unpack(const SceneDev* __restrict__ sd, size_t n, float* x, float* v,
+                                                float* FE, float* Jp, float* volume) {
+  const SceneDev& S = *sd;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t j = S.pid[i];
+    if (j >= n) continue;  // cannot happen: pid is a permutation
+    const float4 xm = S.xm[i], vv = S.vv[i];
+    if (x) {
+      x[3 * j] = xm.x;
+      x[3 * j + 1] = xm.y;
+      x[3 * j + 2] = xm.z;
+    }
+    if (v) {
+      v[3 * j] = vv.x;
+      v[3 * j + 1] = vv.y;
+      v[3 * j + 2] = vv.z;
+    }
+    const float2 c = S.fc[i];
+    if (FE) {
+      // fa = (m00, m01, m02, m10), fb = (m11, m12, m20, m21), fc = (m22, Jp); m[c][r]
+      const float4 a = S.fa[i], b = S.fb[i];
+      const float mcr[9] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x};
+#pragma unroll
+      for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int q = 0; q < 3; q++) FE[9 * j + 3 * r + q] = mcr[3 * q + r];
+    }
+    if (Jp) Jp[j] = c.y;
+    if (volume) volume[j] = vv.w;
+  }
+}
+
 // Dense copies of the P2G sums (acc) and of v* (pool) of the active blocks.
 __global__ void k_download_grid(const SceneDev* __restrict__ sd, float* mass, float* mom, float* force, float* vstar) {
   const SceneDev& S = *sd;
@@ -1226,6 +1291,22 @@ void fast_stats(const SceneDev* sd_dev, int n, StatsAccum* out_dev, cudaStream_t
   int g = (n + 255) / 256;
   if (g > num_sms() * 2) g = num_sms() * 2;
   k_stats<<<g, 256, 0, st>>>(sd_dev, n, out_dev);
+}
+
+void fast_pack(const float* x, const float* v, const float* m, const float* FE, const float* FP, size_t n,
+               const SceneDev& sd, cudaStream_t st) {
+  if (n == 0) return;
+  size_t g = (n + 255) / 256;
+  if (g > (size_t)num_sms() * 8) g = (size_t)num_sms() * 8;
+  k_pack<<<(int)g, 256, 0, st>>>(x, v, m, FE, FP, n, sd.xm, sd.vv, sd.fa, sd.fb, sd.fc, sd.pid);
+}
+
+void fast_unpack(const SceneDev* sd_dev, size_t n, float* x, float* v, float* FE, float* Jp, float* volume,
+                 cudaStream_t st) {
+  if (n == 0) return;
+  size_t g = (n + 255) / 256;
+  if (g > (size_t)num_sms() * 8) g = (size_t)num_sms() * 8;
+  k_unpack<<<(int)g, 256, 0, st>>>(sd_dev, n, x, v, FE, Jp, volume);
 }
 
 void fast_download_grid(const SceneDev* sd_dev, float* mass, float* mom, float* force, float* vstar,

@@ -27,6 +27,9 @@ struct snow_ctx {
   std::string err;
   bool profiling = false;
   bool graphs = true;  // replay each step as a captured CUDA graph
+  // device memory of scenes and batches comes from this pool, which keeps
+  // freed blocks for reuse (scenes of a serving loop come and go)
+  cudaMemPool_t pool = nullptr;
   StatsAccum* d_stats = nullptr;
   StatsAccum* h_stats = nullptr;  // pinned
   int* h_counters = nullptr;      // pinned, kCounterStride ints
@@ -115,11 +118,13 @@ snow_status dalloc(snow_ctx* ctx, std::vector<std::pair<void*, size_t>>& owner, 
   bytes = (bytes + 255) & ~(size_t)255;
   if (ctx->budget && ctx->used + bytes > ctx->budget)
     return fail(ctx, SNOW_EBUDGET, "HBM budget exceeded");
-  const cudaError_t e = cudaMalloc(out, bytes);
+  // stream-ordered, then waited for, so the memory is usable from any stream
+  cudaError_t e = cudaMallocFromPoolAsync(out, bytes, ctx->pool, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) {
     cudaGetLastError();
     *out = nullptr;
-    return fail(ctx, SNOW_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return fail(ctx, SNOW_ENOMEM, std::string("cudaMallocFromPoolAsync: ") + cudaGetErrorString(e));
   }
   ctx->used += bytes;
   owner_bytes += bytes;
@@ -129,7 +134,7 @@ snow_status dalloc(snow_ctx* ctx, std::vector<std::pair<void*, size_t>>& owner, 
 
 void dfree_all(snow_ctx* ctx, std::vector<std::pair<void*, size_t>>& owner, size_t& owner_bytes) {
   for (auto& a : owner) {
-    cudaFree(a.first);
+    cudaFreeAsync(a.first, ctx->stream);
     ctx->used -= a.second;
   }
   owner.clear();
@@ -139,7 +144,7 @@ void dfree_all(snow_ctx* ctx, std::vector<std::pair<void*, size_t>>& owner, size
 void dfree_one(snow_ctx* ctx, snow_scene* s, void* p) {
   for (size_t i = 0; i < s->allocs.size(); i++)
     if (s->allocs[i].first == p) {
-      cudaFree(p);
+      cudaFreeAsync(p, ctx->stream);
       ctx->used -= s->allocs[i].second;
       s->bytes -= s->allocs[i].second;
       s->allocs.erase(s->allocs.begin() + (long)i);
@@ -487,6 +492,17 @@ snow_status snow_ctx_create(int device, size_t hbm_budget_bytes, snow_ctx** out)
   ctx->budget = hbm_budget_bytes;
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    e = cudaMemPoolCreate(&ctx->pool, &props);
+  }
+  if (e == cudaSuccess) {
+    uint64_t keep = UINT64_MAX;  // hold freed memory until the context goes
+    e = cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
   if (e == cudaSuccess) e = cudaMalloc(&ctx->d_stats, sizeof(StatsAccum));
   if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_stats, sizeof(StatsAccum));
   if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_counters, kCounterStride * sizeof(int));
@@ -510,7 +526,11 @@ void snow_ctx_destroy(snow_ctx* ctx) {
   if (ctx->d_stats) cudaFree(ctx->d_stats);
   if (ctx->h_stats) cudaFreeHost(ctx->h_stats);
   if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
-  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->stream) {
+    cudaStreamSynchronize(ctx->stream);  // pending frees into the pool
+    cudaStreamDestroy(ctx->stream);
+  }
+  if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
   delete ctx;
 }
 
@@ -543,10 +563,11 @@ size_t snow_scene_footprint(const snow_params* p, size_t n) {
   // + binning scratch (2 key + 2 value words, 4 x 16 B + 8 B + 4 B permutation
   // targets, radix histograms) + work items (16 B each) + per block the dense
   // P2G sums (448 floats), flags, slot and bin tables (5 ints) + the output
-  // pool at its largest (every block: 384 floats + 1 int).
+  // pool at its largest (every block: 384 floats + 1 int) + the upload's
+  // staging copy of the caller's arrays (x, v, m, F_E, F_P: 100 B).
   const double tiles = (double)radix_tiles(n);
   const double items = (double)n / kMinItemMax + std::min((double)n, nb) + 1;
-  return (size_t)(n * (76.0 + 92.0) + tiles * 256 * 4.0 + 4096.0 + items * 16.0 + nb * (448 * 4.0 + 5 * 4.0) +
+  return (size_t)(n * (76.0 + 92.0 + 100.0) + tiles * 256 * 4.0 + 4096.0 + items * 16.0 + nb * (448 * 4.0 + 5 * 4.0) +
                   nb * (384 * 4.0 + 4.0) + 1024.0);
 }
 
@@ -639,20 +660,35 @@ snow_status snow_scene_upload(snow_scene* s, const float* x, const float* v, con
     s->uploaded = true;
     return SNOW_OK;
   }
-  std::vector<float4> xm(n), vv(n), fa(n), fb(n);
-  std::vector<float2> fc(n);
-  static const float I[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
-  for (size_t i = 0; i < n; i++) {
-    xm[i] = make_float4(x[3 * i], x[3 * i + 1], x[3 * i + 2], m[i]);
-    vv[i] = make_float4(v[3 * i], v[3 * i + 1], v[3 * i + 2], 0.0f);
-    const float* F = FE ? FE + 9 * i : I;
-    fa[i] = make_float4(F[0], F[3], F[6], F[1]);
-    fb[i] = make_float4(F[4], F[7], F[2], F[5]);
-    fc[i] = make_float2(F[8], FP ? (float)det_rowmajor(FP + 9 * i) : 1.0f);
-  }
+  // the caller's arrays go to a staging buffer as they are (one copy each,
+  // straight from pinned memory when the caller's is) and are packed into
+  // the particle streams on the device
   s->sd.n = (int)n;
-  st = fast_upload_soa(s, xm, vv, fa, fb, fc);
-  if (st) return st;
+  if (n > 0) {
+    const size_t words = n * (3 + 3 + 1 + (FE ? 9 : 0) + (FP ? 9 : 0));
+    std::vector<std::pair<void*, size_t>> tmp;
+    size_t tmp_bytes = 0;
+    float* stage = nullptr;
+    st = dalloc(ctx, tmp, tmp_bytes, words * sizeof(float), (void**)&stage);
+    if (st) return st;
+    float* dx = stage;
+    float* dv = dx + 3 * n;
+    float* dm = dv + 3 * n;
+    float* dfe = FE ? dm + n : nullptr;
+    float* dfp = FP ? (FE ? dfe + 9 * n : dm + n) : nullptr;
+    cudaError_t e = cudaMemcpyAsync(dx, x, 3 * n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dv, v, 3 * n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dm, m, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess && FE) e = cudaMemcpyAsync(dfe, FE, 9 * n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess && FP) e = cudaMemcpyAsync(dfp, FP, 9 * n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) {
+      fast_pack(dx, dv, dm, dfe, dfp, n, s->sd, ctx->stream);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);  // the caller may reuse its arrays
+    dfree_all(ctx, tmp, tmp_bytes);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "snow_scene_upload");
+  }
   s->uploaded = true;
   return SNOW_OK;
 }
@@ -929,37 +965,37 @@ snow_status snow_scene_download(snow_scene* s, float* x, float* v, float* FE, fl
     return SNOW_OK;
   }
   if (FP) return fail(ctx, SNOW_EUNSUPPORTED, "F_P is not kept in SNOW_MODE_FAST (J_p is)");
-  std::vector<float4> xm(n), vv(n), fa(n), fb(n);
-  std::vector<float2> fc(n);
-  std::vector<uint32_t> pid(n);
-  CK(cudaMemcpy(xm.data(), s->sd.xm, n * sizeof(float4), cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(vv.data(), s->sd.vv, n * sizeof(float4), cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(fa.data(), s->sd.fa, n * sizeof(float4), cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(fb.data(), s->sd.fb, n * sizeof(float4), cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(fc.data(), s->sd.fc, n * sizeof(float2), cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(pid.data(), s->sd.pid, n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
-  for (size_t i = 0; i < n; i++) {
-    const size_t j = pid[i];
-    if (j >= n) return fail(ctx, SNOW_ECUDA, "corrupt particle index stream");
-    if (x) {
-      x[3 * j] = xm[i].x;
-      x[3 * j + 1] = xm[i].y;
-      x[3 * j + 2] = xm[i].z;
-    }
-    if (v) {
-      v[3 * j] = vv[i].x;
-      v[3 * j + 1] = vv[i].y;
-      v[3 * j + 2] = vv[i].z;
-    }
-    if (FE) {
-      // fa = (m00, m01, m02, m10), fb = (m11, m12, m20, m21), fc = (m22, Jp); m[c][r]
-      const float mcr[9] = {fa[i].x, fa[i].y, fa[i].z, fa[i].w, fb[i].x, fb[i].y, fb[i].z, fb[i].w, fc[i].x};
-      for (int r = 0; r < 3; r++)
-        for (int c = 0; c < 3; c++) FE[9 * j + 3 * r + c] = mcr[3 * c + r];
-    }
-    if (Jp) Jp[j] = fc[i].y;
-    if (volume) volume[j] = vv[i].w;
-  }
+  if (n == 0) return SNOW_OK;
+  // unpacked on the device into upload order, then one copy per requested
+  // array straight into the caller's memory (a DMA when it is pinned)
+  const size_t words = n * ((x ? 3 : 0) + (v ? 3 : 0) + (FE ? 9 : 0) + (Jp ? 1 : 0) + (volume ? 1 : 0));
+  if (words == 0) return SNOW_OK;
+  std::vector<std::pair<void*, size_t>> tmp;
+  size_t tmp_bytes = 0;
+  float* stage = nullptr;
+  snow_status st = dalloc(ctx, tmp, tmp_bytes, words * sizeof(float), (void**)&stage);
+  if (st) return st;
+  float* p = stage;
+  float* dx = x ? p : nullptr;
+  p += x ? 3 * n : 0;
+  float* dv = v ? p : nullptr;
+  p += v ? 3 * n : 0;
+  float* dfe = FE ? p : nullptr;
+  p += FE ? 9 * n : 0;
+  float* djp = Jp ? p : nullptr;
+  p += Jp ? n : 0;
+  float* dvol = volume ? p : nullptr;
+  fast_unpack(s->sd_dev, n, dx, dv, dfe, djp, dvol, ctx->stream);
+  cudaError_t e = cudaGetLastError();
+  const std::pair<float*, float*> out[5] = {{x, dx}, {v, dv}, {FE, dfe}, {Jp, djp}, {volume, dvol}};
+  const size_t width[5] = {3, 3, 9, 1, 1};
+  for (int k = 0; k < 5 && e == cudaSuccess; k++)
+    if (out[k].first)
+      e = cudaMemcpyAsync(out[k].first, out[k].second, width[k] * n * sizeof(float), cudaMemcpyDeviceToHost,
+                          ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  dfree_all(ctx, tmp, tmp_bytes);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "snow_scene_download");
   return SNOW_OK;
 }
 

@@ -160,6 +160,10 @@ struct StatsAccum {
 void fast_stats(const SceneDev* sd_dev, int n, StatsAccum* out_dev, cudaStream_t st);
 void ref_stats(const RefArgs& a, StatsAccum* out_dev, cudaStream_t st);
 void fast_download_grid(const SceneDev* sd_dev, float* mass, float* mom, float* force, float* vstar, cudaStream_t st);
+void fast_pack(const float* x, const float* v, const float* m, const float* FE, const float* FP, size_t n,
+               const SceneDev& sd, cudaStream_t st);
+void fast_unpack(const SceneDev* sd_dev, size_t n, float* x, float* v, float* FE, float* Jp, float* volume,
+                 cudaStream_t st);
 
 int num_sms();
 
