@@ -278,7 +278,6 @@ struct ItemShared {
   int nrows;
   short cells[kCells];               // occupied tile cells
   int ncells;
-  int touched[27];                   // tile blocks that received P2G sums
   int4 item_q[2];                    // this and the next work item of the CTA
   int scene_q[2];                    // ... and their scenes
   int next_slots[27];                // pool slots of the next item's tile blocks
@@ -366,7 +365,6 @@ __device__ __forceinline__ void tile_zero(ItemShared& sh, int nf) {
 __device__ __forceinline__ void tile_init(ItemShared& sh) {
   for (int i = threadIdx.x; i < kCells; i += blockDim.x) sh.ccount[i] = 0;
   if (threadIdx.x == 32) sh.nrows = 0;
-  if (threadIdx.x < 27) sh.touched[threadIdx.x] = 0;
   if (threadIdx.x == 0) mbar_init(&sh.bar, 1);
   __syncthreads();
 }
@@ -487,7 +485,10 @@ __device__ __forceinline__ void advance_particle(const SceneDev& S, int p, const
     for (int r = 0; r < 3; r++) step.m[c][r] = (c == r ? 1.0f : 0.0f) + S.dt * L[r][c];
   const M3 fe_trial = m3_mul(step, FE);
   M3 W, Sg, V;
-  svd3<false>(fe_trial, W, Sg, V);
+  const float4 q4 = S.vq[p];
+  float q[4] = {q4.x, q4.y, q4.z, q4.w};
+  svd3_warm(fe_trial, q, W, Sg, V);
+  S.vq[p] = make_float4(q[0], q[1], q[2], q[3]);
   float ratio = 1.0f;
 #pragma unroll
   for (int i = 0; i < 3; i++) {
@@ -596,7 +597,8 @@ __device__ __forceinline__ int cell_row_node(int ci, int b, int c) {
 //      x-row (b, c) = (l & 3, l >> 2) of the cell's stencil over the cell's
 //      particles in registers and adds the row to the shared tile;
 //   4. the tile's non-empty nodes are added to acc (row by row, vector
-//      atomics) and their blocks flagged.
+//      atomics) and their blocks flagged. The caller separates this item's
+//      flush from the next item's use of the tile with a barrier.
 // `between` runs between steps 3 and 4, long after the staged G2P tile was
 // last read (the fused kernel issues the next item's copies there).
 template <bool MASS_ONLY, class Between>
@@ -633,6 +635,7 @@ __device__ __forceinline__ void p2g_tile_pass(ItemShared& sh, const SceneDev& S,
     d[9] = make_float4(w.gz[0], w.gz[1], w.gz[2], w.gz[3]);
   }
   __syncthreads();  // counts and P2G data done
+  if (threadIdx.x == 32) sh.nrows = 0;  // the previous item's flush is long done
   // exclusive scan of the cell counts and list of the occupied cells, one
   // cell per thread
   const int t = threadIdx.x;
@@ -737,31 +740,23 @@ __device__ __forceinline__ void p2g_tile_pass(ItemShared& sh, const SceneDev& S,
 #pragma unroll
     for (int x = 0; x < kTile; x++) v[x] = ((mask >> x) & 1u) ? row[x] : 0.0f;
     const int g1 = oy + r % kTile, g2 = oz + r / kTile;
-    const int kyz = 3 * ((g1 >> 2) - by + 1) + 9 * ((g2 >> 2) - bz + 1);
     float* base = S.acc + f * kBlockNodes + 4 * (g1 & 3) + 16 * (g2 & 3);
     if (mask & 0x3u) {
       const int blk = block_id(S, bx - 1, g1 >> 2, g2 >> 2);
       atomicAdd(reinterpret_cast<float2*>(base + (size_t)blk * kAccBlockFloats + 2), make_float2(v[0], v[1]));
-      if (f == 0) sh.touched[kyz] = 1;
+      if (f == 0) S.blk_flag[blk] = 1;
     }
     if (mask & 0x3cu) {
       const int blk = block_id(S, bx, g1 >> 2, g2 >> 2);
       atomicAdd(reinterpret_cast<float4*>(base + (size_t)blk * kAccBlockFloats), make_float4(v[2], v[3], v[4], v[5]));
-      if (f == 0) sh.touched[kyz + 1] = 1;
+      if (f == 0) S.blk_flag[blk] = 1;
     }
     if (mask & 0x1c0u) {
       const int blk = block_id(S, bx + 1, g1 >> 2, g2 >> 2);
       atomicAdd(reinterpret_cast<float4*>(base + (size_t)blk * kAccBlockFloats), make_float4(v[6], v[7], v[8], 0.0f));
-      if (f == 0) sh.touched[kyz + 2] = 1;
+      if (f == 0) S.blk_flag[blk] = 1;
     }
   }
-  __syncthreads();
-  if (threadIdx.x < 27 && sh.touched[threadIdx.x]) {
-    const int k = threadIdx.x;
-    sh.touched[k] = 0;
-    S.blk_flag[block_id(S, bx - 1 + k % 3, by - 1 + (k / 3) % 3, bz - 1 + k / 9)] = 1;
-  }
-  if (threadIdx.x == 32) sh.nrows = 0;
 }
 
 // ===========================================================================
@@ -1109,7 +1104,7 @@ __global__ void __launch_bounds__(256) k_stats(const SceneDev* __restrict__ sd, 
 __global__ void __launch_bounds__(256) k_pack(const float* __restrict__ x, const float* __restrict__ v,
                                               const float* __restrict__ m, const float* __restrict__ FE,
                                               const float* __restrict__ FP, size_t n, float4* xm, float4* vv,
-                                              float4* fa, float4* fb, float2* fc, uint32_t* pid) {
+                                              float4* fa, float4* fb, float2* fc, uint32_t* pid, float4* vq) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     xm[i] = make_float4(x[3 * i], x[3 * i + 1], x[3 * i + 2], m[i]);
     vv[i] = make_float4(v[3 * i], v[3 * i + 1], v[3 * i + 2], 0.0f);
@@ -1130,6 +1125,7 @@ __global__ void __launch_bounds__(256) k_pack(const float* __restrict__ x, const
     }
     fc[i] = make_float2(F[8], jp);
     pid[i] = (uint32_t)i;
+    vq[i] = make_float4(1.0f, 0.0f, 0.0f, 0.0f);  // no previous SVD: identity frame
   }
 }
 
@@ -1298,7 +1294,7 @@ void fast_pack(const float* x, const float* v, const float* m, const float* FE, 
   if (n == 0) return;
   size_t g = (n + 255) / 256;
   if (g > (size_t)num_sms() * 8) g = (size_t)num_sms() * 8;
-  k_pack<<<(int)g, 256, 0, st>>>(x, v, m, FE, FP, n, sd.xm, sd.vv, sd.fa, sd.fb, sd.fc, sd.pid);
+  k_pack<<<(int)g, 256, 0, st>>>(x, v, m, FE, FP, n, sd.xm, sd.vv, sd.fa, sd.fb, sd.fc, sd.pid, sd.vq);
 }
 
 void fast_unpack(const SceneDev* sd_dev, size_t n, float* x, float* v, float* FE, float* Jp, float* volume,

@@ -215,7 +215,8 @@ snow_status fast_alloc_particles(snow_scene* s, size_t cap) {
   SceneDev& d = s->sd;
   snow_status st;
   if ((st = salloc(s, cap, &d.xm)) || (st = salloc(s, cap, &d.vv)) || (st = salloc(s, cap, &d.fa)) ||
-      (st = salloc(s, cap, &d.fb)) || (st = salloc(s, cap, &d.fc)) || (st = salloc(s, cap, &d.pid)))
+      (st = salloc(s, cap, &d.fb)) || (st = salloc(s, cap, &d.fc)) || (st = salloc(s, cap, &d.pid)) ||
+      (st = salloc(s, cap, &d.vq)))
     return st;
   BinScratch& b = s->bin;
   const size_t tiles = radix_tiles(cap);
@@ -224,7 +225,8 @@ snow_status fast_alloc_particles(snow_scene* s, size_t cap) {
   if ((st = salloc(s, cap, &b.keys[0])) || (st = salloc(s, cap, &b.keys[1])) || (st = salloc(s, cap, &b.vals[0])) ||
       (st = salloc(s, cap, &b.vals[1])) || (st = salloc(s, hist, &b.hist)) || (st = salloc(s, partial, &b.scan_tmp)) ||
       (st = salloc(s, cap, &b.tmp4[0])) || (st = salloc(s, cap, &b.tmp4[1])) || (st = salloc(s, cap, &b.tmp4[2])) ||
-      (st = salloc(s, cap, &b.tmp4[3])) || (st = salloc(s, cap, &b.tmp2)) || (st = salloc(s, cap, &b.tmp_pid)))
+      (st = salloc(s, cap, &b.tmp4[3])) || (st = salloc(s, cap, &b.tmp4[4])) || (st = salloc(s, cap, &b.tmp2)) ||
+      (st = salloc(s, cap, &b.tmp_pid)))
     return st;
   b.n_cap = cap;
   d.item_cap = (int)(cap / kMinItemMax + std::min<size_t>(cap, (size_t)d.nblocks) + 1);
@@ -435,6 +437,8 @@ snow_status fast_upload_soa(snow_scene* s, const std::vector<float4>& xm, const 
   CK(cudaMemcpyAsync(s->sd.fb, fb.data(), n * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(s->sd.fc, fc.data(), n * sizeof(float2), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(s->sd.pid, pid.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream));
+  const std::vector<float4> frame(n, make_float4(1.0f, 0.0f, 0.0f, 0.0f));  // no previous SVD: identity
+  CK(cudaMemcpyAsync(s->sd.vq, frame.data(), n * sizeof(float4), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   return SNOW_OK;
 }
@@ -559,15 +563,15 @@ size_t snow_scene_footprint(const snow_params* p, size_t n) {
   const double G = (double)p->grid_dim[0] * p->grid_dim[1] * p->grid_dim[2];
   if (p->mode == SNOW_MODE_REFERENCE) return (size_t)(n * (16.0 * 6 + 128.0) + G * 48.0);
   const double nb = (double)((p->grid_dim[0] + 3) / 4) * ((p->grid_dim[1] + 3) / 4) * ((p->grid_dim[2] + 3) / 4);
-  // An upper bound: particle streams (xm, vv, fa, fb: 16 B, fc: 8 B, pid: 4 B)
-  // + binning scratch (2 key + 2 value words, 4 x 16 B + 8 B + 4 B permutation
+  // An upper bound: particle streams (xm, vv, fa, fb, vq: 16 B, fc: 8 B, pid: 4 B)
+  // + binning scratch (2 key + 2 value words, 5 x 16 B + 8 B + 4 B permutation
   // targets, radix histograms) + work items (16 B each) + per block the dense
   // P2G sums (448 floats), flags, slot and bin tables (5 ints) + the output
   // pool at its largest (every block: 384 floats + 1 int) + the upload's
   // staging copy of the caller's arrays (x, v, m, F_E, F_P: 100 B).
   const double tiles = (double)radix_tiles(n);
   const double items = (double)n / kMinItemMax + std::min((double)n, nb) + 1;
-  return (size_t)(n * (76.0 + 92.0 + 100.0) + tiles * 256 * 4.0 + 4096.0 + items * 16.0 + nb * (448 * 4.0 + 5 * 4.0) +
+  return (size_t)(n * (92.0 + 108.0 + 100.0) + tiles * 256 * 4.0 + 4096.0 + items * 16.0 + nb * (448 * 4.0 + 5 * 4.0) +
                   nb * (384 * 4.0 + 4.0) + 1024.0);
 }
 

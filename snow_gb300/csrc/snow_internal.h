@@ -85,6 +85,7 @@ struct SceneDev {
   float4* fa;
   float4* fb;
   float2* fc;
+  float4* vq;       // FAST: the Jacobi frame (quaternion) of each particle's last SVD
   uint32_t* pid;    // upload index of the particle now stored at each slot
   // blocked grid
   int* blk_slot;    // nblocks: pool slot of the block this step, -1 if inactive
@@ -135,7 +136,7 @@ struct BinScratch {
   int* bstart;         // nblocks
   int* bend;           // nblocks
   int* home;           // nblocks
-  float4* tmp4[4];     // permutation targets for xm, vv, fa, fb
+  float4* tmp4[5];     // permutation targets for xm, vv, fa, fb, vq
   float2* tmp2;        // ... and fc
   uint32_t* tmp_pid;   // ... and pid
   size_t n_cap;

@@ -329,6 +329,37 @@ __device__ __forceinline__ void svd3(const M3& A, M3& W, M3& S, M3& V) {
   qr_givens<FAITHFUL>(B, W, S);
 }
 
+// FAST path only: the same SVD with the Jacobi eigen-solve of A^T A started
+// from the frame q of the particle's previous step (in: that frame, out: the
+// new one). F_E changes little per step, so Q^T A^T A Q is nearly diagonal and
+// one or two sweeps reach the convergence the four cold sweeps give; sweeps
+// stop once the off-diagonal part is below 1e-6 of the diagonal (at most 4).
+__device__ __forceinline__ void svd3_warm(const M3& A, float q[4], M3& W, M3& S, M3& V) {
+  const M3 ata = m3_mul_at(A, A);
+  quat_normalize(q);
+  const M3 Q = quat_to_m3(q);
+  const M3 t = m3_mul(m3_mul_at(Q, ata), Q);  // Q^T A^T A Q
+  M3 sym;
+#pragma unroll
+  for (int c = 0; c < 3; c++)
+#pragma unroll
+    for (int r = 0; r < 3; r++) sym.m[c][r] = r <= c ? t.m[c][r] : t.m[r][c];
+#pragma unroll 1
+  for (int sweep = 0; sweep < 4; sweep++) {
+    const float off = sym.m[1][0] * sym.m[1][0] + sym.m[2][0] * sym.m[2][0] + sym.m[2][1] * sym.m[2][1];
+    const float dia = sym.m[0][0] * sym.m[0][0] + sym.m[1][1] * sym.m[1][1] + sym.m[2][2] * sym.m[2][2];
+    if (off <= 1e-12f * dia) break;
+    jacobi_step<false, 0, 1, 2>(sym, q);
+    jacobi_step<false, 1, 2, 0>(sym, q);
+    jacobi_step<false, 2, 0, 1>(sym, q);
+  }
+  quat_normalize(q);
+  V = quat_to_m3(q);
+  M3 B = m3_mul(A, V);
+  sort_singular(B, V);
+  qr_givens<false>(B, W, S);
+}
+
 // ---- lame.include.glsl:11-27 -------------------------------------------------
 __device__ __forceinline__ float lame_mu(float young, float poisson, float hardening, float jp) {
   return young / (2.0f * (1.0f + poisson)) * expf(hardening * (1.0f - jp));

@@ -205,7 +205,7 @@ __global__ void k_keys(const SceneDev* __restrict__ sd, uint32_t* __restrict__ k
 
 __global__ void k_permute(const SceneDev* __restrict__ sd, const uint32_t* __restrict__ perm, float4* __restrict__ xm,
                           float4* __restrict__ vv, float4* __restrict__ fa, float4* __restrict__ fb,
-                          float2* __restrict__ fc, uint32_t* __restrict__ pid) {
+                          float2* __restrict__ fc, uint32_t* __restrict__ pid, float4* __restrict__ vq) {
   const SceneDev& S = *sd;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
     const uint32_t src = perm[i];
@@ -215,6 +215,7 @@ __global__ void k_permute(const SceneDev* __restrict__ sd, const uint32_t* __res
     fb[i] = S.fb[src];
     fc[i] = S.fc[src];
     pid[i] = S.pid[src];
+    vq[i] = S.vq[src];
   }
 }
 
@@ -293,13 +294,14 @@ void fast_apply_bins(const SceneDev& sd, const SceneDev* sd_dev, BinScratch& b, 
   if (sd.n <= 0) return;
   const size_t n = (size_t)sd.n;
   k_permute<<<grid_for(n, 256, 8), 256, 0, st>>>(sd_dev, b.vals[0], b.tmp4[0], b.tmp4[1], b.tmp4[2], b.tmp4[3],
-                                                  b.tmp2, b.tmp_pid);
+                                                  b.tmp2, b.tmp_pid, b.tmp4[4]);
   cudaMemcpyAsync(sd.xm, b.tmp4[0], n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(sd.vv, b.tmp4[1], n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(sd.fa, b.tmp4[2], n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(sd.fb, b.tmp4[3], n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(sd.fc, b.tmp2, n * sizeof(float2), cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(sd.pid, b.tmp_pid, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st);
+  cudaMemcpyAsync(sd.vq, b.tmp4[4], n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
   cudaMemsetAsync(sd.counters + CNT_ITEMS, 0, sizeof(int), st);
   cudaMemsetAsync(sd.counters + CNT_HOME, 0, sizeof(int), st);
   k_heads<<<grid_for(n, 256, 8), 256, 0, st>>>(sd_dev, b.keys[0], b.bstart, b.bend, b.home);

@@ -166,6 +166,33 @@ def test_fast_single_step_from_deformed_state_within_1e5(ctx, warm_steps):
 
 
 @gpu
+def test_fast_step_with_warm_svd_frames_within_1e5(ctx):
+    """The FAST advance starts each particle's Jacobi eigen-solve from the
+    frame of its previous SVD. Step the GPU once from a deformed state (the
+    frames become warm), restart the FP64 oracle from the GPU's state after
+    that step, and compare the next step of both."""
+    s2, o, g = _deformed_restart(ctx, 20, seed=61)
+    g.step(s2.dt, 1)
+    y = g.download()
+    n = len(y["x"])
+    fp = np.zeros((n, 3, 3))
+    fp[:, 0, 0] = y["Jp"]
+    fp[:, 1, 1] = fp[:, 2, 2] = 1.0  # only det F_P enters the step
+    s3 = scenes.Scene(**{k: getattr(s2, k) for k in ("grid_pos", "grid_dim", "grid_spacing", "young", "poisson",
+                                                     "hardening", "crit_compression", "crit_stretch", "alpha",
+                                                     "gravity", "dt")})
+    assert all(c.vel == (0.0, 0.0, 0.0) or tuple(c.vel) == (0.0, 0.0, 0.0) for c in s2.colliders)
+    s3.colliders = list(s2.colliders)  # static walls
+    s3.x, s3.v, s3.m = y["x"], y["v"], s2.m.copy()
+    rho = np.where(y["volume"] > 0, s3.m.astype(np.float64) / np.maximum(y["volume"], 1e-30), 0.0)
+    o2 = _exact_oracle(s3).upload(FE=y["FE"].astype(np.float64), FP=fp).set_density(rho)
+    o2.step()
+    g.step(s2.dt, 1)
+    e = field_errors(g.download(), o2.state())
+    assert max(e["x"], e["v"], e["FE"], e["Jp"]) <= REL_TOL, repr(e)
+
+
+@gpu
 def test_fast_grid_after_p2g_and_grid_update(ctx):
     from snow_gb300 import native as N
     s2, o, g = _deformed_restart(ctx, 20, seed=51)
