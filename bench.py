@@ -121,7 +121,7 @@ def measured_peak_hbm():
 
 
 def kernels_per_step(n_colliders, sort_step, key_bits):
-    plain = (1 if n_colliders else 0) + 5  # rigid, begin, compact, prefix, grid, g2p2g
+    plain = 4  # begin (counters, colliders), compact (+ prefixes), grid, g2p2g
     if not sort_step:
         return plain
     passes = (key_bits + 7) // 8

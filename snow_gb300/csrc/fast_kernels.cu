@@ -760,25 +760,35 @@ __device__ __forceinline__ void p2g_tile_pass(ItemShared& sh, const SceneDev& S,
 }
 
 // ===========================================================================
-__global__ void k_prefix(const SceneDev* __restrict__ scenes, int nscenes, int* items, int* active) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    int ai = 0, aa = 0;
-    for (int s = 0; s < nscenes; s++) {
-      items[s] = ai;
-      active[s] = aa;
-      ai += scenes[s].counters[CNT_ITEMS];
-      aa += min(scenes[s].counters[CNT_ACTIVE], scenes[s].pool_cap);
-    }
-    items[nscenes] = ai;
-    active[nscenes] = aa;
+__device__ __forceinline__ void form_prefixes(const SceneDev* __restrict__ scenes, int nscenes, int* items,
+                                              int* active) {
+  int ai = 0, aa = 0;
+  for (int s = 0; s < nscenes; s++) {
+    items[s] = ai;
+    active[s] = aa;
+    ai += *(volatile int*)&scenes[s].counters[CNT_ITEMS];
+    aa += min(*(volatile int*)&scenes[s].counters[CNT_ACTIVE], scenes[s].pool_cap);
   }
+  items[nscenes] = ai;
+  active[nscenes] = aa;
 }
 
-__global__ void k_begin_step(const SceneDev* __restrict__ scenes, int nscenes) {
-  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nscenes; s += gridDim.x * blockDim.x) {
-    scenes[s].counters[CNT_ACTIVE] = 0;
-    scenes[s].counters[CNT_OVERFLOW] = 0;
+__global__ void k_prefix(const SceneDev* __restrict__ scenes, int nscenes, int* items, int* active) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) form_prefixes(scenes, nscenes, items, active);
+}
+
+// One CTA per scene: the step's counters reset, colliders advanced.
+__global__ void k_begin_step(const SceneDev* __restrict__ scenes, int nscenes, int rigid) {
+  const int s = blockIdx.x;
+  if (s >= nscenes) return;
+  const SceneDev& S = scenes[s];
+  if (threadIdx.x == 0) {
+    S.counters[CNT_ACTIVE] = 0;
+    S.counters[CNT_OVERFLOW] = 0;
   }
+  if (rigid)  // rigidAdvance.glsl:14-18
+    for (int i = threadIdx.x; i < S.ncoll; i += blockDim.x)
+      for (int k = 0; k < 3; k++) S.coll[i].pos[k] = S.coll[i].pos[k] + S.dt * S.coll[i].vel[k];
 }
 
 __global__ void k_count_flags(const SceneDev* __restrict__ sd, int nblocks) {
@@ -790,9 +800,10 @@ __global__ void k_count_flags(const SceneDev* __restrict__ sd, int nblocks) {
   if ((threadIdx.x & 31) == 0 && c) atomicAdd(&sd->counters[CNT_ACTIVE], c);
 }
 
-// Flags -> active-block list and pool slots (one thread per block).
+// Flags -> active-block list and pool slots (one thread per block); the CTA
+// that finishes last forms the item and active-block prefixes.
 __global__ void k_compact(const SceneDev* __restrict__ scenes, const int* __restrict__ block_prefix, int nscenes,
-                          long long total) {
+                          long long total, int* items_prefix, int* active_prefix) {
   for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < total;
        u += (long long)gridDim.x * blockDim.x) {
     const int s = find_scene(block_prefix, nscenes, u);
@@ -810,6 +821,18 @@ __global__ void k_compact(const SceneDev* __restrict__ scenes, const int* __rest
       }
     }
     S.blk_slot[b] = slot;
+  }
+  __shared__ bool last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(&scenes[0].counters[CNT_DONE], 1) == (int)gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    form_prefixes(scenes, nscenes, items_prefix, active_prefix);
+    scenes[0].counters[CNT_DONE] = 0;
   }
 }
 
@@ -1053,14 +1076,6 @@ __global__ void __launch_bounds__(kItemMax, 2) k_g2p2g(const SceneDev* __restric
   }
 }
 
-__global__ void k_rigid(const SceneDev* __restrict__ scenes, int nscenes) {  // rigidAdvance.glsl:14-18
-  const int s = blockIdx.x;
-  if (s >= nscenes) return;
-  const SceneDev& S = scenes[s];
-  for (int i = threadIdx.x; i < S.ncoll; i += blockDim.x)
-    for (int k = 0; k < 3; k++) S.coll[i].pos[k] = S.coll[i].pos[k] + S.dt * S.coll[i].vel[k];
-}
-
 // Bulk statistics: per-thread sums in FP32 over a dozen particles, then FP64
 // across threads (FP64 arithmetic is slow on this part: the per-particle work
 // stays in FP32).
@@ -1230,8 +1245,8 @@ void fast_prefix(const SceneDev* scenes, int nscenes, int* items_prefix, int* ac
   k_prefix<<<1, 32, 0, st>>>(scenes, nscenes, items_prefix, active_prefix);
 }
 
-void fast_begin_step(const SceneDev* scenes, int nscenes, cudaStream_t st) {
-  if (nscenes > 0) k_begin_step<<<(nscenes + 127) / 128, 128, 0, st>>>(scenes, nscenes);
+void fast_begin_step(const SceneDev* scenes, int nscenes, bool rigid, cudaStream_t st) {
+  if (nscenes > 0) k_begin_step<<<nscenes, 32, 0, st>>>(scenes, nscenes, rigid ? 1 : 0);
 }
 
 void fast_count_flags(const SceneDev* sd_dev, int nblocks, cudaStream_t st) {
@@ -1242,11 +1257,10 @@ void fast_count_flags(const SceneDev* sd_dev, int nblocks, cudaStream_t st) {
 }
 
 void fast_compact(const SceneDev* scenes, const int* block_prefix, int nscenes, long long total_blocks,
-                  cudaStream_t st) {
-  if (total_blocks <= 0) return;
+                  int* items_prefix, int* active_prefix, cudaStream_t st) {
   long long g = (total_blocks + 255) / 256;
-  g = g > (long long)num_sms() * 16 ? (long long)num_sms() * 16 : g;
-  k_compact<<<(int)g, 256, 0, st>>>(scenes, block_prefix, nscenes, total_blocks);
+  g = g > (long long)num_sms() * 16 ? (long long)num_sms() * 16 : (g < 1 ? 1 : g);
+  k_compact<<<(int)g, 256, 0, st>>>(scenes, block_prefix, nscenes, total_blocks, items_prefix, active_prefix);
 }
 
 void fast_p2g(const SceneDev* scenes, const int* item_prefix, int nscenes, int grid_ctas, bool mass_only,
@@ -1276,10 +1290,6 @@ void fast_g2p_advance(const SceneDev* scenes, const int* item_prefix, int nscene
 
 void fast_g2p2g(const SceneDev* scenes, const int* item_prefix, int nscenes, int grid_ctas, cudaStream_t st) {
   k_g2p2g<<<grid_ctas, kItemMax, item_smem(), st>>>(scenes, item_prefix, nscenes);
-}
-
-void fast_rigid(const SceneDev* scenes, int nscenes, cudaStream_t st) {
-  if (nscenes > 0) k_rigid<<<nscenes, 32, 0, st>>>(scenes, nscenes);
 }
 
 void fast_stats(const SceneDev* sd_dev, int n, StatsAccum* out_dev, cudaStream_t st) {

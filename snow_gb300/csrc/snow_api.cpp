@@ -288,10 +288,9 @@ void fast_bin(snow_scene* s, cudaStream_t st) {
 }
 
 // Active blocks of the pending P2G sums -> pool slots (and prefixes).
-void fast_enqueue_compact(snow_scene* s, cudaStream_t st) {
-  fast_begin_step(s->sd_dev, 1, st);
-  fast_compact(s->sd_dev, s->d_prefix + 6, 1, s->sd.nblocks, st);
-  fast_prefix(s->sd_dev, 1, s->d_prefix + 0, s->d_prefix + 2, st);
+void fast_enqueue_compact(snow_scene* s, cudaStream_t st, bool counters_reset = false) {
+  if (!counters_reset) fast_begin_step(s->sd_dev, 1, false, st);
+  fast_compact(s->sd_dev, s->d_prefix + 6, 1, s->sd.nblocks, s->d_prefix + 0, s->d_prefix + 2, st);
 }
 void fast_enqueue_p2g(snow_scene* s, bool mass_only, cudaStream_t st) {
   fast_p2g(s->sd_dev, s->d_prefix + 0, 1, item_ctas(s->tune), mass_only, st);
@@ -302,9 +301,9 @@ void fast_enqueue_grid(snow_scene* s, bool clear_only, cudaStream_t st) {
 // One step of a scene whose P2G sums of the current state are pending in
 // acc: rigid advance, [binning], grid update, G2P + advance + next P2G.
 void fast_enqueue_step(snow_scene* s, bool bin, cudaStream_t st) {
-  if (s->ncoll > 0) fast_rigid(s->sd_dev, 1, st);
+  fast_begin_step(s->sd_dev, 1, s->ncoll > 0, st);
   if (bin) fast_bin(s, st);
-  fast_enqueue_compact(s, st);
+  fast_enqueue_compact(s, st, true);
   fast_enqueue_grid(s, false, st);
   fast_g2p2g(s->sd_dev, s->d_prefix + 0, 1, item_ctas(s->tune), st);
 }
@@ -809,7 +808,7 @@ snow_status snow_dispatch(snow_scene* s, int kernel, double dt) {
   if (r) return r;
   switch (kernel) {
     case SNOW_K_RIGID_ADVANCE:
-      if (s->ncoll > 0) fast_rigid(s->sd_dev, 1, st);
+      if (s->ncoll > 0) fast_begin_step(s->sd_dev, 1, true, st);
       break;
     case SNOW_K_G_RESET:  // discard pending P2G sums
       if (s->p2g_ready) {
@@ -888,10 +887,10 @@ snow_status snow_scene_step(snow_scene* s, double dt, int n_steps) {
     if (ctx->profiling) {
       cudaEvent_t* ev = ctx->ev;
       CK(cudaEventRecord(ev[0], st));
-      if (s->ncoll > 0) fast_rigid(s->sd_dev, 1, st);
+      fast_begin_step(s->sd_dev, 1, s->ncoll > 0, st);
       if (bin) fast_bin(s, st);
       CK(cudaEventRecord(ev[1], st));
-      fast_enqueue_compact(s, st);
+      fast_enqueue_compact(s, st, true);
       fast_enqueue_grid(s, false, st);
       CK(cudaEventRecord(ev[2], st));
       fast_g2p2g(s->sd_dev, s->d_prefix + 0, 1, item_ctas(s->tune), st);
@@ -1227,13 +1226,11 @@ void batch_enqueue_step(snow_batch* b, int phase, int interval, cudaStream_t st)
   int* items = pre;
   int* active = pre + (n + 1);
   int* blocks = pre + 3 * (n + 1);
-  fast_rigid(b->d_scenes, n, st);
+  fast_begin_step(b->d_scenes, n, true, st);
   // re-bin a staggered subset of scenes each step
   for (int i = 0; i < n; i++)
     if ((i % interval) == phase) fast_bin(b->scenes[i], st);
-  fast_begin_step(b->d_scenes, n, st);
-  fast_compact(b->d_scenes, blocks, n, b->total_blocks, st);
-  fast_prefix(b->d_scenes, n, items, active, st);
+  fast_compact(b->d_scenes, blocks, n, b->total_blocks, items, active, st);
   fast_grid(b->d_scenes, active, n, grid_ctas(), false, st);
   fast_g2p2g(b->d_scenes, items, n, item_ctas(b->scenes[0]->tune), st);
 }

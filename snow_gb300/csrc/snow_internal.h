@@ -60,6 +60,7 @@ enum {
   CNT_HOME = 4,       // occupied home blocks at the last binning
   CNT_FALLBACK = 5,   // particles that left their P2G tile (diagnostic, cumulative)
   CNT_TIMEOUT = 6,    // bounded waits that ran out (cumulative)
+  CNT_DONE = 7,       // CTAs of the compaction finished (the last forms the prefixes)
   kCounterStride = 8
 };
 
@@ -112,10 +113,15 @@ constexpr int kMinItemMax = 64;
 // are only known on the device; fast_prefix() forms both prefixes there.
 void fast_prefix(const SceneDev* scenes, int nscenes, int* items_prefix, int* active_prefix, cudaStream_t st);
 // Zeroes the per-step counters (active blocks, overflow) of every scene.
-void fast_begin_step(const SceneDev* scenes, int nscenes, cudaStream_t st);
+// Start of a step: resets the per-step counters and, with `rigid`, moves the
+// colliders by dt * velocity (rigidAdvance.glsl:14-18).
+void fast_begin_step(const SceneDev* scenes, int nscenes, bool rigid, cudaStream_t st);
 // Counts flagged blocks of one scene into counters[CNT_ACTIVE] (pool sizing).
 void fast_count_flags(const SceneDev* sd_dev, int nblocks, cudaStream_t st);
+// Flags -> active list and pool slots; its last CTA then forms the item and
+// active-block prefixes (as fast_prefix does).
 void fast_compact(const SceneDev* scenes, const int* block_prefix, int nscenes, long long total_blocks,
+                  int* items_prefix, int* active_prefix,
                   cudaStream_t st);
 void fast_p2g(const SceneDev* scenes, const int* item_prefix, int nscenes, int grid_ctas, bool mass_only,
               cudaStream_t st);
@@ -124,7 +130,6 @@ void fast_grid(const SceneDev* scenes, const int* active_prefix, int nscenes, in
 void fast_volume(const SceneDev* sd_dev, int n, cudaStream_t st);
 void fast_g2p_advance(const SceneDev* scenes, const int* item_prefix, int nscenes, int grid_ctas, cudaStream_t st);
 void fast_g2p2g(const SceneDev* scenes, const int* item_prefix, int nscenes, int grid_ctas, cudaStream_t st);
-void fast_rigid(const SceneDev* scenes, int nscenes, cudaStream_t st);
 
 // Binning of one scene (host-side sizes known): keys -> radix sort ->
 // permutation of the particle streams -> P2G work items.
