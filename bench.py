@@ -43,10 +43,14 @@ L2_FLUSH_BYTES = 256 << 20
 BYTES_G2P2G = (72 + 128, 16 + 24)
 BYTES_GRID = (0, 40)
 
-# DRAM bytes (read + write) per launch of the fused kernel from an ncu
-# capture of this workload (profiles/k_g2p2g_dram_traffic_two_snowballs_1M_256.md),
-# keyed by (particles, grid edge); other workloads report null.
-TRAFFIC_MEASURED = {(1 << 20, 256): 108.3e6}
+# From an ncu capture of the fused kernel on this workload
+# (profiles/k_g2p2g_two_snowballs_1M_256.md), keyed by (particles, grid edge);
+# other workloads report null: DRAM bytes (read + write) per launch, and warp
+# instructions per launch for the issue roofline.
+TRAFFIC_MEASURED = {(1 << 20, 256): 144.5e6}
+INSTRUCTIONS_MEASURED = {(1 << 20, 256): 181.1e6}
+# warp-instruction issue peak: 152 SMs x 4 schedulers x 2.07 GHz
+ISSUE_PEAK = 152 * 4 * 2.07e9
 
 
 def rank_info():
@@ -608,6 +612,14 @@ def main():
                      "traffic": (TRAFFIC_MEASURED.get((args.particles, args.grid))
                                  if res["dominant"] == "g2p2g" else None),
                      "algorithmic_bytes_per_launch": res["alg_bytes"], "active_nodes": res["A"]},
+        "issue_roofline": ({"achieved": INSTRUCTIONS_MEASURED[(args.particles, args.grid)] /
+                                        (res["per"]["g2p2g"] * 1e-3),
+                            "peak": ISSUE_PEAK, "unit": "warp-instructions/s",
+                            "frac": INSTRUCTIONS_MEASURED[(args.particles, args.grid)] /
+                                    (res["per"]["g2p2g"] * 1e-3) / ISSUE_PEAK,
+                            "kernel": "g2p2g", "instructions_per_launch": INSTRUCTIONS_MEASURED[
+                                (args.particles, args.grid)]}
+                           if (args.particles, args.grid) in INSTRUCTIONS_MEASURED else None),
         "phase_ms": res["per"],
         "clocks": res["clocks"],
         "e2e": {"value": n * res["e2e_steps"] / res["e2e_s"], "unit": UNIT,
