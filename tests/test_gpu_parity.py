@@ -223,11 +223,16 @@ def test_fast_grid_after_p2g_and_grid_update(ctx):
 
 
 @gpu
-def test_fast_short_horizon_bulk_statistics(ctx):
-    """100 steps of the cfg1-like snowball: trajectories diverge, bulk
-    quantities agree."""
+@pytest.mark.parametrize("which", ["small", "cfg1"])
+def test_fast_short_horizon_bulk_statistics(ctx, which):
+    """100 steps of a snowball (a small one, and the plain CPU-checkable
+    workload itself: 32,768 particles in a 64^3 grid dropped at 2 m/s):
+    trajectories diverge, bulk quantities agree with the FP64 oracle."""
     from snow_gb300 import native as N
-    s = scenes.small_scene(n=8000, grid_edge=48, seed=61, v0=(0.0, -2.0, 0.0), center=(0.5, 0.3, 0.5))
+    if which == "cfg1":
+        s = scenes.cfg1_snowball()
+    else:
+        s = scenes.small_scene(n=8000, grid_edge=48, seed=61, v0=(0.0, -2.0, 0.0), center=(0.5, 0.3, 0.5))
     g = sim(ctx, s, N.MODE_FAST).upload().init().step(s.dt, 100)
     o = _exact_oracle(s).upload().init().step(n=100)
     st = g.stats()
@@ -243,6 +248,23 @@ def test_fast_short_horizon_bulk_statistics(ctx):
     assert abs(st["mean_jp"] - ref["Jp"].mean()) <= 1e-4
     assert np.abs(st["bbox_min"] - ref["x"].min(0)).max() <= 1e-3
     assert np.abs(st["bbox_max"] - ref["x"].max(0)).max() <= 1e-3
+
+
+@gpu
+def test_reference_mode_cfg1_100_steps_tracks_the_faithful_oracle(ctx):
+    """REFERENCE mode (the shaders' FP32 + int32 fixed-point arithmetic) on
+    the plain CPU-checkable workload for its 100 steps, against the FP32
+    fixed-point restatement: per-particle state stays within float rounding
+    of the shader arithmetic (exp differs by ~2 ulp), far tighter than the
+    FAST bound."""
+    from snow_gb300 import native as N
+    s = scenes.cfg1_snowball()
+    g = sim(ctx, s, N.MODE_REFERENCE).upload_std140(*s.std140()).init().step(s.dt, 100)
+    o = O.OracleSim(s, mode=O.FAITHFUL32).upload_std140(*s.std140()).init().step(n=100)
+    got, ref = g.download(), o.state()
+    assert np.abs(got["x"] - ref["x"]).max() <= 1e-5
+    assert np.abs(got["v"] - ref["v"]).max() <= 1e-3 * max(1.0, np.abs(ref["v"]).max())
+    assert np.abs(got["Jp"] - ref["Jp"]).max() <= 1e-4
 
 
 # ---------------------------------------------------------------------------
