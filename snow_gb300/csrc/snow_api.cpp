@@ -503,7 +503,9 @@ snow_status snow_ctx_create(int device, size_t hbm_budget_bytes, snow_ctx** out)
     e = cudaMemPoolCreate(&ctx->pool, &props);
   }
   if (e == cudaSuccess) {
-    uint64_t keep = UINT64_MAX;  // hold freed memory until the context goes
+    // keep freed memory for reuse, up to the budget (all of it without one);
+    // the pool returns what exceeds that at synchronisation points
+    uint64_t keep = hbm_budget_bytes ? (uint64_t)hbm_budget_bytes : UINT64_MAX;
     e = cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep);
   }
   if (e == cudaSuccess) e = cudaMalloc(&ctx->d_stats, sizeof(StatsAccum));
