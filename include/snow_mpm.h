@@ -189,6 +189,15 @@ snow_status snow_scene_download_std140(snow_scene* s, float* pxm, int32_t* pv, f
 snow_status snow_scene_download_grid(snow_scene* s, float* mass, float* momentum, float* force, float* vstar);
 snow_status snow_scene_download_colliders(snow_scene* s, snow_collider* out);
 snow_status snow_scene_stats(snow_scene* s, snow_stats* out);
+/* The same statistics without waiting: snow_scene_stats_enqueue queues them
+ * into one of the context's SNOW_STATS_SLOTS slots (after the work already
+ * queued on the context's stream) and returns; snow_ctx_stats_read waits for
+ * that slot and returns them. A stepping loop can read step i's statistics
+ * while step i + 1 runs. Enqueueing into a slot that holds unread statistics
+ * waits for them first. (No counterpart in the reference.) */
+#define SNOW_STATS_SLOTS 8
+snow_status snow_scene_stats_enqueue(snow_scene* s, int slot);
+snow_status snow_ctx_stats_read(snow_ctx* ctx, int slot, snow_stats* out);
 size_t snow_scene_size(const snow_scene* s);
 
 /* Particle -> cell binning as used by the FAST path: per-particle block-major

@@ -44,6 +44,11 @@ class Context:
     def set_profiling(self, on: bool):
         self.check(self.L.snow_ctx_set_profiling(self.h, int(bool(on))))
 
+    def stats_read(self, slot: int = 0) -> dict:
+        s = N.SnowStats()
+        self.check(self.L.snow_ctx_stats_read(self.h, int(slot), C.byref(s)))
+        return _stats_dict(s)
+
     def set_graphs(self, on: bool):
         """False: single-scene steps launch kernels one by one (no CUDA graph)."""
         self.check(self.L.snow_ctx_set_graphs(self.h, int(bool(on))))
@@ -213,6 +218,12 @@ class SimScene:
     def set_tuning(self, sort_interval: int, items_max: int = 256, ctas_per_sm: int = 2):
         t = N.SnowTuning(int(sort_interval), int(items_max), int(ctas_per_sm), 0, 0.0)
         self.ctx.check(self.L.snow_scene_set_tuning(self.h, C.byref(t)))
+        return self
+
+    def stats_enqueue(self, slot: int = 0):
+        """Queues this scene's statistics into a context slot; read them with
+        Context.stats_read(slot) (a loop can read step i while i + 1 runs)."""
+        self.ctx.check(self.L.snow_scene_stats_enqueue(self.h, int(slot)))
         return self
 
     def cell_keys(self):

@@ -30,8 +30,13 @@ struct snow_ctx {
   // device memory of scenes and batches comes from this pool, which keeps
   // freed blocks for reuse (scenes of a serving loop come and go)
   cudaMemPool_t pool = nullptr;
-  StatsAccum* d_stats = nullptr;
-  StatsAccum* h_stats = nullptr;  // pinned
+  // statistics: slot 0 for snow_scene_stats, slots 1..SNOW_STATS_SLOTS for
+  // the queued reads; the pinned init record resets an accumulator
+  StatsAccum* d_stats = nullptr;   // 1 + SNOW_STATS_SLOTS accumulators
+  StatsAccum* h_stats = nullptr;   // pinned, 1 + SNOW_STATS_SLOTS + 1 (init)
+  cudaEvent_t stat_ev[SNOW_STATS_SLOTS] = {};
+  size_t stat_n[SNOW_STATS_SLOTS] = {};
+  bool stat_pending[SNOW_STATS_SLOTS] = {};
   int* h_counters = nullptr;      // pinned, kCounterStride ints
   cudaEvent_t ev[8] = {};
   // live children, destroyed with the context if the caller did not
@@ -508,8 +513,18 @@ snow_status snow_ctx_create(int device, size_t hbm_budget_bytes, snow_ctx** out)
     uint64_t keep = hbm_budget_bytes ? (uint64_t)hbm_budget_bytes : UINT64_MAX;
     e = cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep);
   }
-  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_stats, sizeof(StatsAccum));
-  if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_stats, sizeof(StatsAccum));
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_stats, sizeof(StatsAccum) * (1 + SNOW_STATS_SLOTS));
+  if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_stats, sizeof(StatsAccum) * (2 + SNOW_STATS_SLOTS));
+  if (e == cudaSuccess) {
+    StatsAccum& init = ctx->h_stats[1 + SNOW_STATS_SLOTS];
+    std::memset(&init, 0, sizeof init);
+    for (int k = 0; k < 3; k++) {
+      init.bmin_key[k] = 0x7fffffff;
+      init.bmax_key[k] = (int)0x80000000;
+    }
+  }
+  for (int i = 0; i < SNOW_STATS_SLOTS && e == cudaSuccess; i++)
+    e = cudaEventCreateWithFlags(&ctx->stat_ev[i], cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_counters, kCounterStride * sizeof(int));
   for (int i = 0; i < 8 && e == cudaSuccess; i++) e = cudaEventCreate(&ctx->ev[i]);
   if (e != cudaSuccess) {
@@ -528,6 +543,8 @@ void snow_ctx_destroy(snow_ctx* ctx) {
   while (!ctx->scenes.empty()) snow_scene_destroy(*ctx->scenes.begin());
   for (int i = 0; i < 8; i++)
     if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+  for (int i = 0; i < SNOW_STATS_SLOTS; i++)
+    if (ctx->stat_ev[i]) cudaEventDestroy(ctx->stat_ev[i]);
   if (ctx->d_stats) cudaFree(ctx->d_stats);
   if (ctx->h_stats) cudaFreeHost(ctx->h_stats);
   if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
@@ -1075,22 +1092,20 @@ snow_status snow_scene_download_colliders(snow_scene* s, snow_collider* out) {
   return SNOW_OK;
 }
 
-snow_status snow_scene_stats(snow_scene* s, snow_stats* out) {
-  if (!s || !out) return SNOW_EINVAL;
+static snow_status stats_enqueue(snow_scene* s, int k) {
   snow_ctx* ctx = s->ctx;
-  StatsAccum init{};
-  for (int k = 0; k < 3; k++) {
-    init.bmin_key[k] = 0x7fffffff;
-    init.bmax_key[k] = (int)0x80000000;
-  }
-  CK(cudaMemcpyAsync(ctx->d_stats, &init, sizeof init, cudaMemcpyHostToDevice, ctx->stream));
+  StatsAccum* d = ctx->d_stats + k;
+  CK(cudaMemcpyAsync(d, ctx->h_stats + 1 + SNOW_STATS_SLOTS, sizeof(StatsAccum), cudaMemcpyHostToDevice,
+                     ctx->stream));
   if (s->mode == SNOW_MODE_REFERENCE)
-    ref_stats(ref_args(s), ctx->d_stats, ctx->stream);
+    ref_stats(ref_args(s), d, ctx->stream);
   else
-    fast_stats(s->sd_dev, (int)s->n, ctx->d_stats, ctx->stream);
-  CK(cudaMemcpyAsync(ctx->h_stats, ctx->d_stats, sizeof(StatsAccum), cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
-  const StatsAccum& a = *ctx->h_stats;
+    fast_stats(s->sd_dev, (int)s->n, d, ctx->stream);
+  CK(cudaMemcpyAsync(ctx->h_stats + k, d, sizeof(StatsAccum), cudaMemcpyDeviceToHost, ctx->stream));
+  return SNOW_OK;
+}
+
+static void stats_convert(const StatsAccum& a, size_t n, snow_stats* out) {
   std::memset(out, 0, sizeof *out);
   out->mass = a.mass;
   for (int k = 0; k < 3; k++) {
@@ -1106,8 +1121,38 @@ snow_status snow_scene_stats(snow_scene* s, snow_stats* out) {
   }
   out->kinetic_energy = a.ke;
   out->nonfinite = a.nonfinite;
-  out->n = s->n;
-  out->mean_jp = s->n > a.nonfinite ? a.jp / (double)(s->n - a.nonfinite) : 0.0;
+  out->n = n;
+  out->mean_jp = n > a.nonfinite ? a.jp / (double)(n - a.nonfinite) : 0.0;
+}
+
+snow_status snow_scene_stats(snow_scene* s, snow_stats* out) {
+  if (!s || !out) return SNOW_EINVAL;
+  snow_ctx* ctx = s->ctx;
+  snow_status r = stats_enqueue(s, 0);
+  if (r) return r;
+  CK(cudaStreamSynchronize(ctx->stream));
+  stats_convert(ctx->h_stats[0], s->n, out);
+  return SNOW_OK;
+}
+
+snow_status snow_scene_stats_enqueue(snow_scene* s, int slot) {
+  if (!s || slot < 0 || slot >= SNOW_STATS_SLOTS) return fail(s ? s->ctx : nullptr, SNOW_EINVAL, "stats slot");
+  snow_ctx* ctx = s->ctx;
+  if (ctx->stat_pending[slot]) CK(cudaEventSynchronize(ctx->stat_ev[slot]));  // reusing an unread slot
+  snow_status r = stats_enqueue(s, 1 + slot);
+  if (r) return r;
+  CK(cudaEventRecord(ctx->stat_ev[slot], ctx->stream));
+  ctx->stat_n[slot] = s->n;
+  ctx->stat_pending[slot] = true;
+  return SNOW_OK;
+}
+
+snow_status snow_ctx_stats_read(snow_ctx* ctx, int slot, snow_stats* out) {
+  if (!ctx || !out || slot < 0 || slot >= SNOW_STATS_SLOTS) return fail(ctx, SNOW_EINVAL, "stats slot");
+  if (!ctx->stat_pending[slot]) return fail(ctx, SNOW_ESTATE, "no statistics queued in this slot");
+  CK(cudaEventSynchronize(ctx->stat_ev[slot]));
+  ctx->stat_pending[slot] = false;
+  stats_convert(ctx->h_stats[1 + slot], ctx->stat_n[slot], out);
   return SNOW_OK;
 }
 

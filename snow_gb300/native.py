@@ -29,7 +29,8 @@ EXPORTS = [
     "snow_scene_cell_keys", "snow_scene_phase_times", "snow_batch_create", "snow_batch_destroy",
     "snow_batch_step", "snow_batch_autotune", "snow_sort_keys_static", "snow_server_create", "snow_server_destroy",
     "snow_server_submit", "snow_server_poll", "snow_server_fetch", "snow_server_stats", "snow_server_drain",
-    "snow_scene_set_tuning", "snow_batch_set_tuning", "snow_ctx_set_graphs",
+    "snow_scene_set_tuning", "snow_batch_set_tuning", "snow_ctx_set_graphs", "snow_scene_stats_enqueue",
+    "snow_ctx_stats_read",
 ]
 SORT_STATIC_MAX_KEYS = 262144  # SNOW_SORT_STATIC_MAX_KEYS
 
@@ -139,6 +140,8 @@ def load(path: str = LIB_PATH):
     L.snow_scene_download_grid.argtypes = [vp, fp, fp, fp, fp]
     L.snow_scene_download_colliders.argtypes = [vp, C.POINTER(SnowCollider)]
     L.snow_scene_stats.argtypes = [vp, C.POINTER(SnowStats)]
+    L.snow_scene_stats_enqueue.argtypes = [vp, C.c_int]
+    L.snow_ctx_stats_read.argtypes = [vp, C.c_int, C.POINTER(SnowStats)]
     L.snow_scene_size.argtypes = [vp]
     L.snow_scene_size.restype = sz
     L.snow_scene_cell_keys.argtypes = [vp, up, up]

@@ -131,3 +131,24 @@ def test_autotune_picks_a_candidate_and_reuses_the_cache(ctx, tmp_path):
         assert sim.stats()["nonfinite"] == 0
     bad = N.SnowTuning(0, 256, 2, 0, 0.0)
     assert N.load().snow_batch_set_tuning(b.h, ctypes.byref(bad)) == -1
+
+
+@gpu
+def test_queued_statistics_match_the_waiting_read(ctx):
+    from snow_gb300 import api, native as N
+    s = scenes.small_scene(n=3000, grid_edge=32, seed=95, v0=(1.0, -2.0, 0.5))
+    sim = api.SimScene(ctx, s).upload().init()
+    want = []
+    for i in range(4):
+        sim.step(s.dt, 1)
+        sim.stats_enqueue(i % 3)
+        want.append(sim.stats())
+    # slot 0 was reused by step 3: it holds step 3's statistics
+    got = {k: ctx.stats_read(k) for k in range(3)}
+    for slot, step in ((0, 3), (1, 1), (2, 2)):
+        for key in ("mass", "kinetic_energy", "mean_jp"):
+            assert got[slot][key] == want[step][key]
+        assert np.array_equal(got[slot]["momentum"], want[step]["momentum"])
+    with pytest.raises(N.SnowError) as e:
+        ctx.stats_read(0)  # already read
+    assert e.value.status == -7
