@@ -484,25 +484,47 @@ __device__ __forceinline__ void advance_particle(const SceneDev& S, int p, const
 #pragma unroll
     for (int r = 0; r < 3; r++) step.m[c][r] = (c == r ? 1.0f : 0.0f) + S.dt * L[r][c];
   const M3 fe_trial = m3_mul(step, FE);
-  M3 W, Sg, V;
+  M3 V;
+  float lam[3];
   const float4 q4 = S.vq[p];
   float q[4] = {q4.x, q4.y, q4.z, q4.w};
-  svd3_warm(fe_trial, q, W, Sg, V);
+  eigen_warm(fe_trial, q, V, lam);
   S.vq[p] = make_float4(q[0], q[1], q[2], q[3]);
-  float ratio = 1.0f;
+  const float lo2 = S.crit_lo * S.crit_lo, hi2 = S.crit_hi * S.crit_hi;
+  const bool elastic = lam[0] >= lo2 && lam[0] <= hi2 && lam[1] >= lo2 && lam[1] <= hi2 && lam[2] >= lo2 &&
+                       lam[2] <= hi2;
+  if (elastic) {
+    // every singular value inside [1 - theta_c, 1 + theta_s]: the clamp
+    // leaves F_E' = W S V^T = FE_trial and J_p as they are; the polar
+    // rotation is R = FE_trial V S^-1 V^T
+    out.fe = fe_trial;
+    M3 B = m3_mul(fe_trial, V);
 #pragma unroll
-  for (int i = 0; i < 3; i++) {
-    const float sv = Sg.m[i][i];
-    const float cl = fminf(fmaxf(sv, S.crit_lo), S.crit_hi);
-    ratio *= __fdividef(sv, cl);
-    Sg.m[i][i] = cl;
+    for (int c = 0; c < 3; c++) {
+      const float inv = rsqrt_nr(lam[c]);
+#pragma unroll
+      for (int r = 0; r < 3; r++) B.m[c][r] *= inv;
+    }
+    out.R = m3_mul_bt(B, V);
+    out.jp = jp;
+  } else {
+    M3 W, Sg;
+    svd3_from_v(fe_trial, V, W, Sg);
+    float ratio = 1.0f;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const float sv = Sg.m[i][i];
+      const float cl = fminf(fmaxf(sv, S.crit_lo), S.crit_hi);
+      ratio *= __fdividef(sv, cl);
+      Sg.m[i][i] = cl;
+    }
+    out.fe = m3_mul_bt(m3_mul(W, Sg), V);
+    out.R = m3_mul_bt(W, V);
+    // det F_P' = det F_P * det(FE_trial) / det(FE'): the shader's
+    // F_P' = V S^-1 W^T (I + dt L) FE FP (particleAdvance.glsl:132) has this
+    // determinant; only det F_P is ever read (p2gTransfer.glsl:119).
+    out.jp = jp * ratio;
   }
-  out.fe = m3_mul_bt(m3_mul(W, Sg), V);
-  out.R = m3_mul_bt(W, V);
-  // det F_P' = det F_P * det(FE_trial) / det(FE'): the shader's
-  // F_P' = V S^-1 W^T (I + dt L) FE FP (particleAdvance.glsl:132) has this
-  // determinant; only det F_P is ever read (p2gTransfer.glsl:119).
-  out.jp = jp * ratio;
   float v[3] = {S.alpha * vv.x + dv[0], S.alpha * vv.y + dv[1], S.alpha * vv.z + dv[2]};
   const float xold[3] = {xm.x, xm.y, xm.z};
   collide(coll, S.ncoll, xold, v);

@@ -329,12 +329,14 @@ __device__ __forceinline__ void svd3(const M3& A, M3& W, M3& S, M3& V) {
   qr_givens<FAITHFUL>(B, W, S);
 }
 
-// FAST path only: the same SVD with the Jacobi eigen-solve of A^T A started
-// from the frame q of the particle's previous step (in: that frame, out: the
-// new one). F_E changes little per step, so Q^T A^T A Q is nearly diagonal and
-// one or two sweeps reach the convergence the four cold sweeps give; sweeps
-// stop once the off-diagonal part is below 1e-6 of the diagonal (at most 4).
-__device__ __forceinline__ void svd3_warm(const M3& A, float q[4], M3& W, M3& S, M3& V) {
+// FAST path only: the Jacobi eigen-solve of A^T A started from the frame q
+// of the particle's previous step (in: that frame, out: the new one). F_E
+// changes little per step, so Q^T A^T A Q is nearly diagonal and one or two
+// sweeps reach the convergence the four cold sweeps give; sweeps stop once
+// the off-diagonal part is below 1e-6 of the diagonal (at most 4). Returns V
+// (the eigenvectors, unsorted) and lam, the eigenvalues sigma_i^2 in V's
+// column order.
+__device__ __forceinline__ void eigen_warm(const M3& A, float q[4], M3& V, float lam[3]) {
   const M3 ata = m3_mul_at(A, A);
   quat_normalize(q);
   const M3 Q = quat_to_m3(q);
@@ -355,6 +357,14 @@ __device__ __forceinline__ void svd3_warm(const M3& A, float q[4], M3& W, M3& S,
   }
   quat_normalize(q);
   V = quat_to_m3(q);
+  lam[0] = sym.m[0][0];
+  lam[1] = sym.m[1][1];
+  lam[2] = sym.m[2][2];
+}
+
+// The rest of the SVD from eigen_warm's V: B = A V, sorted columns, Givens
+// QR (A = W S V^T, as svd3).
+__device__ __forceinline__ void svd3_from_v(const M3& A, M3& V, M3& W, M3& S) {
   M3 B = m3_mul(A, V);
   sort_singular(B, V);
   qr_givens<false>(B, W, S);
