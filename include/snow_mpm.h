@@ -332,7 +332,7 @@ snow_status snow_scene_set_tuning(snow_scene* s, const snow_tuning* t);
 /* Applies a tuning to every scene of the batch (e.g. one kept from an
  * earlier autotune); takes effect at each scene's next re-binning. */
 snow_status snow_batch_set_tuning(snow_batch* b, const snow_tuning* t);
-/* Times candidate tunings (sort interval 4/8/16 x 128/256 particles per work
+/* Times candidate tunings (sort interval 4/8/12/16 x 128/256 particles per work
  * item x 1/2 CTAs per SM) on real steps of the batch and keeps the fastest.
  * The steps advance the scenes like snow_batch_step (out->steps_taken says
  * how many); dt as for snow_batch_step. */

@@ -194,8 +194,8 @@ __device__ __forceinline__ void p2g_stress(const SceneDev& S, const M3& F, const
                                            P2GParticle& q) {
   const float je = m3_det(F);
   const float e = expf(S.hardening * (1.0f - jp));
-  const float mu = S.young / (2.0f * (1.0f + S.poisson)) * e;
-  const float lam = S.young * S.poisson / ((1.0f + S.poisson) * (1.0f - 2.0f * S.poisson)) * e;
+  const float mu = S.mu0 * e;
+  const float lam = S.lambda0 * e;
   M3 D;
 #pragma unroll
   for (int c = 0; c < 3; c++)

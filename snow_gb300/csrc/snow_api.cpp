@@ -197,6 +197,13 @@ void fill_sd_params(snow_scene* s) {
   d.inv_h = 1.0f / s->p.grid_spacing;
   d.nblocks = d.bdim[0] * d.bdim[1] * d.bdim[2];
   d.young = s->p.young;
+  // mu0 = E / (2 (1 + nu)), lambda0 = E nu / ((1 + nu)(1 - 2 nu)), in the
+  // order and precision lame.include.glsl evaluates them per particle
+  {
+    const float E = s->p.young, nu = s->p.poisson;
+    d.mu0 = E / (2.0f * (1.0f + nu));
+    d.lambda0 = E * nu / ((1.0f + nu) * (1.0f - 2.0f * nu));
+  }
   d.poisson = s->p.poisson;
   d.hardening = s->p.hardening;
   d.crit_lo = 1.0f - s->p.crit_compression;
@@ -1366,11 +1373,11 @@ snow_status snow_batch_set_tuning(snow_batch* b, const snow_tuning* t) {
 // Times each candidate (sort interval x particles per work item x CTAs per
 // SM) over real steps of the batch -- one sort interval to re-bin every scene
 // with the candidate's work items and capture its graphs, then two intervals
-// (at least 8 steps) timed with events -- and keeps the fastest.
+// (at least 32 steps) timed with events -- and keeps the fastest.
 snow_status snow_batch_autotune(snow_batch* b, const double* dt, snow_tuning* out) {
   if (!b) return SNOW_EINVAL;
   snow_ctx* ctx = b->ctx;
-  static const int kIntervals[] = {4, 8, 16};
+  static const int kIntervals[] = {4, 8, 12, 16};
   static const int kItems[] = {128, 256};
   static const int kCtas[] = {1, 2};
   snow_tuning best{};
@@ -1386,7 +1393,7 @@ snow_status snow_batch_autotune(snow_batch* b, const double* dt, snow_tuning* ou
         snow_tuning t{si, im, cp, 0, 0.0};
         if ((r = snow_batch_set_tuning(b, &t))) goto done;
         if ((r = snow_batch_step(b, dt, si))) goto done;
-        const int k = std::max(8, 2 * si);
+        const int k = std::max(32, 2 * si);
         if (cudaEventRecord(e0, ctx->stream) != cudaSuccess) { r = cuda_fail(ctx, cudaGetLastError(), "event"); goto done; }
         if ((r = snow_batch_step(b, dt, k))) goto done;
         if (cudaEventRecord(e1, ctx->stream) != cudaSuccess) { r = cuda_fail(ctx, cudaGetLastError(), "event"); goto done; }

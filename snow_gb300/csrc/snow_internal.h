@@ -73,6 +73,7 @@ struct SceneDev {
   int bdim[3];
   int nblocks;
   float young, poisson, hardening, crit_lo, crit_hi, alpha;
+  float mu0, lambda0;  // Lame parameters at J_p = 1 (lame.include.glsl:11-27)
   float grav[3];
   float dt;
   int ncoll;
