@@ -3,8 +3,8 @@ reference's own GLSL compute shaders as C++ for the host cores.
 
 The reference runs its MPM step as GLSL 4.40 compute shaders
 (shader/compute/mpm/*.glsl and their #includes). No OpenGL stack exists
-on these machines, so instead of running the shaders through a driver this
-recipe turns each shader into a C++ translation unit and compiles it against
+on these machines, so instead of running the shaders through an OpenGL
+implementation this recipe turns each shader into a C++ translation unit and compiles it against
 oracle/glsl_compat.hpp, which gives the GLSL types and built-ins their GLSL
 meaning. The kernel bodies are not edited: only declarations change.
 

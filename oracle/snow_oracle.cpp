@@ -1,6 +1,6 @@
 // ORACLE / TEST INFRASTRUCTURE ONLY. The product never links, loads or calls
 // this file: tests/, __graft_entry__.smoke() and bench.py's CPU baseline use
-// it as the checker.
+// it to check results and to time the CPU.
 //
 // A CPU restatement of the snow reference's explicit MPM step (the GLSL
 // compute shaders under shader/compute/), written independently of them and

@@ -3,8 +3,8 @@
 // streams into key order and the P2G work items (home block, particle range).
 //
 // The reference has no sort (it scatters every (particle, neighbour) pair with
-// global int atomics, p2gTransfer.cpp:22-23); binning is this build's device
-// for shared-memory tiling. Cell of a particle: ivec3((x - gGridPos) /
+// global int atomics, p2gTransfer.cpp:22-23); binning is what makes the
+// shared-memory tiling of this implementation possible. Cell of a particle: ivec3((x - gGridPos) /
 // gridSpacing) as p2gTransfer.glsl:76-81 computes it (truncation toward
 // zero), clamped into the grid. Key: block-major cell index
 //   key = block(i>>2, j>>2, k>>2) * 64 + (i&3) + 4 (j&3) + 16 (k&3)
