@@ -472,11 +472,29 @@ struct Advanced {
   float jp;
 };
 
-__device__ __forceinline__ void advance_particle(const SceneDev& S, int p, const PState& ps, const float dv[3],
-                                                 const float L[3][3], const snow_collider* coll, Advanced& out) {
+// F_E, J_p and the previous SVD frame of one particle.
+struct PDef {
+  float4 fa, fb, vq;
+  float2 fc;
+};
+
+__device__ __forceinline__ PDef load_def(const SceneDev& S, int p) {
+  PDef d;
+  d.fa = S.fa[p];
+  d.fb = S.fb[p];
+  d.vq = S.vq[p];
+  d.fc = S.fc[p];
+  return d;
+}
+
+__device__ __forceinline__ void advance_particle(const SceneDev& S, int p, const PState& ps, const PDef& def,
+                                                 const float dv[3], const float L[3][3], const snow_collider* coll,
+                                                 Advanced& out) {
   M3 FE;
-  float jp;
-  load_fe(S, p, FE, jp);
+  FE.m[0][0] = def.fa.x; FE.m[0][1] = def.fa.y; FE.m[0][2] = def.fa.z;
+  FE.m[1][0] = def.fa.w; FE.m[1][1] = def.fb.x; FE.m[1][2] = def.fb.y;
+  FE.m[2][0] = def.fb.z; FE.m[2][1] = def.fb.w; FE.m[2][2] = def.fc.x;
+  const float jp = def.fc.y;
   float4 xm = ps.xm, vv = ps.vv;
   M3 step;
 #pragma unroll
@@ -486,45 +504,38 @@ __device__ __forceinline__ void advance_particle(const SceneDev& S, int p, const
   const M3 fe_trial = m3_mul(step, FE);
   M3 V;
   float lam[3];
-  const float4 q4 = S.vq[p];
-  float q[4] = {q4.x, q4.y, q4.z, q4.w};
+  float q[4] = {def.vq.x, def.vq.y, def.vq.z, def.vq.w};
   eigen_warm(fe_trial, q, V, lam);
   S.vq[p] = make_float4(q[0], q[1], q[2], q[3]);
-  const float lo2 = S.crit_lo * S.crit_lo, hi2 = S.crit_hi * S.crit_hi;
-  const bool elastic = lam[0] >= lo2 && lam[0] <= hi2 && lam[1] >= lo2 && lam[1] <= hi2 && lam[2] >= lo2 &&
-                       lam[2] <= hi2;
-  if (elastic) {
-    // every singular value inside [1 - theta_c, 1 + theta_s]: the clamp
-    // leaves F_E' = W S V^T = FE_trial and J_p as they are; the polar
-    // rotation is R = FE_trial V S^-1 V^T
-    out.fe = fe_trial;
-    M3 B = m3_mul(fe_trial, V);
+  // With FE_trial = W S V^T and B = FE_trial V = W S (columns of norm
+  // sigma_i), the clamped F_E' = W clamp(S) V^T = B diag(clamp(sigma)/sigma) V^T
+  // and the polar rotation R = W V^T = B diag(1/sigma) V^T: the sort and QR
+  // of the shader's SVD (which only serve to find W) are not needed here.
+  const M3 B = m3_mul(fe_trial, V);
+  M3 Br, Bc;
+  float ratio = 1.0f;
+  bool clamped = false;
 #pragma unroll
-    for (int c = 0; c < 3; c++) {
-      const float inv = rsqrt_nr(lam[c]);
+  for (int c = 0; c < 3; c++) {
+    const float inv = rsqrt_nr(fmaxf(lam[c], 1e-30f));
+    const float sig = lam[c] * inv;
+    const float cl = fminf(fmaxf(sig, S.crit_lo), S.crit_hi);
+    clamped = clamped || cl != sig;
+    ratio *= __fdividef(sig, cl);
+    const float sc = cl * inv;
 #pragma unroll
-      for (int r = 0; r < 3; r++) B.m[c][r] *= inv;
+    for (int r = 0; r < 3; r++) {
+      Br.m[c][r] = B.m[c][r] * inv;
+      Bc.m[c][r] = B.m[c][r] * sc;
     }
-    out.R = m3_mul_bt(B, V);
-    out.jp = jp;
-  } else {
-    M3 W, Sg;
-    svd3_from_v(fe_trial, V, W, Sg);
-    float ratio = 1.0f;
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-      const float sv = Sg.m[i][i];
-      const float cl = fminf(fmaxf(sv, S.crit_lo), S.crit_hi);
-      ratio *= __fdividef(sv, cl);
-      Sg.m[i][i] = cl;
-    }
-    out.fe = m3_mul_bt(m3_mul(W, Sg), V);
-    out.R = m3_mul_bt(W, V);
-    // det F_P' = det F_P * det(FE_trial) / det(FE'): the shader's
-    // F_P' = V S^-1 W^T (I + dt L) FE FP (particleAdvance.glsl:132) has this
-    // determinant; only det F_P is ever read (p2gTransfer.glsl:119).
-    out.jp = jp * ratio;
   }
+  out.R = m3_mul_bt(Br, V);
+  // no singular value clamped: F_E' = FE_trial exactly, J_p unchanged
+  out.fe = clamped ? m3_mul_bt(Bc, V) : fe_trial;
+  // det F_P' = det F_P * det(FE_trial) / det(FE'): the shader's
+  // F_P' = V S^-1 W^T (I + dt L) FE FP (particleAdvance.glsl:132) has this
+  // determinant; only det F_P is ever read (p2gTransfer.glsl:119).
+  out.jp = clamped ? jp * ratio : jp;
   float v[3] = {S.alpha * vv.x + dv[0], S.alpha * vv.y + dv[1], S.alpha * vv.z + dv[2]};
   const float xold[3] = {xm.x, xm.y, xm.z};
   collide(coll, S.ncoll, xold, v);
@@ -999,7 +1010,7 @@ __global__ void __launch_bounds__(kItemMax) k_g2p_advance(const SceneDev* __rest
       float dv[3], L[3][3];
       g2p_gather(sh, S, bx, by, bz, base, w, dv, L);
       Advanced adv;
-      advance_particle(S, p, ps, dv, L, coll, adv);
+      advance_particle(S, p, ps, load_def(S, p), dv, L, coll, adv);
     }
     __syncthreads();
   }
@@ -1076,8 +1087,9 @@ __global__ void __launch_bounds__(kItemMax, 2) k_g2p2g(const SceneDev* __restric
       all_weights(pg, base, w);
       float dv[3], L[3][3];
       g2p_gather(sh, S, bx, by, bz, base, w, dv, L);
+      const PDef def = load_def(S, p);
       Advanced adv;
-      advance_particle(S, p, ps, dv, L, coll, adv);
+      advance_particle(S, p, ps, def, dv, L, coll, adv);
       // P2G quantities of the advanced particle
       q.m = adv.xm.w;
       if (fabsf(q.m) <= 100.0f) {  // p2gTransfer.glsl:64-66

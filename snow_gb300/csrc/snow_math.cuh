@@ -362,14 +362,6 @@ __device__ __forceinline__ void eigen_warm(const M3& A, float q[4], M3& V, float
   lam[2] = sym.m[2][2];
 }
 
-// The rest of the SVD from eigen_warm's V: B = A V, sorted columns, Givens
-// QR (A = W S V^T, as svd3).
-__device__ __forceinline__ void svd3_from_v(const M3& A, M3& V, M3& W, M3& S) {
-  M3 B = m3_mul(A, V);
-  sort_singular(B, V);
-  qr_givens<false>(B, W, S);
-}
-
 // ---- lame.include.glsl:11-27 -------------------------------------------------
 __device__ __forceinline__ float lame_mu(float young, float poisson, float hardening, float jp) {
   return young / (2.0f * (1.0f + poisson)) * expf(hardening * (1.0f - jp));
