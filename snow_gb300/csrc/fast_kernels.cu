@@ -143,40 +143,69 @@ __device__ __forceinline__ bool node_in_grid(const SceneDev& S, int g0, int g1, 
   return g0 >= 0 && g1 >= 0 && g2 >= 0 && g0 < S.dim[0] && g1 < S.dim[1] && g2 < S.dim[2];
 }
 
-// Collider projection of gForceCompute.glsl:72-93 / particleAdvance.glsl:182-204.
+// Collider projection of gForceCompute.glsl:72-93 / particleAdvance.glsl:182-204
+// for one collider that the point x hits: the velocity relative to the
+// collider loses its normal inward part, with Coulomb friction.
+__device__ __forceinline__ void collide_hit(const snow_collider& c, const float x[3], float v[3]) {
+  float n[3] = {c.normal[0], c.normal[1], c.normal[2]};
+  if (c.type == 1) {
+    const float d[3] = {x[0] - c.pos[0], x[1] - c.pos[1], x[2] - c.pos[2]};
+    const float len = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    n[0] = d[0] / len;
+    n[1] = d[1] / len;
+    n[2] = d[2] / len;
+  }
+  const float vrel[3] = {v[0] - c.vel[0], v[1] - c.vel[1], v[2] - c.vel[2]};
+  const float vn = vrel[0] * n[0] + vrel[1] * n[1] + vrel[2] * n[2];
+  if (vn < 0.0f) {
+    const float vt[3] = {vrel[0] - n[0] * vn, vrel[1] - n[1] * vn, vrel[2] - n[2] * vn};
+    const float muvn = c.friction * vn;
+    const float lvt = sqrtf(vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2]);
+    if (lvt <= -muvn) {
+      v[0] = c.vel[0];
+      v[1] = c.vel[1];
+      v[2] = c.vel[2];
+    } else {
+      const float s = muvn / lvt;
+#pragma unroll
+      for (int k = 0; k < 3; k++) v[k] = vt[k] + s * vt[k] + c.vel[k];
+    }
+  }
+}
+
+// All colliders in order (half-plane: dot(x - c, n) <= 0; sphere: |x - c| < r).
 __device__ __forceinline__ void collide(const snow_collider* coll, int ncoll, const float x[3], float v[3]) {
   for (int i = 0; i < ncoll; i++) {
     const snow_collider c = coll[i];
-    float n[3] = {c.normal[0], c.normal[1], c.normal[2]};
     bool hit = false;
     if (c.type == 0) {
       hit = (x[0] - c.pos[0]) * c.normal[0] + (x[1] - c.pos[1]) * c.normal[1] + (x[2] - c.pos[2]) * c.normal[2] <=
             0.0f;
     } else if (c.type == 1) {
       const float d[3] = {x[0] - c.pos[0], x[1] - c.pos[1], x[2] - c.pos[2]};
-      const float len = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-      n[0] = d[0] / len;
-      n[1] = d[1] / len;
-      n[2] = d[2] / len;
-      hit = len < c.radius;
+      hit = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) < c.radius;
     }
-    if (!hit) continue;
-    const float vrel[3] = {v[0] - c.vel[0], v[1] - c.vel[1], v[2] - c.vel[2]};
-    const float vn = vrel[0] * n[0] + vrel[1] * n[1] + vrel[2] * n[2];
-    if (vn < 0.0f) {
-      const float vt[3] = {vrel[0] - n[0] * vn, vrel[1] - n[1] * vn, vrel[2] - n[2] * vn};
-      const float muvn = c.friction * vn;
-      const float lvt = sqrtf(vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2]);
-      if (lvt <= -muvn) {
-        v[0] = c.vel[0];
-        v[1] = c.vel[1];
-        v[2] = c.vel[2];
-      } else {
-        const float s = muvn / lvt;
-#pragma unroll
-        for (int k = 0; k < 3; k++) v[k] = vt[k] + s * vt[k] + c.vel[k];
-      }
+    if (hit) collide_hit(c, x, v);
+  }
+}
+
+// The same with the hit tests on a packed form of the colliders (half-plane:
+// (n, n . c), tested as n . x <= n . c; sphere: (c, r^2), tested as
+// |x - c|^2 < r^2): one 16-byte shared load per collider, the full record
+// only for the rare hit.
+__device__ __forceinline__ void collide_packed(const snow_collider* coll, const float4* hitf, const int* type,
+                                               int ncoll, const float x[3], float v[3]) {
+  for (int i = 0; i < ncoll; i++) {
+    const float4 h = hitf[i];
+    const int t = type[i];
+    bool hit = false;
+    if (t == 0) {
+      hit = fmaf(h.z, x[2], fmaf(h.y, x[1], h.x * x[0])) <= h.w;
+    } else if (t == 1) {
+      const float d0 = x[0] - h.x, d1 = x[1] - h.y, d2 = x[2] - h.z;
+      hit = fmaf(d2, d2, fmaf(d1, d1, d0 * d0)) < h.w;
     }
+    if (hit) collide_hit(coll[i], x, v);
   }
 }
 
@@ -284,6 +313,8 @@ struct ItemShared {
   int coll_scene;                    // scene whose colliders sit in coll
   uint64_t bar;
   snow_collider coll[kShColliders];
+  float4 chit[kShColliders];         // packed hit tests of the colliders
+  int ctype[kShColliders];
 };
 
 // Tile block k (0..26) around home block (bx, by, bz), or -1 outside the grid.
@@ -346,7 +377,18 @@ __device__ __forceinline__ void stage_wait(ItemShared& sh, const SceneDev& S, ui
 // Colliders of scene S into shared memory (when they fit). Ends with
 // __syncthreads.
 __device__ __forceinline__ void load_colliders(ItemShared& sh, const SceneDev& S) {
-  if (S.ncoll <= kShColliders && threadIdx.x < S.ncoll) sh.coll[threadIdx.x] = S.coll[threadIdx.x];
+  if (S.ncoll <= kShColliders && threadIdx.x < S.ncoll) {
+    const snow_collider c = S.coll[threadIdx.x];
+    sh.coll[threadIdx.x] = c;
+    sh.ctype[threadIdx.x] = c.type;
+    float4 h = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (c.type == 0)
+      h = make_float4(c.normal[0], c.normal[1], c.normal[2],
+                      fmaf(c.normal[2], c.pos[2], fmaf(c.normal[1], c.pos[1], c.normal[0] * c.pos[0])));
+    else if (c.type == 1)
+      h = make_float4(c.pos[0], c.pos[1], c.pos[2], c.radius * c.radius);
+    sh.chit[threadIdx.x] = h;
+  }
   __syncthreads();
 }
 
@@ -488,7 +530,7 @@ __device__ __forceinline__ PDef load_def(const SceneDev& S, int p) {
 }
 
 __device__ __forceinline__ void advance_particle(const SceneDev& S, int p, const PState& ps, const PDef& def,
-                                                 const float dv[3], const float L[3][3], const snow_collider* coll,
+                                                 const float dv[3], const float L[3][3], const ItemShared& sh,
                                                  Advanced& out) {
   M3 FE;
   FE.m[0][0] = def.fa.x; FE.m[0][1] = def.fa.y; FE.m[0][2] = def.fa.z;
@@ -538,7 +580,10 @@ __device__ __forceinline__ void advance_particle(const SceneDev& S, int p, const
   out.jp = clamped ? jp * ratio : jp;
   float v[3] = {S.alpha * vv.x + dv[0], S.alpha * vv.y + dv[1], S.alpha * vv.z + dv[2]};
   const float xold[3] = {xm.x, xm.y, xm.z};
-  collide(coll, S.ncoll, xold, v);
+  if (S.ncoll <= kShColliders)
+    collide_packed(sh.coll, sh.chit, sh.ctype, S.ncoll, xold, v);
+  else
+    collide(S.coll, S.ncoll, xold, v);
   xm.x += S.dt * v[0];
   xm.y += S.dt * v[1];
   xm.z += S.dt * v[2];
@@ -998,7 +1043,6 @@ __global__ void __launch_bounds__(kItemMax) k_g2p_advance(const SceneDev* __rest
     if (threadIdx.x < 32) stage_issue(sh, S, tile_slot(S, it, threadIdx.x));
     load_colliders(sh, S);
     stage_wait(sh, S, phase);
-    const snow_collider* coll = S.ncoll <= kShColliders ? sh.coll : S.coll;
     for (int i = threadIdx.x; i < it.z; i += blockDim.x) {
       const int p = it.y + i;
       const PState ps = load_state(S, p);
@@ -1010,7 +1054,7 @@ __global__ void __launch_bounds__(kItemMax) k_g2p_advance(const SceneDev* __rest
       float dv[3], L[3][3];
       g2p_gather(sh, S, bx, by, bz, base, w, dv, L);
       Advanced adv;
-      advance_particle(S, p, ps, load_def(S, p), dv, L, coll, adv);
+      advance_particle(S, p, ps, load_def(S, p), dv, L, sh, adv);
     }
     __syncthreads();
   }
@@ -1068,7 +1112,6 @@ __global__ void __launch_bounds__(kItemMax, 2) k_g2p2g(const SceneDev* __restric
     }
     int bx, by, bz;
     home_coords(S, it.x, bx, by, bz);
-    const snow_collider* coll = S.ncoll <= kShColliders ? sh.coll : S.coll;
     const int i = threadIdx.x;
     const bool mine = i < min(it.z, kItemMax);
     const int p = it.y + i;
@@ -1089,7 +1132,7 @@ __global__ void __launch_bounds__(kItemMax, 2) k_g2p2g(const SceneDev* __restric
       g2p_gather(sh, S, bx, by, bz, base, w, dv, L);
       const PDef def = load_def(S, p);
       Advanced adv;
-      advance_particle(S, p, ps, def, dv, L, coll, adv);
+      advance_particle(S, p, ps, def, dv, L, sh, adv);
       // P2G quantities of the advanced particle
       q.m = adv.xm.w;
       if (fabsf(q.m) <= 100.0f) {  // p2gTransfer.glsl:64-66
