@@ -154,7 +154,8 @@ void snow_scene_destroy(snow_scene* s);
  * most (in SNOW_MODE_FAST the output pool counted at its largest). */
 size_t snow_scene_footprint(const snow_params* p, size_t n);
 
-/* x, v: N x 3; m: N; FE, FP: N x 9 row-major or NULL for identity. */
+/* x, v: N x 3; m: N; FE, FP: N x 9 row-major or NULL for identity; N >= 1
+ * (SNOW_EINVAL otherwise). */
 snow_status snow_scene_upload(snow_scene* s, const float* x, const float* v, const float* m, const float* FE,
                               const float* FP, size_t n);
 /* The reference's buffers as ParticleSystem::initSSBO fills them: pxm N x

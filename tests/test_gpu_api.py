@@ -152,3 +152,32 @@ def test_queued_statistics_match_the_waiting_read(ctx):
     with pytest.raises(N.SnowError) as e:
         ctx.stats_read(0)  # already read
     assert e.value.status == -7
+
+
+@gpu
+def test_empty_upload_is_rejected(ctx):
+    from snow_gb300 import api, native as N
+    s = scenes.small_scene(n=1, grid_edge=16, seed=97)
+    s.x, s.v, s.m = s.x[:0], s.v[:0], s.m[:0]
+    with pytest.raises(N.SnowError) as e:
+        api.SimScene(ctx, s).upload()
+    assert e.value.status == -1  # SNOW_EINVAL: a scene holds at least one particle
+
+
+@gpu
+@pytest.mark.parametrize("n", [1, 2])
+def test_tiny_scenes_step_in_both_modes(ctx, n):
+    """One- and two-particle scenes: upload, init, steps, statistics and
+    download work (the reference's smallest scene is one particle)."""
+    from snow_gb300 import api, native as N
+    s = scenes.small_scene(n=max(n, 1), grid_edge=16, seed=97)
+    s.x, s.v, s.m = s.x[:n], s.v[:n], s.m[:n]
+    for mode in (N.MODE_FAST, N.MODE_REFERENCE):
+        sim = api.SimScene(ctx, s, mode=mode).upload().init().step(s.dt, 5)
+        st = sim.stats()
+        out = sim.download()
+        assert st["n"] == n and st["nonfinite"] == 0
+        assert out["x"].shape == (n, 3)
+        if n:
+            assert np.all(np.isfinite(out["x"])) and out["x"][:, 1].max() < s.x[:, 1].max()  # falling
+        sim.close()
