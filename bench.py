@@ -48,7 +48,7 @@ BYTES_GRID = (0, 40)
 # other workloads report null: DRAM bytes (read + write) per launch, and warp
 # instructions per launch for the issue roofline.
 TRAFFIC_MEASURED = {(1 << 20, 256): 144.5e6}
-INSTRUCTIONS_MEASURED = {(1 << 20, 256): 181.1e6}
+INSTRUCTIONS_MEASURED = {(1 << 20, 256): 168.6e6}
 # warp-instruction issue peak: 152 SMs x 4 schedulers x 2.07 GHz
 ISSUE_PEAK = 152 * 4 * 2.07e9
 
