@@ -39,6 +39,12 @@ struct snow_ctx {
   bool stat_pending[SNOW_STATS_SLOTS] = {};
   int* h_counters = nullptr;      // pinned, kCounterStride ints
   cudaEvent_t ev[8] = {};
+  // side streams for independent per-scene work inside a batch step (the
+  // re-binning of several scenes runs as parallel graph branches)
+  static constexpr int kAux = 8;
+  cudaStream_t aux[kAux] = {};
+  cudaEvent_t fork_ev = nullptr;
+  cudaEvent_t join_ev[kAux] = {};
   // live children, destroyed with the context if the caller did not
   std::set<snow_scene*> scenes;
   std::set<snow_batch*> batches;
@@ -534,6 +540,11 @@ snow_status snow_ctx_create(int device, size_t hbm_budget_bytes, snow_ctx** out)
     e = cudaEventCreateWithFlags(&ctx->stat_ev[i], cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_counters, kCounterStride * sizeof(int));
   for (int i = 0; i < 8 && e == cudaSuccess; i++) e = cudaEventCreate(&ctx->ev[i]);
+  for (int i = 0; i < snow_ctx::kAux && e == cudaSuccess; i++) {
+    e = cudaStreamCreateWithFlags(&ctx->aux[i], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->join_ev[i], cudaEventDisableTiming);
+  }
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming);
   if (e != cudaSuccess) {
     cudaGetLastError();
     snow_ctx_destroy(ctx);
@@ -550,6 +561,14 @@ void snow_ctx_destroy(snow_ctx* ctx) {
   while (!ctx->scenes.empty()) snow_scene_destroy(*ctx->scenes.begin());
   for (int i = 0; i < 8; i++)
     if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+  for (int i = 0; i < snow_ctx::kAux; i++) {
+    if (ctx->aux[i]) {
+      cudaStreamSynchronize(ctx->aux[i]);
+      cudaStreamDestroy(ctx->aux[i]);
+    }
+    if (ctx->join_ev[i]) cudaEventDestroy(ctx->join_ev[i]);
+  }
+  if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
   for (int i = 0; i < SNOW_STATS_SLOTS; i++)
     if (ctx->stat_ev[i]) cudaEventDestroy(ctx->stat_ev[i]);
   if (ctx->d_stats) cudaFree(ctx->d_stats);
@@ -1281,9 +1300,25 @@ void batch_enqueue_step(snow_batch* b, int phase, int interval, cudaStream_t st)
   int* active = pre + (n + 1);
   int* blocks = pre + 3 * (n + 1);
   fast_begin_step(b->d_scenes, n, true, st);
-  // re-bin a staggered subset of scenes each step
+  // re-bin a staggered subset of scenes each step; the scenes' binnings are
+  // independent, so they run on side streams (parallel branches of the
+  // step's graph) and join before the compaction
+  std::vector<int> bins;
   for (int i = 0; i < n; i++)
-    if ((i % interval) == phase) fast_bin(b->scenes[i], st);
+    if ((i % interval) == phase) bins.push_back(i);
+  snow_ctx* ctx = b->ctx;
+  if (bins.size() < 2) {
+    for (int i : bins) fast_bin(b->scenes[i], st);
+  } else {
+    const int lanes = std::min((int)bins.size(), (int)snow_ctx::kAux);
+    cudaEventRecord(ctx->fork_ev, st);
+    for (int k = 0; k < lanes; k++) cudaStreamWaitEvent(ctx->aux[k], ctx->fork_ev, 0);
+    for (size_t k = 0; k < bins.size(); k++) fast_bin(b->scenes[bins[k]], ctx->aux[k % lanes]);
+    for (int k = 0; k < lanes; k++) {
+      cudaEventRecord(ctx->join_ev[k], ctx->aux[k]);
+      cudaStreamWaitEvent(st, ctx->join_ev[k], 0);
+    }
+  }
   fast_compact(b->d_scenes, blocks, n, b->total_blocks, items, active, st);
   fast_grid(b->d_scenes, active, n, grid_ctas(), false, st);
   fast_g2p2g(b->d_scenes, items, n, item_ctas(b->scenes[0]->tune), st);
