@@ -203,10 +203,16 @@ __global__ void k_keys(const SceneDev* __restrict__ sd, uint32_t* __restrict__ k
   }
 }
 
+// Gathers the particle streams into key order (into the scratch copies;
+// k_heads copies them back) and zeroes the item and home counters.
 __global__ void k_permute(const SceneDev* __restrict__ sd, const uint32_t* __restrict__ perm, float4* __restrict__ xm,
                           float4* __restrict__ vv, float4* __restrict__ fa, float4* __restrict__ fb,
                           float2* __restrict__ fc, uint32_t* __restrict__ pid, float4* __restrict__ vq) {
   const SceneDev& S = *sd;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    S.counters[CNT_ITEMS] = 0;
+    S.counters[CNT_HOME] = 0;
+  }
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
     const uint32_t src = perm[i];
     xm[i] = S.xm[src];
@@ -219,11 +225,23 @@ __global__ void k_permute(const SceneDev* __restrict__ sd, const uint32_t* __res
   }
 }
 
+// Block ranges of the sorted keys and the list of home blocks; also copies
+// the permuted streams back from the scratch copies.
 __global__ void k_heads(const SceneDev* __restrict__ sd, const uint32_t* __restrict__ keys, int* __restrict__ bstart,
-                        int* __restrict__ bend, int* __restrict__ home) {
+                        int* __restrict__ bend, int* __restrict__ home, const float4* __restrict__ xm,
+                        const float4* __restrict__ vv, const float4* __restrict__ fa, const float4* __restrict__ fb,
+                        const float2* __restrict__ fc, const uint32_t* __restrict__ pid,
+                        const float4* __restrict__ vq) {
   const SceneDev& S = *sd;
   const int n = S.n;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    S.xm[i] = xm[i];
+    S.vv[i] = vv[i];
+    S.fa[i] = fa[i];
+    S.fb[i] = fb[i];
+    S.fc[i] = fc[i];
+    S.pid[i] = pid[i];
+    S.vq[i] = vq[i];
     const uint32_t b = keys[i] >> 6;
     if (i == 0 || (keys[i - 1] >> 6) != b) {
       bstart[b] = i;
@@ -295,16 +313,8 @@ void fast_apply_bins(const SceneDev& sd, const SceneDev* sd_dev, BinScratch& b, 
   const size_t n = (size_t)sd.n;
   k_permute<<<grid_for(n, 256, 8), 256, 0, st>>>(sd_dev, b.vals[0], b.tmp4[0], b.tmp4[1], b.tmp4[2], b.tmp4[3],
                                                   b.tmp2, b.tmp_pid, b.tmp4[4]);
-  cudaMemcpyAsync(sd.xm, b.tmp4[0], n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
-  cudaMemcpyAsync(sd.vv, b.tmp4[1], n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
-  cudaMemcpyAsync(sd.fa, b.tmp4[2], n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
-  cudaMemcpyAsync(sd.fb, b.tmp4[3], n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
-  cudaMemcpyAsync(sd.fc, b.tmp2, n * sizeof(float2), cudaMemcpyDeviceToDevice, st);
-  cudaMemcpyAsync(sd.pid, b.tmp_pid, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st);
-  cudaMemcpyAsync(sd.vq, b.tmp4[4], n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
-  cudaMemsetAsync(sd.counters + CNT_ITEMS, 0, sizeof(int), st);
-  cudaMemsetAsync(sd.counters + CNT_HOME, 0, sizeof(int), st);
-  k_heads<<<grid_for(n, 256, 8), 256, 0, st>>>(sd_dev, b.keys[0], b.bstart, b.bend, b.home);
+  k_heads<<<grid_for(n, 256, 8), 256, 0, st>>>(sd_dev, b.keys[0], b.bstart, b.bend, b.home, b.tmp4[0], b.tmp4[1],
+                                                b.tmp4[2], b.tmp4[3], b.tmp2, b.tmp_pid, b.tmp4[4]);
   const size_t maxhome = n < (size_t)sd.nblocks ? n : (size_t)sd.nblocks;
   k_items<<<grid_for(maxhome, 256, 4), 256, 0, st>>>(sd_dev, b.bstart, b.bend, b.home, items_max);
 }
