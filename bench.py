@@ -162,16 +162,21 @@ def bench_ours(args, local_rank, barrier=lambda: None):
     sim.upload().init()
     n = s.n
     dt = s.dt
-    # work split chosen by the autotuner (on real steps of this scene), or
-    # given with --tuning
+    # work split chosen by the autotuner (on real steps of a copy of this
+    # scene), or given with --tuning
     if args.tuning:
         si, im, cp = (int(v) for v in args.tuning.split(","))
         sim.set_tuning(si, im, cp)
         tuning = dict(sort_interval=si, items_max=im, ctas_per_sm=cp, steps_taken=0)
     else:
-        tb = api.Batch(ctx, [sim])
+        # tuned on a scratch copy, so the timed run starts from the scene's
+        # initial state
+        scratch = api.SimScene(ctx, s, mode=N.MODE_FAST).upload().init()
+        tb = api.Batch(ctx, [scratch])
         tuning = tb.autotune([dt])
         tb.close()
+        scratch.close()
+        sim.set_tuning(tuning["sort_interval"], tuning["items_max"], tuning["ctas_per_sm"])
     # active grid nodes (nodes with mass) after one step, for the roofline
     sim.step(dt, 1)
     ctx.synchronize()
