@@ -346,9 +346,17 @@ def bench_batched(args, local_rank, at_scale=False):
         sim.close()
     del plain
 
+    # the work split is tuned on scratch copies (autotuning takes real steps),
+    # so the timed batch covers the same steps as the per-scene loop
+    scratch = [api.SimScene(ctx, s).upload().init() for s in scs]
+    tb = api.Batch(ctx, scratch)
+    tuning = tb.autotune(dts)
+    tb.close()
+    for sim in scratch:
+        sim.close()
+    del scratch
     sims = [api.SimScene(ctx, s).upload().init() for s in scs]
-    batch = api.Batch(ctx, sims)
-    tuning = batch.autotune(dts)  # times candidate work splits on real steps
+    batch = api.Batch(ctx, sims).set_tuning(tuning["sort_interval"], tuning["items_max"], tuning["ctas_per_sm"])
     for _ in range(W):
         batch.step(1, dts)
     batch_ms = timed(lambda: batch.step(K, dts))
@@ -360,7 +368,7 @@ def bench_batched(args, local_rank, at_scale=False):
     # copies of the check scenes to the same step count
     for i in check:
         p = api.SimScene(ctx, scs[i]).upload().init()
-        p.step(dts[i], tuning["steps_taken"] + W + K + 3)
+        p.step(dts[i], W + K + 3)
         a, b = p.download(), sims[i].download()
         diff = max(diff, float(np.abs(a["x"] - b["x"]).max()))
         p.close()
