@@ -827,6 +827,7 @@ snow_status snow_scene_init(snow_scene* s) {
 snow_status snow_dispatch(snow_scene* s, int kernel, double dt) {
   if (!s) return SNOW_EINVAL;
   snow_ctx* ctx = s->ctx;
+  if (!(dt >= 0.0) || !std::isfinite(dt)) return fail(ctx, SNOW_EINVAL, "snow_dispatch: dt must be finite and >= 0");
   if (!s->uploaded) return fail(ctx, SNOW_ESTATE, "dispatch before upload");
   const float fdt = (float)dt;  // glUniform1f of the double dt
   cudaStream_t st = ctx->stream;
@@ -896,6 +897,7 @@ snow_status snow_dispatch(snow_scene* s, int kernel, double dt) {
 snow_status snow_scene_step(snow_scene* s, double dt, int n_steps) {
   if (!s || n_steps < 0) return SNOW_EINVAL;
   snow_ctx* ctx = s->ctx;
+  if (!(dt >= 0.0) || !std::isfinite(dt)) return fail(ctx, SNOW_EINVAL, "snow_scene_step: dt must be finite and >= 0");
   if (!s->initialized) return fail(ctx, SNOW_ESTATE, "snow_scene_step before snow_scene_init");
   const float fdt = (float)dt;
   cudaStream_t st = ctx->stream;
@@ -1329,6 +1331,9 @@ void batch_enqueue_step(snow_batch* b, int phase, int interval, cudaStream_t st)
 snow_status snow_batch_step(snow_batch* b, const double* dt, int n_steps) {
   if (!b || n_steps < 0) return SNOW_EINVAL;
   snow_ctx* ctx = b->ctx;
+  if (dt)
+    for (size_t i = 0; i < b->scenes.size(); i++)
+      if (!(dt[i] >= 0.0) || !std::isfinite(dt[i])) return fail(ctx, SNOW_EINVAL, "snow_batch_step: bad dt");
   cudaStream_t st = ctx->stream;
   for (size_t i = 0; i < b->scenes.size(); i++) {
     snow_scene* s = b->scenes[i];

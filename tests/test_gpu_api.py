@@ -155,6 +155,19 @@ def test_queued_statistics_match_the_waiting_read(ctx):
 
 
 @gpu
+def test_bad_time_steps_are_rejected(ctx):
+    from snow_gb300 import api, native as N
+    s = scenes.small_scene(n=500, grid_edge=16, seed=98)
+    sim = api.SimScene(ctx, s).upload().init()
+    for dt in (-1e-4, float("nan"), float("inf")):
+        with pytest.raises(N.SnowError) as e:
+            sim.step(dt, 1)
+        assert e.value.status == -1
+    sim.step(s.dt, 1)  # the scene is unaffected
+    assert sim.stats()["nonfinite"] == 0
+
+
+@gpu
 def test_empty_upload_is_rejected(ctx):
     from snow_gb300 import api, native as N
     s = scenes.small_scene(n=1, grid_edge=16, seed=97)
