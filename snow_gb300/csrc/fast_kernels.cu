@@ -309,7 +309,6 @@ struct ItemShared {
   int ncells;
   int4 item_q[2];                    // this and the next work item of the CTA
   int scene_q[2];                    // ... and their scenes
-  int next_slots[27];                // pool slots of the next item's tile blocks
   int coll_scene;                    // scene whose colliders sit in coll
   uint64_t bar;
   snow_collider coll[kShColliders];
@@ -1100,15 +1099,15 @@ __global__ void __launch_bounds__(kItemMax, 2) k_g2p2g(const SceneDev* __restric
     }
     const int4 it = sh.item_q[par];
     const int un = u + gridDim.x;
+    // the next item's descriptor and pool slots: loaded now, used (and put
+    // in shared memory) after this item's per-cell sums, so the loads'
+    // latency overlaps this item's work instead of delaying the last warp
+    int sn = 0, slot = -1;
+    int4 itn = make_int4(0, 0, 0, 0);
     if (lastw && un < total) {
-      const int sn = find_scene(item_prefix, nscenes, un);
-      const int4 itn = scenes[sn].items[un - item_prefix[sn]];
-      const int slot = tile_slot(scenes[sn], itn, lane);
-      if (lane < 27) sh.next_slots[lane] = slot;
-      if (lane == 0) {
-        sh.item_q[par ^ 1] = itn;
-        sh.scene_q[par ^ 1] = sn;
-      }
+      sn = find_scene(item_prefix, nscenes, un);
+      itn = scenes[sn].items[un - item_prefix[sn]];
+      slot = tile_slot(scenes[sn], itn, lane);
     }
     int bx, by, bz;
     home_coords(S, it.x, bx, by, bz);
@@ -1148,7 +1147,13 @@ __global__ void __launch_bounds__(kItemMax, 2) k_g2p2g(const SceneDev* __restric
       }
     }
     p2g_tile_pass<false>(sh, S, bx, by, bz, have, q, wn, nbase, [&] {
-      if (lastw && un < total) stage_issue(sh, scenes[sh.scene_q[par ^ 1]], lane < 27 ? sh.next_slots[lane] : -1);
+      if (lastw && un < total) {
+        if (lane == 0) {
+          sh.item_q[par ^ 1] = itn;
+          sh.scene_q[par ^ 1] = sn;
+        }
+        stage_issue(sh, scenes[sn], lane < 27 ? slot : -1);
+      }
     });
   }
 }
