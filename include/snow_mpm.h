@@ -87,6 +87,14 @@ typedef struct snow_params {
   float gravity[3];       /* (0, -9.81, 0) in gForceCompute.glsl  */
   int mode;               /* snow_mode                            */
   int sort_interval;      /* FAST: re-bin particles every k steps (0 = library default) */
+  /* Semi-implicit velocity update (the reference's SemiImplicitTimeUpdate,
+   * an empty stub in semiimplicittimeupdate.cpp:3-5; Stomakhin et al. 2013,
+   * eq. 9): with implicit_beta > 0 each step solves
+   * (M + beta dt^2 K) v = M v* on the grid by conjugate residuals before
+   * G2P. 0 keeps the explicit step. FAST mode only. */
+  float implicit_beta;      /* 0 (explicit) .. 1 (backward Euler)             */
+  float implicit_tolerance; /* stop at |r| <= tol |M^1/2 v*| (0 = 1e-5)      */
+  int implicit_max_iters;   /* at most this many iterations a step (0 = 50, <= 128) */
 } snow_params;
 
 /* One collision object: the reference's cx = (pos, type), cv = (vel,
@@ -209,6 +217,17 @@ size_t snow_scene_size(const snow_scene* s);
 snow_status snow_scene_cell_keys(snow_scene* s, uint32_t* keys, uint32_t* perm);
 
 snow_status snow_scene_phase_times(snow_scene* s, snow_phase_times* out, int reset);
+
+/* The semi-implicit solve of the last step: iterations taken and the
+ * relative residuals |r|/|M^1/2 v*| of the mass-scaled system before and
+ * after (waits for the stream; SNOW_EUNSUPPORTED for an explicit scene). */
+typedef struct snow_solver_report {
+  int iterations;
+  int max_iters;
+  double residual;
+  double initial_residual;
+} snow_solver_report;
+snow_status snow_scene_solver_report(snow_scene* s, snow_solver_report* out);
 
 /* ---- Serving ---------------------------------------------------------------
  * A worker thread that owns one context and runs simulation jobs: it admits

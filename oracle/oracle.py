@@ -19,7 +19,7 @@ import numpy as np
 from . import build as _build
 
 FAITHFUL32, EXACT64, EXACT32, FAITHFUL64 = 0, 1, 2, 3
-PH_RIGID, PH_RESET, PH_P2G, PH_GRID, PH_G2P, PH_ADVANCE, PH_GMASS, PH_PVOLUME = range(8)
+PH_RIGID, PH_RESET, PH_P2G, PH_GRID, PH_G2P, PH_ADVANCE, PH_GMASS, PH_PVOLUME, PH_IMPLICIT = range(9)
 
 _lib = None
 _ref = None
@@ -53,6 +53,10 @@ def lib():
         _lib.oracle_svd.argtypes = [dp, dp, dp, dp, C.c_int, C.c_int, C.c_int]
         _lib.oracle_lame.argtypes = [C.c_float, C.c_float, C.c_float, C.c_float, fp, fp]
         _lib.oracle_cell_keys.argtypes = [fp, C.c_size_t, fp, ip, C.c_float, up, up, up]
+        _lib.oracle_set_implicit.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_int]
+        _lib.oracle_hessian.argtypes = [C.c_void_p, dp, dp]
+        _lib.oracle_force_at.argtypes = [C.c_void_p, dp, C.c_double, dp]
+        _lib.oracle_solver_report.argtypes = [C.c_void_p, dp]
     return _lib
 
 
@@ -226,6 +230,30 @@ class OracleSim:
         out = np.zeros((max(1, len(self.scene.colliders)), 3))
         self.L.oracle_download_colliders(self.h, _p(out, C.c_double))
         return out[:len(self.scene.colliders)]
+
+    # ---- semi-implicit velocity update (EXACT modes) ----
+    def set_implicit(self, beta, tol=1e-6, max_iters=50):
+        self.L.oracle_set_implicit(self.h, float(beta), float(tol), int(max_iters))
+        return self
+
+    def hessian(self, u):
+        """K u for a grid field u (G x 3) at the current particle state."""
+        u = np.ascontiguousarray(u, np.float64).reshape(self.G, 3)
+        out = np.zeros((self.G, 3))
+        self.L.oracle_hessian(self.h, _p(u, C.c_double), _p(out, C.c_double))
+        return out
+
+    def force_at(self, u, eps):
+        """Grid force with every particle's F_E deformed by the grid field eps u."""
+        u = np.ascontiguousarray(u, np.float64).reshape(self.G, 3)
+        out = np.zeros((self.G, 3))
+        self.L.oracle_force_at(self.h, _p(u, C.c_double), float(eps), _p(out, C.c_double))
+        return out
+
+    def solver_report(self):
+        out = np.zeros(3)
+        self.L.oracle_solver_report(self.h, _p(out, C.c_double))
+        return dict(iterations=int(out[0]), residual=float(out[1]), initial_residual=float(out[2]))
 
 
 class RefSim:

@@ -32,6 +32,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <limits>
 #include <numeric>
 #include <vector>
 
@@ -348,10 +349,16 @@ struct OracleBase {
   virtual void download_accumulators(double* vpic, double* dv) const = 0;
   virtual void download_colliders(double* pos) const = 0;
   virtual void set_density(const double* rho) = 0;
+  // semi-implicit velocity update (EXACT modes only)
+  virtual void set_implicit(double beta, double tol, int max_iters) = 0;
+  virtual void hessian(const double* u, double* out) const = 0;
+  virtual void force_at(const double* u, double eps, double* out) const = 0;
+  virtual void solver_report(double* out) const = 0;
 };
 
 enum {
   PH_RIGID = 0, PH_RESET = 1, PH_P2G = 2, PH_GRID = 3, PH_G2P = 4, PH_ADVANCE = 5, PH_GMASS = 6, PH_PVOLUME = 7,
+  PH_IMPLICIT = 8,
 };
 
 template <class T> inline void atomic_add(T& dst, T v, bool par) {
@@ -802,6 +809,246 @@ struct Oracle : OracleBase {
     }
   }
 
+  // ---- semi-implicit velocity update ------------------------------------
+  // The reference ships SemiImplicitTimeUpdate as an empty stub
+  // (src/snow/simulation/timeUpdate/semiimplicittimeupdate.cpp:3-5). This
+  // restates the scheme of Stomakhin et al. 2013 (sec. 4, eq. 9, and the
+  // force differential below it) on top of the explicit step: after the grid
+  // update has formed v* (with colliders), solve
+  //     (M + beta dt^2 K) v = M v*
+  // by conjugate residuals, K u = sum_p V0_p dP(F_p; G_p F_p) F_p^T grad w_ip,
+  // G_p = sum_j u_j (grad w_jp)^T, then apply the colliders to v again. The
+  // weight gradients are the explicit force's own (grid units, as
+  // p2gTransfer.glsl:121-146 uses them), so K is the derivative of the force
+  // the explicit step applies. Only the EXACT modes (no fixed point) solve.
+  R imp_beta = R(0), imp_tol = R(1e-6);
+  int imp_maxit = 0;
+  int imp_iters = 0;
+  double imp_res = 0.0, imp_res0 = 0.0;
+
+  void set_implicit(double beta, double tol, int max_iters) override {
+    imp_beta = R(beta);
+    imp_tol = R(tol);
+    imp_maxit = max_iters;
+  }
+  void solver_report(double* out) const override {
+    out[0] = imp_iters;
+    out[1] = imp_res;
+    out[2] = imp_res0;
+  }
+
+  // Calls fn(node, w, grad w) for each in-grid stencil node of particle p
+  // (the neighbour order and distances of p2gTransfer.glsl:83-91,121-122).
+  template <class Fn> void stencil(size_t p, Fn fn) const {
+    const V3<R> pg = particle_in_grid(p);
+    const int base[3] = {(int)pg[0], (int)pg[1], (int)pg[2]};
+    for (int y = 0; y < 64; y++) {
+      int o[3];
+      neighbour_offset(y, o);
+      const int g[3] = {base[0] + o[0], base[1] + o[1], base[2] + o[2]};
+      if (!in_grid(g)) continue;
+      const V3<R> d = v3<R>(R(g[0]) - pg[0], R(g[1]) - pg[1], R(g[2]) - pg[2]);
+      fn(node_index(g), weight3(d), weight3_grad(vneg(d)));
+    }
+  }
+  // The particles that carry a stress force (p2gTransfer.glsl:64-66,126).
+  bool has_force(size_t p) const { return !(std::fabs(m[p]) > R(100)) && density(p) > R(0); }
+
+  // Cofactor matrix J F^-T: columns f1 x f2, f2 x f0, f0 x f1.
+  static V3<R> cross3(const V3<R>& a, const V3<R>& b) {
+    return v3<R>(a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]);
+  }
+  static M3<R> cofactor(const M3<R>& F) {
+    M3<R> C;
+    C[0] = cross3(F[1], F[2]);
+    C[1] = cross3(F[2], F[0]);
+    C[2] = cross3(F[0], F[1]);
+    return C;
+  }
+  // First Piola-Kirchhoff stress of the fixed-corotated energy,
+  // P = 2 mu (F - R) + lambda (J - 1) J F^-T; P F^T is the shader's stress.
+  // R is the polar rotation to working precision (Newton's iteration
+  // R <- (R + R^-T) / 2, which converges quadratically for det F > 0), so
+  // that finite differences of the force resolve the differential below
+  // rather than the approximate SVD's residual.
+  static M3<R> polar_rotation(const M3<R>& F) {
+    M3<R> Rp = F;
+    for (int it = 0; it < 60; it++) {
+      const M3<R> inv_t = msmul(R(1) / mdet(Rp), cofactor(Rp));
+      const M3<R> next = msmul(R(0.5), madd(Rp, inv_t));
+      R delta = R(0);
+      for (int c = 0; c < 3; c++)
+        for (int r = 0; r < 3; r++) delta = std::max(delta, std::fabs(next[c][r] - Rp[c][r]));
+      Rp = next;
+      if (delta <= R(4) * std::numeric_limits<R>::epsilon()) break;
+    }
+    return Rp;
+  }
+  M3<R> piola(const M3<R>& F, R mu_, R lam_) const {
+    const M3<R> Rp = polar_rotation(F);
+    return madd(msmul(R(2) * mu_, msub(F, Rp)), msmul(lam_ * (mdet(F) - R(1)), cofactor(F)));
+  }
+  // dP(F; dF). The rotation's differential: with F = W S V^T and
+  // G = W^T dF V, dR = W X V^T, X skew with X_ij = (G_ij - G_ji)/(s_i + s_j)
+  // (from R^T dF - dF^T R = X' S + S X' in the frame of V).
+  M3<R> stress_differential(const M3<R>& F, R mu_, R lam_, const M3<R>& dF) const {
+    M3<R> W, S, V;
+    svd3(F, W, S, V, vround);
+    const M3<R> Gm = mmul(mmul(mtrans(W), dF), V);
+    M3<R> X = mdiag<R>(0);
+    for (int i = 0; i < 3; i++)
+      for (int j = i + 1; j < 3; j++) {
+        const R xij = (Gm[j][i] - Gm[i][j]) / (S[i][i] + S[j][j]);  // row i, column j
+        X[j][i] = xij;
+        X[i][j] = -xij;
+      }
+    const M3<R> dR = mmul(mmul(W, X), mtrans(V));
+    const M3<R> C = cofactor(F);
+    R dJ = R(0);
+    for (int c = 0; c < 3; c++)
+      for (int r = 0; r < 3; r++) dJ += C[c][r] * dF[c][r];
+    M3<R> dC;
+    dC[0] = vadd(cross3(dF[1], F[2]), cross3(F[1], dF[2]));
+    dC[1] = vadd(cross3(dF[2], F[0]), cross3(F[2], dF[0]));
+    dC[2] = vadd(cross3(dF[0], F[1]), cross3(F[0], dF[1]));
+    return madd(msmul(R(2) * mu_, msub(dF, dR)),
+                madd(msmul(lam_ * dJ, C), msmul(lam_ * (mdet(F) - R(1)), dC)));
+  }
+  // G_p = sum_j u_j (grad w_jp)^T.
+  M3<R> particle_gradient(size_t p, const std::vector<V3<R>>& u) const {
+    M3<R> Gm = mdiag<R>(0);
+    stencil(p, [&](size_t gI, R, const V3<R>& gw) {
+      for (int c = 0; c < 3; c++)
+        for (int r = 0; r < 3; r++) Gm[c][r] += u[gI][r] * gw[c];
+    });
+    return Gm;
+  }
+  // out = K u on the dense grid.
+  void hessian_action(const std::vector<V3<R>>& u, std::vector<V3<R>>& out) const {
+    out.assign(G, v3<R>(0, 0, 0));
+    const bool pp = par();
+#pragma omp parallel for schedule(dynamic, 256) num_threads(threads) if (pp)
+    for (long long pl = 0; pl < (long long)N; pl++) {
+      const size_t p = (size_t)pl;
+      if (!has_force(p)) continue;
+      const R jpp = mdet(FP[p]);
+      const M3<R> dF = mmul(particle_gradient(p, u), FE[p]);
+      const M3<R> dP = stress_differential(FE[p], mu(jpp), lambda(jpp), dF);
+      const M3<R> A = msmul(m[p] / density(p), mmul(dP, mtrans(FE[p])));
+      stencil(p, [&](size_t gI, R, const V3<R>& gw) {
+        const V3<R> f = mvmul(A, gw);
+        for (int k = 0; k < 3; k++) atomic_add(out[gI][k], f[k], pp);
+      });
+    }
+  }
+  // The grid force at the deformed positions x_i + eps u_i:
+  // f_i = -sum_p V0 P((I + eps G_p) F_p) F_p^T grad w_ip (finite-difference
+  // checks of K: K u = -(f(eps) - f(-eps)) / (2 eps) + O(eps^2)).
+  void force_at_grid(const std::vector<V3<R>>& u, R eps, std::vector<V3<R>>& out) const {
+    out.assign(G, v3<R>(0, 0, 0));
+    const bool pp = par();
+#pragma omp parallel for schedule(dynamic, 256) num_threads(threads) if (pp)
+    for (long long pl = 0; pl < (long long)N; pl++) {
+      const size_t p = (size_t)pl;
+      if (!has_force(p)) continue;
+      const R jpp = mdet(FP[p]);
+      const M3<R> Fh = mmul(madd(mdiag<R>(1), msmul(eps, particle_gradient(p, u))), FE[p]);
+      const M3<R> A = msmul(-(m[p] / density(p)), mmul(piola(Fh, mu(jpp), lambda(jpp)), mtrans(FE[p])));
+      stencil(p, [&](size_t gI, R, const V3<R>& gw) {
+        const V3<R> f = mvmul(A, gw);
+        for (int k = 0; k < 3; k++) atomic_add(out[gI][k], f[k], pp);
+      });
+    }
+  }
+  static std::vector<V3<R>> grid_from(const double* a, size_t n) {
+    std::vector<V3<R>> u(n);
+    for (size_t g = 0; g < n; g++) u[g] = v3<R>(R(a[3 * g]), R(a[3 * g + 1]), R(a[3 * g + 2]));
+    return u;
+  }
+  static void grid_to(const std::vector<V3<R>>& u, double* a) {
+    for (size_t g = 0; g < u.size(); g++)
+      for (int k = 0; k < 3; k++) a[3 * g + k] = double(u[g][k]);
+  }
+  void hessian(const double* u, double* out) const override {
+    std::vector<V3<R>> r;
+    hessian_action(grid_from(u, G), r);
+    grid_to(r, out);
+  }
+  void force_at(const double* u, double eps, double* out) const override {
+    std::vector<V3<R>> r;
+    force_at_grid(grid_from(u, G), R(eps), r);
+    grid_to(r, out);
+  }
+
+  // Conjugate residuals on the mass-scaled system
+  //     (I + c M^-1/2 K M^-1/2) y = M^1/2 v*,   v = M^-1/2 y,   c = beta dt^2,
+  // (the same solution as (M + c K) v = M v*; the scaling by the lumped
+  // masses keeps the nodes at the material's edge, whose masses are tiny,
+  // from stalling the iteration), from y = M^1/2 v*. Stops when
+  // |r| <= tol |M^1/2 v*| (the residual in the kinetic-energy norm) or after
+  // imp_maxit iterations. Nodes without mass keep v = 0.
+  void implicit_solve(R dt) {
+    imp_iters = 0;
+    imp_res = imp_res0 = 0.0;
+    if (FIXED || !(imp_beta > R(0))) return;
+    const R c = imp_beta * dt * dt;
+    std::vector<R> sq(G, R(0)), isq(G, R(0));
+    for (size_t g = 0; g < G; g++)
+      if (node_mass(g) > R(0)) {
+        sq[g] = std::sqrt(node_mass(g));
+        isq[g] = R(1) / sq[g];
+      }
+    auto dotg = [&](const std::vector<V3<R>>& a, const std::vector<V3<R>>& b) {
+      R t = R(0);
+      for (size_t g = 0; g < G; g++) t += dot3(a[g], b[g]);
+      return t;
+    };
+    std::vector<V3<R>> u(G), ku;
+    // out = y + c M^-1/2 K M^-1/2 y on the nodes with mass
+    auto apply = [&](const std::vector<V3<R>>& y, std::vector<V3<R>>& out) {
+      for (size_t g = 0; g < G; g++) u[g] = smul(isq[g], y[g]);
+      hessian_action(u, ku);
+      out.resize(G);
+      for (size_t g = 0; g < G; g++) out[g] = sq[g] > R(0) ? vadd(y[g], smul(c * isq[g], ku[g])) : v3<R>(0, 0, 0);
+    };
+    std::vector<V3<R>> y(G), b(G), r(G), p, Ar, Ap;
+    for (size_t g = 0; g < G; g++) b[g] = y[g] = smul(sq[g], gvn[g]);
+    const R bb = dotg(b, b);
+    apply(y, Ar);
+    for (size_t g = 0; g < G; g++) r[g] = vsub(b[g], Ar[g]);
+    R rr = dotg(r, r);
+    imp_res0 = bb > R(0) ? double(std::sqrt(rr / bb)) : 0.0;
+    const R tol2 = imp_tol * imp_tol * bb;
+    if (rr > tol2) {
+      apply(r, Ar);
+      p = r;
+      Ap = Ar;
+      R rAr = dotg(r, Ar);
+      for (int k = 1; k <= imp_maxit; k++) {
+        const R ApAp = dotg(Ap, Ap);
+        const R alpha_k = ApAp > R(0) ? rAr / ApAp : R(0);
+        for (size_t g = 0; g < G; g++) {
+          y[g] = vadd(y[g], smul(alpha_k, p[g]));
+          r[g] = vsub(r[g], smul(alpha_k, Ap[g]));
+        }
+        rr = dotg(r, r);
+        imp_iters = k;
+        if (rr <= tol2 || k == imp_maxit) break;
+        apply(r, Ar);
+        const R rAr_new = dotg(r, Ar);
+        const R beta_k = rAr != R(0) ? rAr_new / rAr : R(0);
+        rAr = rAr_new;
+        for (size_t g = 0; g < G; g++) {
+          p[g] = vadd(r[g], smul(beta_k, p[g]));
+          Ap[g] = vadd(Ar[g], smul(beta_k, Ap[g]));
+        }
+      }
+    }
+    imp_res = bb > R(0) ? double(std::sqrt(rr / bb)) : 0.0;
+    for (size_t g = 0; g < G; g++)
+      gvn[g] = sq[g] > R(0) ? collide(node_pos(g), smul(isq[g], y[g])) : v3<R>(0, 0, 0);
+  }
+
   void phase(int which, double dt_d) override {
     const R dt = R(float(dt_d));
     switch (which) {
@@ -813,6 +1060,7 @@ struct Oracle : OracleBase {
       case PH_ADVANCE: advance(dt); break;
       case PH_GMASS: p2g(true); break;
       case PH_PVOLUME: p_volume(); break;
+      case PH_IMPLICIT: implicit_solve(dt); break;
       default: break;
     }
   }
@@ -949,6 +1197,7 @@ void oracle_step(void* h, double dt, int n_steps) {
     o->phase(PH_RESET, dt);
     o->phase(PH_P2G, dt);
     o->phase(PH_GRID, dt);
+    o->phase(PH_IMPLICIT, dt);  // no-op unless a semi-implicit update was set
     o->phase(PH_G2P, dt);
     o->phase(PH_ADVANCE, dt);
   }
@@ -970,6 +1219,19 @@ void oracle_download_accumulators(void* h, double* vpic, double* dv) {
 }
 void oracle_set_density(void* h, const double* rho) { static_cast<OracleBase*>(h)->set_density(rho); }
 void oracle_download_colliders(void* h, double* pos) { static_cast<OracleBase*>(h)->download_colliders(pos); }
+// Semi-implicit velocity update: beta = 0 keeps the explicit step.
+void oracle_set_implicit(void* h, double beta, double tol, int max_iters) {
+  static_cast<OracleBase*>(h)->set_implicit(beta, tol, max_iters);
+}
+// K u on the dense grid (G x 3) for the current particle state.
+void oracle_hessian(void* h, const double* u, double* out) { static_cast<OracleBase*>(h)->hessian(u, out); }
+// The grid force with every particle's F_E deformed by eps u (G x 3).
+void oracle_force_at(void* h, const double* u, double eps, double* out) {
+  static_cast<OracleBase*>(h)->force_at(u, eps, out);
+}
+// (iterations, final relative residual, initial relative residual) of the
+// last solve.
+void oracle_solver_report(void* h, double* out) { static_cast<OracleBase*>(h)->solver_report(out); }
 
 // 3x3 SVD of row-major matrices (KAT / property tests): A = W S V^T.
 void oracle_svd(const double* a, double* w, double* s, double* vmat, int n, int fp64, int vround) {

@@ -6,6 +6,8 @@ layer:
   TimeUpdate(PhysicalScene&&)                   ExplicitTimeUpdate(scene, ...)
   ExplicitTimeUpdate::init()  (explicittimeupdate.cpp:4-34)   .init()
   ExplicitTimeUpdate::update(double dt) (:36-63)              .update(dt)
+  SemiImplicitTimeUpdate (empty in the reference:  SemiImplicitTimeUpdate(scene, beta=...)
+    semiimplicittimeupdate.cpp:3-5)
   MPMPhysicEngine(unique_ptr<TimeUpdate>)       MPMPhysicEngine(time_update)
   MPMPhysicEngine::init() / update(dt)          .init() / .update(dt)
 
@@ -15,6 +17,7 @@ colliders, material). Errors raise SnowError with the library's status.
 from __future__ import annotations
 
 import ctypes as C
+import dataclasses
 from typing import List, Optional, Sequence
 
 import numpy as np
@@ -86,6 +89,9 @@ def params_for(scene: Scene, mode: int, sort_interval: int = 0) -> N.SnowParams:
     p.alpha = scene.alpha
     p.mode = int(mode)
     p.sort_interval = int(sort_interval)
+    p.implicit_beta = float(getattr(scene, "implicit_beta", 0.0))
+    p.implicit_tolerance = float(getattr(scene, "implicit_tolerance", 0.0))
+    p.implicit_max_iters = int(getattr(scene, "implicit_max_iters", 0))
     return p
 
 
@@ -235,8 +241,15 @@ class SimScene:
     def phase_times(self, reset: bool = False) -> dict:
         t = N.SnowPhaseTimes()
         self.ctx.check(self.L.snow_scene_phase_times(self.h, C.byref(t), int(bool(reset))))
-        return dict(sort_ms=t.sort_ms, p2g_ms=t.p2g_ms, grid_ms=t.grid_ms, g2p_ms=t.g2p_ms, total_ms=t.total_ms,
-                    steps=int(t.steps))
+        return dict(sort_ms=t.sort_ms, p2g_ms=t.p2g_ms, grid_ms=t.grid_ms, g2p_ms=t.g2p_ms,
+                    solve_ms=t.other_ms, total_ms=t.total_ms, steps=int(t.steps))
+
+    def solver_report(self) -> dict:
+        """The last step's semi-implicit solve (iterations, relative residuals)."""
+        r = N.SnowSolverReport()
+        self.ctx.check(self.L.snow_scene_solver_report(self.h, C.byref(r)))
+        return dict(iterations=r.iterations, max_iters=r.max_iters, residual=r.residual,
+                    initial_residual=r.initial_residual)
 
 
 class Batch:
@@ -414,6 +427,20 @@ class ExplicitTimeUpdate:
 
     def update(self, dt: float):
         self.sim.step(dt, 1)
+
+
+class SemiImplicitTimeUpdate(ExplicitTimeUpdate):
+    """The reference's SemiImplicitTimeUpdate : TimeUpdate
+    (src/snow/simulation/timeUpdate/semiimplicittimeupdate.hpp:6-12), whose
+    init/update are empty there (semiimplicittimeupdate.cpp:3-5), carried out:
+    each update solves (M + beta dt^2 K) v = M v* on the grid before G2P
+    (Stomakhin et al. 2013, eq. 9). FAST mode."""
+
+    def __init__(self, physical_scene: Scene, ctx: Optional[Context] = None, beta: float = 1.0,
+                 tolerance: float = 0.0, max_iters: int = 0):
+        scene = dataclasses.replace(physical_scene, implicit_beta=float(beta),
+                                    implicit_tolerance=float(tolerance), implicit_max_iters=int(max_iters))
+        super().__init__(scene, ctx=ctx, mode=N.MODE_FAST)
 
 
 class MPMPhysicEngine:

@@ -20,6 +20,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE
 SOURCES = {
     "ref_kernels.cu": ["-fmad=false"],
     "fast_kernels.cu": [],
+    "implicit.cu": [],
     "sort.cu": [],
     "snow_api.cpp": [],
     "server.cpp": [],

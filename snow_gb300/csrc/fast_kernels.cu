@@ -28,813 +28,10 @@
 #include "snow_math.cuh"
 #include "snow_stats.cuh"
 #include "snow_tma.cuh"
+#include "fast_item.cuh"
 
 namespace snow {
 namespace {
-
-constexpr int kTile = 9;  // tile nodes per axis: [4b-2, 4b+6]
-constexpr int kTile3 = kTile * kTile * kTile;
-// A work item holds up to kItemMax particles binned to one home block b. A
-// particle whose base cell lies in [4b-1, 4b+4] (the home block plus one
-// cell of drift each way) has its whole stencil inside the tile; its base
-// cell has tile-local coordinates lc = base - (4b-2) - 1 in [0, 5]^3.
-constexpr int kItemMax = 256;
-constexpr int kCellsPerAxis = kTile - 3;  // 6
-constexpr int kCells = kCellsPerAxis * kCellsPerAxis * kCellsPerAxis;
-constexpr int kPd = 10;           // float4 per particle of P2G data in shared memory
-constexpr int kShColliders = 16;  // colliders cached in shared memory
-constexpr uint32_t kWaitPolls = 1u << 24;
-
-__device__ __forceinline__ int find_scene(const int* __restrict__ prefix, int nscenes, long long u) {
-  int lo = 0, hi = nscenes;
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if ((long long)prefix[mid] <= u)
-      lo = mid;
-    else
-      hi = mid;
-  }
-  return lo;
-}
-
-__device__ __forceinline__ float sel4(int i, float a0, float a1, float a2, float a3) {
-  return i == 0 ? a0 : (i == 1 ? a1 : (i == 2 ? a2 : a3));
-}
-
-// Axis weights of the 4 stencil nodes base-1 .. base+2 (cubic.include.glsl):
-// w[a] = N(d_a), g[a] = N'(-d_a) with d_a = node - x/h, as the shaders
-// evaluate weighting(d) and weightingGradient(-d).
-__device__ __forceinline__ void axis_weights_general(float pg, int base, float w[4], float g[4]) {
-#pragma unroll
-  for (int a = 0; a < 4; a++) {
-    const float d = (float)(base + a - 1) - pg;
-    w[a] = bspline(d);
-    g[a] = bspline_d(-d);
-  }
-}
-
-// The same weights without branches for pg >= 0, where base = floor(pg) and
-// f = pg - base is in [0, 1): the stencil distances are |d| = 1+f, f, 1-f,
-// 2-f, each on a known piece of the spline. With u = 1 - f:
-//   w = (u^3/6, f^3/2 - f^2 + 2/3, u^3/2 - u^2 + 2/3, f^3/6)
-//   g = (-u^2/2, 3f^2/2 - 2f, -3u^2/2 + 2u, f^2/2)
-// Particles below the grid origin (pg < 0, truncated toward zero) take the
-// general path.
-__device__ __forceinline__ void axis_weights(float pg, int base, float w[4], float g[4]) {
-  if (pg < 0.0f) {
-    axis_weights_general(pg, base, w, g);
-    return;
-  }
-  const float f = pg - (float)base;
-  const float u = 1.0f - f;
-  const float f2 = f * f, u2 = u * u;
-  const float f3 = f2 * f, u3 = u2 * u;
-  w[0] = u3 * (1.0f / 6.0f);
-  w[1] = 0.5f * f3 - f2 + 2.0f / 3.0f;
-  w[2] = 0.5f * u3 - u2 + 2.0f / 3.0f;
-  w[3] = f3 * (1.0f / 6.0f);
-  g[0] = -0.5f * u2;
-  g[1] = 1.5f * f2 - 2.0f * f;
-  g[2] = -1.5f * u2 + 2.0f * u;
-  g[3] = 0.5f * f2;
-}
-
-struct AxisW {
-  float wx[4], gx[4], wy[4], gy[4], wz[4], gz[4];
-};
-
-// Grid coordinates (x - gGridPos) / h. Multiplying by 1/h can move a value
-// by an ulp against the shaders' division; at a cell boundary that only
-// swaps which stencil end carries the (zero) weight, so the sums agree.
-__device__ __forceinline__ void grid_coords(const SceneDev& S, float4 xm, float pg[3], int base[3]) {
-  pg[0] = (xm.x - S.gpos[0]) * S.inv_h;
-  pg[1] = (xm.y - S.gpos[1]) * S.inv_h;
-  pg[2] = (xm.z - S.gpos[2]) * S.inv_h;
-#pragma unroll
-  for (int k = 0; k < 3; k++) base[k] = (int)pg[k];  // ivec3(): truncation toward zero
-}
-
-__device__ __forceinline__ void all_weights(const float pg[3], const int base[3], AxisW& w) {
-  axis_weights(pg[0], base[0], w.wx, w.gx);
-  axis_weights(pg[1], base[1], w.wy, w.gy);
-  axis_weights(pg[2], base[2], w.wz, w.gz);
-}
-
-__device__ __forceinline__ void load_fe(const SceneDev& S, int p, M3& F, float& jp) {
-  const float4 a = S.fa[p];
-  const float4 b = S.fb[p];
-  const float2 c = S.fc[p];
-  F.m[0][0] = a.x; F.m[0][1] = a.y; F.m[0][2] = a.z;
-  F.m[1][0] = a.w; F.m[1][1] = b.x; F.m[1][2] = b.y;
-  F.m[2][0] = b.z; F.m[2][1] = b.w; F.m[2][2] = c.x;
-  jp = c.y;
-}
-__device__ __forceinline__ void store_fe(const SceneDev& S, int p, const M3& F, float jp) {
-  S.fa[p] = make_float4(F.m[0][0], F.m[0][1], F.m[0][2], F.m[1][0]);
-  S.fb[p] = make_float4(F.m[1][1], F.m[1][2], F.m[2][0], F.m[2][1]);
-  S.fc[p] = make_float2(F.m[2][2], jp);
-}
-
-__device__ __forceinline__ int block_id(const SceneDev& S, int bx, int by, int bz) {
-  return (bz * S.bdim[1] + by) * S.bdim[0] + bx;
-}
-
-__device__ __forceinline__ bool node_in_grid(const SceneDev& S, int g0, int g1, int g2) {
-  return g0 >= 0 && g1 >= 0 && g2 >= 0 && g0 < S.dim[0] && g1 < S.dim[1] && g2 < S.dim[2];
-}
-
-// Collider projection of gForceCompute.glsl:72-93 / particleAdvance.glsl:182-204
-// for one collider that the point x hits: the velocity relative to the
-// collider loses its normal inward part, with Coulomb friction.
-__device__ __forceinline__ void collide_hit(const snow_collider& c, const float x[3], float v[3]) {
-  float n[3] = {c.normal[0], c.normal[1], c.normal[2]};
-  if (c.type == 1) {
-    const float d[3] = {x[0] - c.pos[0], x[1] - c.pos[1], x[2] - c.pos[2]};
-    const float len = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-    n[0] = d[0] / len;
-    n[1] = d[1] / len;
-    n[2] = d[2] / len;
-  }
-  const float vrel[3] = {v[0] - c.vel[0], v[1] - c.vel[1], v[2] - c.vel[2]};
-  const float vn = vrel[0] * n[0] + vrel[1] * n[1] + vrel[2] * n[2];
-  if (vn < 0.0f) {
-    const float vt[3] = {vrel[0] - n[0] * vn, vrel[1] - n[1] * vn, vrel[2] - n[2] * vn};
-    const float muvn = c.friction * vn;
-    const float lvt = sqrtf(vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2]);
-    if (lvt <= -muvn) {
-      v[0] = c.vel[0];
-      v[1] = c.vel[1];
-      v[2] = c.vel[2];
-    } else {
-      const float s = muvn / lvt;
-#pragma unroll
-      for (int k = 0; k < 3; k++) v[k] = vt[k] + s * vt[k] + c.vel[k];
-    }
-  }
-}
-
-// All colliders in order (half-plane: dot(x - c, n) <= 0; sphere: |x - c| < r).
-__device__ __forceinline__ void collide(const snow_collider* coll, int ncoll, const float x[3], float v[3]) {
-  for (int i = 0; i < ncoll; i++) {
-    const snow_collider c = coll[i];
-    bool hit = false;
-    if (c.type == 0) {
-      hit = (x[0] - c.pos[0]) * c.normal[0] + (x[1] - c.pos[1]) * c.normal[1] + (x[2] - c.pos[2]) * c.normal[2] <=
-            0.0f;
-    } else if (c.type == 1) {
-      const float d[3] = {x[0] - c.pos[0], x[1] - c.pos[1], x[2] - c.pos[2]};
-      hit = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) < c.radius;
-    }
-    if (hit) collide_hit(c, x, v);
-  }
-}
-
-// The same with the hit tests on a packed form of the colliders (half-plane:
-// (n, n . c), tested as n . x <= n . c; sphere: (c, r^2), tested as
-// |x - c|^2 < r^2): one 16-byte shared load per collider, the full record
-// only for the rare hit.
-__device__ __forceinline__ void collide_packed(const snow_collider* coll, const float4* hitf, const int* type,
-                                               int ncoll, const float x[3], float v[3]) {
-  for (int i = 0; i < ncoll; i++) {
-    const float4 h = hitf[i];
-    const int t = type[i];
-    bool hit = false;
-    if (t == 0) {
-      hit = fmaf(h.z, x[2], fmaf(h.y, x[1], h.x * x[0])) <= h.w;
-    } else if (t == 1) {
-      const float d0 = x[0] - h.x, d1 = x[1] - h.y, d2 = x[2] - h.z;
-      hit = fmaf(d2, d2, fmaf(d1, d1, d0 * d0)) < h.w;
-    }
-    if (hit) collide_hit(coll[i], x, v);
-  }
-}
-
-// ---- P2G quantities of one particle -----------------------------------------
-// mass, momentum and A = -V0 * stress, stress = 2 mu(Jp) (FE - R) FE^T +
-// lambda(Jp) (JE - 1) JE I with R the polar rotation of FE
-// (p2gTransfer.glsl:109-141); V0 = m / rho0.
-struct P2GParticle {
-  float m, mv[3];
-  float A[3][3];  // A[r][c]
-  bool force;
-};
-
-__device__ __forceinline__ void p2g_stress(const SceneDev& S, const M3& F, const M3& R, float jp, float vol,
-                                           P2GParticle& q) {
-  const float je = m3_det(F);
-  const float e = expf(S.hardening * (1.0f - jp));
-  const float mu = S.mu0 * e;
-  const float lam = S.lambda0 * e;
-  M3 D;
-#pragma unroll
-  for (int c = 0; c < 3; c++)
-#pragma unroll
-    for (int r = 0; r < 3; r++) D.m[c][r] = F.m[c][r] - R.m[c][r];
-  const M3 P = m3_mul_bt(D, F);  // (FE - R) FE^T
-  const float s2 = lam * (je - 1.0f) * je;
-#pragma unroll
-  for (int r = 0; r < 3; r++)
-#pragma unroll
-    for (int c = 0; c < 3; c++) q.A[r][c] = -vol * (2.0f * mu * P.m[c][r] + (r == c ? s2 : 0.0f));
-  q.force = true;
-}
-
-// From the stored state: R by an SVD of F_E.
-__device__ __forceinline__ P2GParticle p2g_particle(const SceneDev& S, int p, float4 xm, bool mass_only) {
-  P2GParticle q;
-  q.m = xm.w;
-  q.force = false;
-  if (mass_only) return q;
-  const float4 vv = S.vv[p];
-  q.mv[0] = q.m * vv.x;
-  q.mv[1] = q.m * vv.y;
-  q.mv[2] = q.m * vv.z;
-  if (vv.w > 0.0f) {
-    M3 F;
-    float jp;
-    load_fe(S, p, F, jp);
-    M3 W, Sg, V;
-    svd3<false>(F, W, Sg, V);
-    p2g_stress(S, F, m3_mul_bt(W, V), jp, vv.w, q);
-  }
-  return q;
-}
-
-// Scatter of one particle's 64 stencil nodes straight into acc (global
-// atomics) for a particle outside its work item's tile.
-template <bool MASS_ONLY>
-__device__ __forceinline__ void scatter_global(const SceneDev& S, const P2GParticle& q, const AxisW& w,
-                                            const int base[3]) {
-  for (int c = 0; c < 4; c++)
-    for (int b = 0; b < 4; b++)
-      for (int a = 0; a < 4; a++) {
-        const int g0 = base[0] - 1 + a, g1 = base[1] - 1 + b, g2 = base[2] - 1 + c;
-        if (!node_in_grid(S, g0, g1, g2)) continue;
-        const float wxa = sel4(a, w.wx[0], w.wx[1], w.wx[2], w.wx[3]);
-        const float gxa = sel4(a, w.gx[0], w.gx[1], w.gx[2], w.gx[3]);
-        const float wyb = sel4(b, w.wy[0], w.wy[1], w.wy[2], w.wy[3]);
-        const float gyb = sel4(b, w.gy[0], w.gy[1], w.gy[2], w.gy[3]);
-        const float wzc = sel4(c, w.wz[0], w.wz[1], w.wz[2], w.wz[3]);
-        const float gzc = sel4(c, w.gz[0], w.gz[1], w.gz[2], w.gz[3]);
-        const float wgt = wxa * wyb * wzc;
-        const int blk = block_id(S, g0 >> 2, g1 >> 2, g2 >> 2);
-        float* dst = S.acc + (size_t)blk * kAccBlockFloats + (g0 & 3) + 4 * (g1 & 3) + 16 * (g2 & 3);
-        atomicAdd(dst, q.m * wgt);
-        S.blk_flag[blk] = 1;
-        if (MASS_ONLY) continue;
-        const float gw[3] = {gxa * wyb * wzc, wxa * gyb * wzc, wxa * wyb * gzc};
-#pragma unroll
-        for (int r = 0; r < 3; r++) atomicAdd(dst + (1 + r) * kBlockNodes, q.mv[r] * wgt);
-        if (q.force)
-#pragma unroll
-          for (int r = 0; r < 3; r++)
-            atomicAdd(dst + (4 + r) * kBlockNodes, q.A[r][0] * gw[0] + q.A[r][1] * gw[1] + q.A[r][2] * gw[2]);
-      }
-}
-
-// ---- shared memory of one work item --------------------------------------
-struct ItemShared {
-  float stage[27][kOutBlockFloats];  // G2P: the pool blocks around the home block
-  float4 pd[kItemMax][kPd];          // P2G: per-particle data
-  short plist[kItemMax];             // the item's particles in tile-cell order
-  float tile[kAccFields * kTile3];   // P2G sums of the tile's nodes
-  int cstart[kCells + 1];            // first pd slot of each tile cell
-  int ccount[kCells];                // particles per tile cell (zero between items)
-  int wsum[kItemMax / 32];
-  int wocc[kItemMax / 32];
-  short rows[kTile * kTile];         // flush: tile rows holding mass ...
-  uint32_t rowmask[kTile * kTile];   // ... and which of their nodes do
-  int nrows;
-  short cells[kCells];               // occupied tile cells
-  int ncells;
-  int4 item_q[2];                    // this and the next work item of the CTA
-  int scene_q[2];                    // ... and their scenes
-  int coll_scene;                    // scene whose colliders sit in coll
-  uint64_t bar;
-  snow_collider coll[kShColliders];
-  float4 chit[kShColliders];         // packed hit tests of the colliders
-  int ctype[kShColliders];
-};
-
-// Tile block k (0..26) around home block (bx, by, bz), or -1 outside the grid.
-__device__ __forceinline__ int tile_block(const SceneDev& S, int bx, int by, int bz, int k) {
-  const int cx = bx - 1 + k % 3, cy = by - 1 + (k / 3) % 3, cz = bz - 1 + k / 9;
-  const bool in = cx >= 0 && cy >= 0 && cz >= 0 && cx < S.bdim[0] && cy < S.bdim[1] && cz < S.bdim[2];
-  return in ? block_id(S, cx, cy, cz) : -1;
-}
-
-__device__ __forceinline__ void home_coords(const SceneDev& S, int blk, int& bx, int& by, int& bz) {
-  bx = blk % S.bdim[0];
-  by = (blk / S.bdim[0]) % S.bdim[1];
-  bz = blk / (S.bdim[0] * S.bdim[1]);
-}
-
-// Pool slot of tile block k of item `it`; -1: no block.
-__device__ __forceinline__ int tile_slot(const SceneDev& S, int4 it, int k) {
-  if (k >= 27) return -1;
-  int bx, by, bz;
-  home_coords(S, it.x, bx, by, bz);
-  const int b = tile_block(S, bx, by, bz, k);
-  return b < 0 ? -1 : __ldg(&S.blk_slot[b]);
-}
-
-// One full warp issues the bulk copies (TMA) of the tile's pool blocks into
-// `stage` (lane k < 27 copies block k from pool slot `slot`) and zero-fills
-// the blocks without a slot; completion lands on sh.bar. The caller
-// guarantees nobody reads `stage` until the barrier's phase completes and
-// that all earlier reads of `stage` are done.
-__device__ __forceinline__ void stage_issue(ItemShared& sh, const SceneDev& S, int slot) {
-  const int k = threadIdx.x & 31;
-  const bool mine = k < 27 && slot >= 0;
-  const uint32_t valid = __ballot_sync(0xffffffffu, mine);
-  if (k == 0) mbar_arrive_expect_tx(&sh.bar, __popc(valid) * (uint32_t)(kOutBlockFloats * sizeof(float)));
-  __syncwarp();
-  if (mine) {
-    fence_proxy_async_smem();
-    bulk_g2s(sh.stage[k], S.gout + (size_t)slot * kOutBlockFloats, (uint32_t)(kOutBlockFloats * sizeof(float)),
-             &sh.bar);
-  }
-  uint32_t missing = __ballot_sync(0xffffffffu, k < 27 && slot < 0);
-  while (missing) {
-    const int m = __ffs(missing) - 1;
-    missing &= missing - 1;
-    float4* dst = reinterpret_cast<float4*>(sh.stage[m]);
-    for (int i = k; i < kOutBlockFloats / 4; i += 32) dst[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  }
-}
-
-// Every thread waits for the stage copies of the current phase (bounded; a
-// copy that never lands is counted and the kernel carries on).
-__device__ __forceinline__ void stage_wait(ItemShared& sh, const SceneDev& S, uint32_t& phase) {
-  if (!mbar_wait(&sh.bar, phase, kWaitPolls)) {
-    if (threadIdx.x == 0) atomicAdd(&S.counters[CNT_TIMEOUT], 1);
-    mbar_wait(&sh.bar, phase, kWaitPolls);
-  }
-  phase ^= 1u;
-}
-
-// Colliders of scene S into shared memory (when they fit). Ends with
-// __syncthreads.
-__device__ __forceinline__ void load_colliders(ItemShared& sh, const SceneDev& S) {
-  if (S.ncoll <= kShColliders && threadIdx.x < S.ncoll) {
-    const snow_collider c = S.coll[threadIdx.x];
-    sh.coll[threadIdx.x] = c;
-    sh.ctype[threadIdx.x] = c.type;
-    float4 h = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    if (c.type == 0)
-      h = make_float4(c.normal[0], c.normal[1], c.normal[2],
-                      fmaf(c.normal[2], c.pos[2], fmaf(c.normal[1], c.pos[1], c.normal[0] * c.pos[0])));
-    else if (c.type == 1)
-      h = make_float4(c.pos[0], c.pos[1], c.pos[2], c.radius * c.radius);
-    sh.chit[threadIdx.x] = h;
-  }
-  __syncthreads();
-}
-
-// Zeroes the first nf fields of the P2G tile (at the start of each item,
-// after the previous item's flush has read it).
-__device__ __forceinline__ void tile_zero(ItemShared& sh, int nf) {
-  static_assert(offsetof(ItemShared, tile) % 16 == 0, "tile must be 16-byte aligned");
-  float4* t4 = reinterpret_cast<float4*>(sh.tile);
-  const int n4 = nf * kTile3 / 4;
-  for (int i = threadIdx.x; i < n4; i += blockDim.x) t4[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  for (int i = 4 * n4 + threadIdx.x; i < nf * kTile3; i += blockDim.x) sh.tile[i] = 0.0f;
-}
-
-// Kernel start: cell counts, flags and the bulk-copy barrier. Ends with
-// __syncthreads.
-__device__ __forceinline__ void tile_init(ItemShared& sh) {
-  for (int i = threadIdx.x; i < kCells; i += blockDim.x) sh.ccount[i] = 0;
-  if (threadIdx.x == 32) sh.nrows = 0;
-  if (threadIdx.x == 0) mbar_init(&sh.bar, 1);
-  __syncthreads();
-}
-
-// G2P sums of one particle: dv = sum_i w_ip d_i (PIC/FLIP increment,
-// g2pTransfer.glsl:99-104) and L = sum_i v*_i (grad w_ip)^T (velocity
-// gradient, :121-129), contracted along x first for each (y, z) row.
-// node(a, b, c, v6) fills the 6 values (v*, d) of stencil node (a, b, c) or
-// returns false for a node that contributes nothing.
-template <class Node>
-__device__ __forceinline__ void g2p_sums(const AxisW& w, Node node, float dv[3], float L[3][3]) {
-#pragma unroll
-  for (int r = 0; r < 3; r++) {
-    dv[r] = 0.0f;
-    L[r][0] = L[r][1] = L[r][2] = 0.0f;
-  }
-#pragma unroll
-  for (int c = 0; c < 4; c++) {
-#pragma unroll
-    for (int b = 0; b < 4; b++) {
-      float S1[3] = {0.0f, 0.0f, 0.0f}, S2[3] = {0.0f, 0.0f, 0.0f}, D[3] = {0.0f, 0.0f, 0.0f};
-#pragma unroll
-      for (int a = 0; a < 4; a++) {
-        float v6[6];
-        if (!node(a, b, c, v6)) continue;
-#pragma unroll
-        for (int r = 0; r < 3; r++) {
-          S1[r] += w.wx[a] * v6[r];
-          S2[r] += w.gx[a] * v6[r];
-          D[r] += w.wx[a] * v6[3 + r];
-        }
-      }
-      const float t1 = w.wy[b] * w.wz[c], t2 = w.gy[b] * w.wz[c], t3 = w.wy[b] * w.gz[c];
-#pragma unroll
-      for (int r = 0; r < 3; r++) {
-        dv[r] += t1 * D[r];
-        L[r][0] += t1 * S2[r];
-        L[r][1] += t2 * S1[r];
-        L[r][2] += t3 * S1[r];
-      }
-    }
-  }
-}
-
-// Gather for particle at base cell `base` of the item at home block
-// (bx, by, bz): from the staged tile when the stencil lies in it, else from
-// the pool in global memory. Pool nodes are 6-float records (v*, d).
-__device__ __forceinline__ void g2p_gather(const ItemShared& sh, const SceneDev& S, int bx, int by, int bz,
-                                           const int base[3], const AxisW& w, float dv[3], float L[3][3]) {
-  const int tx = base[0] - 1 - (4 * bx - 2), ty = base[1] - 1 - (4 * by - 2), tz = base[2] - 1 - (4 * bz - 2);
-  if (tx >= 0 && ty >= 0 && tz >= 0 && tx <= kTile - 4 && ty <= kTile - 4 && tz <= kTile - 4) {
-    // tile node t (0..8) lies in tile block floor((t + 2) / 4) at local (t + 2) & 3
-    int X[4], Y[4], Z[4];
-#pragma unroll
-    for (int a = 0; a < 4; a++) {
-      const int t = tx + a, q = ty + a, r = tz + a;
-      X[a] = ((t + 2) >> 2) * kOutBlockFloats + kOutFields * ((t + 2) & 3);
-      Y[a] = ((q + 2) >> 2) * 3 * kOutBlockFloats + kOutFields * 4 * ((q + 2) & 3);
-      Z[a] = ((r + 2) >> 2) * 9 * kOutBlockFloats + kOutFields * 16 * ((r + 2) & 3);
-    }
-    const float* st = &sh.stage[0][0];
-    g2p_sums(w,
-             [&](int a, int b, int c, float v6[6]) {
-               const float2* o = reinterpret_cast<const float2*>(st + X[a] + Y[b] + Z[c]);
-               const float2 p0 = o[0], p1 = o[1], p2 = o[2];
-               v6[0] = p0.x; v6[1] = p0.y; v6[2] = p1.x;
-               v6[3] = p1.y; v6[4] = p2.x; v6[5] = p2.y;
-               return true;
-             },
-             dv, L);
-  } else {
-    g2p_sums(w,
-             [&](int a, int b, int c, float v6[6]) {
-               const int g0 = base[0] - 1 + a, g1 = base[1] - 1 + b, g2 = base[2] - 1 + c;
-               if (!node_in_grid(S, g0, g1, g2)) return false;
-               const int sl = __ldg(&S.blk_slot[block_id(S, g0 >> 2, g1 >> 2, g2 >> 2)]);
-               if (sl < 0) return false;
-               const float* o = S.gout + (size_t)sl * kOutBlockFloats +
-                                kOutFields * ((g0 & 3) + 4 * (g1 & 3) + 16 * (g2 & 3));
-#pragma unroll
-               for (int f = 0; f < 6; f++) v6[f] = __ldg(o + f);
-               return true;
-             },
-             dv, L);
-  }
-}
-
-// Position and velocity of one particle, loaded ahead of the gather.
-struct PState {
-  float4 xm, vv;
-};
-
-__device__ __forceinline__ PState load_state(const SceneDev& S, int p) {
-  PState t;
-  t.xm = S.xm[p];
-  t.vv = S.vv[p];
-  return t;
-}
-
-// particleAdvance.glsl:87-210 for particle p given its G2P sums; stores the
-// new state and returns it with the rotation R = W V^T of the SVD.
-struct Advanced {
-  float4 xm, vv;
-  M3 fe, R;
-  float jp;
-};
-
-// F_E, J_p and the previous SVD frame of one particle.
-struct PDef {
-  float4 fa, fb, vq;
-  float2 fc;
-};
-
-__device__ __forceinline__ PDef load_def(const SceneDev& S, int p) {
-  PDef d;
-  d.fa = S.fa[p];
-  d.fb = S.fb[p];
-  d.vq = S.vq[p];
-  d.fc = S.fc[p];
-  return d;
-}
-
-__device__ __forceinline__ void advance_particle(const SceneDev& S, int p, const PState& ps, const PDef& def,
-                                                 const float dv[3], const float L[3][3], const ItemShared& sh,
-                                                 Advanced& out) {
-  M3 FE;
-  FE.m[0][0] = def.fa.x; FE.m[0][1] = def.fa.y; FE.m[0][2] = def.fa.z;
-  FE.m[1][0] = def.fa.w; FE.m[1][1] = def.fb.x; FE.m[1][2] = def.fb.y;
-  FE.m[2][0] = def.fb.z; FE.m[2][1] = def.fb.w; FE.m[2][2] = def.fc.x;
-  const float jp = def.fc.y;
-  float4 xm = ps.xm, vv = ps.vv;
-  M3 step;
-#pragma unroll
-  for (int c = 0; c < 3; c++)
-#pragma unroll
-    for (int r = 0; r < 3; r++) step.m[c][r] = (c == r ? 1.0f : 0.0f) + S.dt * L[r][c];
-  const M3 fe_trial = m3_mul(step, FE);
-  M3 V;
-  float lam[3];
-  float q[4] = {def.vq.x, def.vq.y, def.vq.z, def.vq.w};
-  eigen_warm(fe_trial, q, V, lam);
-  S.vq[p] = make_float4(q[0], q[1], q[2], q[3]);
-  // With FE_trial = W S V^T and B = FE_trial V = W S (columns of norm
-  // sigma_i), the clamped F_E' = W clamp(S) V^T = B diag(clamp(sigma)/sigma) V^T
-  // and the polar rotation R = W V^T = B diag(1/sigma) V^T: the sort and QR
-  // of the shader's SVD (which only serve to find W) are not needed here.
-  const M3 B = m3_mul(fe_trial, V);
-  M3 Br, Bc;
-  float ratio = 1.0f;
-  bool clamped = false;
-#pragma unroll
-  for (int c = 0; c < 3; c++) {
-    const float inv = rsqrt_nr(fmaxf(lam[c], 1e-30f));
-    const float sig = lam[c] * inv;
-    const float cl = fminf(fmaxf(sig, S.crit_lo), S.crit_hi);
-    clamped = clamped || cl != sig;
-    ratio *= __fdividef(sig, cl);
-    const float sc = cl * inv;
-#pragma unroll
-    for (int r = 0; r < 3; r++) {
-      Br.m[c][r] = B.m[c][r] * inv;
-      Bc.m[c][r] = B.m[c][r] * sc;
-    }
-  }
-  out.R = m3_mul_bt(Br, V);
-  // no singular value clamped: F_E' = FE_trial exactly, J_p unchanged
-  out.fe = clamped ? m3_mul_bt(Bc, V) : fe_trial;
-  // det F_P' = det F_P * det(FE_trial) / det(FE'): the shader's
-  // F_P' = V S^-1 W^T (I + dt L) FE FP (particleAdvance.glsl:132) has this
-  // determinant; only det F_P is ever read (p2gTransfer.glsl:119).
-  out.jp = clamped ? jp * ratio : jp;
-  float v[3] = {S.alpha * vv.x + dv[0], S.alpha * vv.y + dv[1], S.alpha * vv.z + dv[2]};
-  const float xold[3] = {xm.x, xm.y, xm.z};
-  if (S.ncoll <= kShColliders)
-    collide_packed(sh.coll, sh.chit, sh.ctype, S.ncoll, xold, v);
-  else
-    collide(S.coll, S.ncoll, xold, v);
-  xm.x += S.dt * v[0];
-  xm.y += S.dt * v[1];
-  xm.z += S.dt * v[2];
-  vv.x = v[0];
-  vv.y = v[1];
-  vv.z = v[2];
-  S.xm[p] = xm;
-  S.vv[p] = vv;
-  store_fe(S, p, out.fe, out.jp);
-  out.xm = xm;
-  out.vv = vv;
-  bool finite = isfinite(xm.x) && isfinite(xm.y) && isfinite(xm.z) && isfinite(v[0]) && isfinite(v[1]) &&
-                isfinite(v[2]) && isfinite(out.jp);
-#pragma unroll
-  for (int c = 0; c < 3; c++)
-#pragma unroll
-    for (int r = 0; r < 3; r++) finite = finite && isfinite(out.fe.m[c][r]);
-  if (!finite) atomicAdd(&S.counters[CNT_NONFINITE], 1);
-}
-
-// Adds the particles of one tile cell (list slots j0..j1) to this lane's
-// x-row (b, c) of the cell's 4x4x4 stencil: acc[a] holds node x = lx + a.
-template <bool MASS_ONLY>
-__device__ __forceinline__ void cell_sums(const ItemShared& sh, int j0, int j1, int b, int c,
-                                          float (&acc)[4][kAccFields]) {
-  for (int j = j0; j < j1; j++) {
-    const float4* d = sh.pd[sh.plist[j]];
-    const float* df = reinterpret_cast<const float*>(d);
-    const float4 w4 = d[4];
-    const float wxa[4] = {w4.x, w4.y, w4.z, w4.w};
-    const float wyb = df[6 * 4 + b], wzc = df[8 * 4 + c];
-    const float t1 = wyb * wzc;
-    const float4 d0 = d[0];
-    const float mw = d0.x * t1;
-    if (MASS_ONLY) {
-#pragma unroll
-      for (int a = 0; a < 4; a++) acc[a][0] += wxa[a] * mw;
-      continue;
-    }
-    const float4 g4 = d[5];
-    const float gxa[4] = {g4.x, g4.y, g4.z, g4.w};
-    const float gyb = df[7 * 4 + b], gzc = df[9 * 4 + c];
-    const float t2 = gyb * wzc, t3 = wyb * gzc;
-    const float4 a1 = d[1], a2 = d[2];
-    const float a22 = df[3 * 4];
-    // A rows: r0 = (a1.x a1.y a1.z), r1 = (a1.w a2.x a2.y), r2 = (a2.z a2.w a22)
-    const float pv[3] = {d0.y * t1, d0.z * t1, d0.w * t1};
-    const float kk[3] = {a1.x * t1, a1.w * t1, a2.z * t1};
-    const float hh[3] = {a1.y * t2 + a1.z * t3, a2.x * t2 + a2.y * t3, a2.w * t2 + a22 * t3};
-#pragma unroll
-    for (int a = 0; a < 4; a++) {
-      acc[a][0] += wxa[a] * mw;
-#pragma unroll
-      for (int r = 0; r < 3; r++) {
-        acc[a][1 + r] += wxa[a] * pv[r];
-        acc[a][4 + r] += gxa[a] * kk[r] + wxa[a] * hh[r];
-      }
-    }
-  }
-}
-
-// Adds the 4 nodes of this lane's row (tile nodes t0 .. t0 + 3) to the
-// shared tile and clears them.
-template <int NF>
-__device__ __forceinline__ void row_flush(ItemShared& sh, int t0, float (&acc)[4][kAccFields]) {
-#pragma unroll
-  for (int a = 0; a < 4; a++) {
-#pragma unroll
-    for (int f = 0; f < NF; f++) {
-      atomicAdd(&sh.tile[f * kTile3 + t0 + a], acc[a][f]);
-      acc[a][f] = 0.0f;
-    }
-  }
-}
-
-__device__ __forceinline__ int cell_row_node(int ci, int b, int c) {
-  const int lx = ci % kCellsPerAxis, ly = (ci / kCellsPerAxis) % kCellsPerAxis, lz = ci / (kCellsPerAxis * kCellsPerAxis);
-  return lx + kTile * (ly + b) + kTile * kTile * (lz + c);
-}
-
-// P2G of the item's particles into acc (every thread of the CTA calls it;
-// thread i holds particle i of the item when `have`):
-//   1. each particle inside the tile counts itself in its base cell and
-//      stores its mass, momentum, A and axis weights (the others scatter
-//      straight to acc);
-//   2. a scan of the cell counts lists the particles in tile-cell order and
-//      the occupied cells;
-//   3. each half-warp owns one occupied cell at a time: lane l sums the
-//      x-row (b, c) = (l & 3, l >> 2) of the cell's stencil over the cell's
-//      particles in registers and adds the row to the shared tile;
-//   4. the tile's non-empty nodes are added to acc (row by row, vector
-//      atomics) and their blocks flagged. The caller separates this item's
-//      flush from the next item's use of the tile with a barrier.
-// `between` runs between steps 3 and 4, long after the staged G2P tile was
-// last read (the fused kernel issues the next item's copies there).
-template <bool MASS_ONLY, class Between>
-__device__ __forceinline__ void p2g_tile_pass(ItemShared& sh, const SceneDev& S, int bx, int by, int bz, bool have,
-                                              const P2GParticle& q, const AxisW& w, const int base[3],
-                                              Between between) {
-  constexpr int nf = MASS_ONLY ? 1 : kAccFields;
-  const int ox = 4 * bx - 2, oy = 4 * by - 2, oz = 4 * bz - 2;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int my_cell = -1, my_rank = 0;
-  if (have) {
-    const int lx = base[0] - 1 - ox, ly = base[1] - 1 - oy, lz = base[2] - 1 - oz;
-    if (lx >= 0 && ly >= 0 && lz >= 0 && lx < kCellsPerAxis && ly < kCellsPerAxis && lz < kCellsPerAxis) {
-      my_cell = lx + kCellsPerAxis * ly + kCellsPerAxis * kCellsPerAxis * lz;
-      my_rank = atomicAdd(&sh.ccount[my_cell], 1);
-    } else {
-      // the particle drifted out of its home block's tile since the last binning
-      atomicAdd(&S.counters[CNT_FALLBACK], 1);
-      scatter_global<MASS_ONLY>(S, q, w, base);
-    }
-  }
-  if (my_cell >= 0) {
-    float4* d = sh.pd[threadIdx.x];
-    const bool f = !MASS_ONLY && q.force;
-    d[0] = MASS_ONLY ? make_float4(q.m, 0.0f, 0.0f, 0.0f) : make_float4(q.m, q.mv[0], q.mv[1], q.mv[2]);
-    d[1] = f ? make_float4(q.A[0][0], q.A[0][1], q.A[0][2], q.A[1][0]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    d[2] = f ? make_float4(q.A[1][1], q.A[1][2], q.A[2][0], q.A[2][1]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    d[3] = make_float4(f ? q.A[2][2] : 0.0f, __int_as_float(my_cell), 0.0f, 0.0f);
-    d[4] = make_float4(w.wx[0], w.wx[1], w.wx[2], w.wx[3]);
-    d[5] = make_float4(w.gx[0], w.gx[1], w.gx[2], w.gx[3]);
-    d[6] = make_float4(w.wy[0], w.wy[1], w.wy[2], w.wy[3]);
-    d[7] = make_float4(w.gy[0], w.gy[1], w.gy[2], w.gy[3]);
-    d[8] = make_float4(w.wz[0], w.wz[1], w.wz[2], w.wz[3]);
-    d[9] = make_float4(w.gz[0], w.gz[1], w.gz[2], w.gz[3]);
-  }
-  __syncthreads();  // counts and P2G data done
-  if (threadIdx.x == 32) sh.nrows = 0;  // the previous item's flush is long done
-  // exclusive scan of the cell counts and list of the occupied cells, one
-  // cell per thread
-  const int t = threadIdx.x;
-  const int cnt = t < kCells ? sh.ccount[t] : 0;
-  int incl = cnt;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int v = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += v;
-  }
-  const uint32_t occ = __ballot_sync(0xffffffffu, cnt > 0);
-  if (lane == 31) {
-    sh.wsum[warp] = incl;
-    sh.wocc[warp] = __popc(occ);
-  }
-  __syncthreads();
-  int off = 0, ooff = 0;
-  for (int k = 0; k < warp; k++) {
-    off += sh.wsum[k];
-    ooff += sh.wocc[k];
-  }
-  if (t < kCells) {
-    sh.cstart[t] = off + incl - cnt;
-    sh.ccount[t] = 0;
-    if (cnt > 0) sh.cells[ooff + __popc(occ & ((1u << lane) - 1u))] = (short)t;
-  }
-  if (t == kCells - 1) sh.cstart[kCells] = off + incl;
-  if (t == blockDim.x - 1) sh.ncells = ooff + __popc(occ);
-  __syncthreads();
-  if (my_cell >= 0) sh.plist[sh.cstart[my_cell] + my_rank] = (short)threadIdx.x;
-  __syncthreads();
-  {
-    // half-warp h takes a contiguous slice of the occupied-cell list (the
-    // two halves of a warp get neighbouring slices, whose particle counts
-    // are alike). Cells of a slice often follow each other along x: the
-    // row's sums then slide one node instead of being flushed, so only the
-    // node that leaves the window goes to the shared tile.
-    constexpr int NF = MASS_ONLY ? 1 : kAccFields;
-    const int hw = threadIdx.x >> 4, l16 = threadIdx.x & 15;
-    const int b = l16 & 3, c = l16 >> 2;
-    const int nhw = blockDim.x >> 4;
-    const int ncells = sh.ncells;
-    const int k0 = (ncells * hw) / nhw, k1 = (ncells * (hw + 1)) / nhw;
-    float acc[4][kAccFields];
-#pragma unroll
-    for (int a = 0; a < 4; a++)
-#pragma unroll
-      for (int f = 0; f < kAccFields; f++) acc[a][f] = 0.0f;
-    int cur = -1;
-    for (int k = k0; k < k1; k++) {
-      const int ci = sh.cells[k];
-      if (cur >= 0) {
-        if (ci == cur + 1 && ci % kCellsPerAxis != 0) {
-          // only node 0 leaves the window: flush it, slide the rest
-#pragma unroll
-          for (int f = 0; f < NF; f++) {
-            atomicAdd(&sh.tile[f * kTile3 + cell_row_node(cur, b, c)], acc[0][f]);
-            acc[0][f] = acc[1][f];
-            acc[1][f] = acc[2][f];
-            acc[2][f] = acc[3][f];
-            acc[3][f] = 0.0f;
-          }
-        } else {
-          row_flush<NF>(sh, cell_row_node(cur, b, c), acc);
-        }
-      }
-      cell_sums<MASS_ONLY>(sh, sh.cstart[ci], sh.cstart[ci + 1], b, c, acc);
-      cur = ci;
-    }
-    if (cur >= 0) row_flush<NF>(sh, cell_row_node(cur, b, c), acc);
-  }
-  __syncthreads();
-  between();
-  // 4a. the tile rows (ty, tz) with nodes that hold mass and lie in the grid
-  for (int r = threadIdx.x; r < kTile * kTile; r += blockDim.x) {
-    const int g1 = oy + r % kTile, g2 = oz + r / kTile;
-    uint32_t mask = 0;
-    if (g1 >= 0 && g2 >= 0 && g1 < S.dim[1] && g2 < S.dim[2]) {
-      const float* row = &sh.tile[r * kTile];
-#pragma unroll
-      for (int x = 0; x < kTile; x++)
-        if (row[x] != 0.0f && ox + x >= 0 && ox + x < S.dim[0]) mask |= 1u << x;
-    }
-    if (mask) {
-      const int k = atomicAdd(&sh.nrows, 1);
-      sh.rows[k] = r;
-      sh.rowmask[k] = mask;
-    }
-  }
-  __syncthreads();
-  // 4b. one (field, row) per thread: the row's nodes x = 4bx-2 .. 4bx+6 lie
-  // in blocks bx-1 (local x 2, 3), bx (0..3) and bx+1 (0..2); each part is one
-  // vector atomic into acc (nodes without mass or outside the grid add 0, as
-  // does the unused fourth lane of the last part).
-  const int nrows = sh.nrows;
-  for (int task = threadIdx.x; task < nf * nrows; task += blockDim.x) {
-    const int f = task / nrows, k = task % nrows;
-    const int r = sh.rows[k];
-    const uint32_t mask = sh.rowmask[k];
-    const float* row = &sh.tile[f * kTile3 + r * kTile];
-    float v[kTile];
-#pragma unroll
-    for (int x = 0; x < kTile; x++) v[x] = ((mask >> x) & 1u) ? row[x] : 0.0f;
-    const int g1 = oy + r % kTile, g2 = oz + r / kTile;
-    float* base = S.acc + f * kBlockNodes + 4 * (g1 & 3) + 16 * (g2 & 3);
-    if (mask & 0x3u) {
-      const int blk = block_id(S, bx - 1, g1 >> 2, g2 >> 2);
-      atomicAdd(reinterpret_cast<float2*>(base + (size_t)blk * kAccBlockFloats + 2), make_float2(v[0], v[1]));
-      if (f == 0) S.blk_flag[blk] = 1;
-    }
-    if (mask & 0x3cu) {
-      const int blk = block_id(S, bx, g1 >> 2, g2 >> 2);
-      atomicAdd(reinterpret_cast<float4*>(base + (size_t)blk * kAccBlockFloats), make_float4(v[2], v[3], v[4], v[5]));
-      if (f == 0) S.blk_flag[blk] = 1;
-    }
-    if (mask & 0x1c0u) {
-      const int blk = block_id(S, bx + 1, g1 >> 2, g2 >> 2);
-      atomicAdd(reinterpret_cast<float4*>(base + (size_t)blk * kAccBlockFloats), make_float4(v[6], v[7], v[8], 0.0f));
-      if (f == 0) S.blk_flag[blk] = 1;
-    }
-  }
-}
 
 // ===========================================================================
 __device__ __forceinline__ void form_prefixes(const SceneDev* __restrict__ scenes, int nscenes, int* items,
@@ -866,6 +63,10 @@ __global__ void k_begin_step(const SceneDev* __restrict__ scenes, int nscenes, i
   if (rigid)  // rigidAdvance.glsl:14-18
     for (int i = threadIdx.x; i < S.ncoll; i += blockDim.x)
       for (int k = 0; k < 3; k++) S.coll[i].pos[k] = S.coll[i].pos[k] + S.dt * S.coll[i].vel[k];
+  if (S.crs) {  // the semi-implicit solve's scalars start from zero each step
+    double* c = reinterpret_cast<double*>(S.crs);
+    for (int i = threadIdx.x; i < (int)(sizeof(CrScalars) / sizeof(double)); i += blockDim.x) c[i] = 0.0;
+  }
 }
 
 __global__ void k_count_flags(const SceneDev* __restrict__ sd, int nblocks) {
@@ -945,7 +146,7 @@ __global__ void __launch_bounds__(kItemMax, 2) k_p2g(const SceneDev* __restrict_
         have = true;
       }
     }
-    p2g_tile_pass<MASS_ONLY>(sh, S, bx, by, bz, have, q, w, base, [] {});
+    p2g_tile_pass<MASS_ONLY ? kP2gMass : kP2gFull>(sh, S, bx, by, bz, have, q, w, base, [] {});
     __syncthreads();
   }
 }
@@ -992,6 +193,14 @@ __global__ void __launch_bounds__(256) k_grid(const SceneDev* __restrict__ scene
     out[0] = make_float2(vs[0], vs[1]);
     out[1] = make_float2(vs[2], d[0]);
     out[2] = make_float2(d[1], d[2]);
+    if (S.crs) {  // semi-implicit: the solve starts from x = v* and applies K to v* first
+      const size_t i = (size_t)slot * kBlockNodes + node;
+      S.crv[i] = make_float4(vs[0], vs[1], vs[2], mi > 0.0f ? mi : 0.0f);
+      float* u = S.cru + (size_t)slot * kImpBlockFloats + 3 * node;
+      u[0] = vs[0];
+      u[1] = vs[1];
+      u[2] = vs[2];
+    }
   }
 }
 
@@ -1146,7 +355,7 @@ __global__ void __launch_bounds__(kItemMax, 2) k_g2p2g(const SceneDev* __restric
         all_weights(npg, nbase, wn);
       }
     }
-    p2g_tile_pass<false>(sh, S, bx, by, bz, have, q, wn, nbase, [&] {
+    p2g_tile_pass<kP2gFull>(sh, S, bx, by, bz, have, q, wn, nbase, [&] {
       if (lastw && un < total) {
         if (lane == 0) {
           sh.item_q[par ^ 1] = itn;

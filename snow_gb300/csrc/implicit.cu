@@ -1,0 +1,493 @@
+// Semi-implicit velocity update of the FAST path for sm_103a.
+//
+// The reference declares SemiImplicitTimeUpdate but leaves it empty
+// (src/snow/simulation/timeUpdate/semiimplicittimeupdate.cpp:3-5). This is
+// the scheme of Stomakhin et al. 2013 (sec. 4, eq. 9): after the grid update
+// has formed v* (colliders applied), solve
+//     (M + beta dt^2 K) v = M v*,   K u = sum_p V0_p dP(F_p; G_p F_p) F_p^T grad w_ip,
+//     G_p = sum_j u_j (grad w_jp)^T,
+// apply the colliders to v, and hand v to G2P in place of v* (d = v - alpha
+// p/m follows). The solve runs conjugate residuals on the mass-scaled form
+//     (I + c M^-1/2 K M^-1/2) y = M^1/2 v*,   v = M^-1/2 y,   c = beta dt^2,
+// from y = M^1/2 v*: the scaling by the lumped masses keeps the nodes at the
+// material's edge, whose masses are tiny, from stalling the iteration, and
+// the residual is measured in the kinetic-energy norm |M^1/2 v*|. P is the first
+// Piola-Kirchhoff stress of the shaders' fixed-corotated energy
+// (p2gTransfer.glsl:109-141 forms P F^T), with F = F_E, mu(J_p), lambda(J_p)
+// held at the step's start; the weight gradients are the explicit force's
+// (grid units), so K is the derivative of the force the explicit step
+// applies.
+//
+// Layout in HBM, per active pool slot (the grid update's slots):
+//   crv  three float4 planes of pool_cap x 64 nodes: (v, m), (p, 0), (A p, 0)
+//        with p and A p in the scaled variables
+//   cru  pool_cap x 192 floats: u = M^-1/2 r, the vector K is applied to,
+//        3 floats per node, so that a work item bulk-copies (TMA) its 27
+//        blocks like the G2P gather does
+//   acc  the dense P2G sums, zero between steps: K u accumulates in its
+//        force slots and is cleared by the pass that consumes it
+//   crs  per scene: |M^1/2 v*|^2 and per iteration (r, A r), |A p|^2, |r|^2 in FP64
+// Kernels of one iteration k: K u over the work items (k_hess), then three
+// passes over the active nodes: (r, A r); the directions p, A p and |A p|^2;
+// v, r and |r|^2. A scene whose residual met the tolerance skips the rest.
+#include "fast_item.cuh"
+
+namespace snow {
+namespace {
+
+// Iteration k (k >= 1) of scene S runs while iteration k - 1 left a residual
+// above the tolerance; iteration 0 is the K v* pass of every implicit scene.
+__device__ __forceinline__ bool cr_running(const SceneDev& S, int k) {
+  if (!S.crs) return false;
+  if (k == 0) return true;
+  if (k > S.imp_maxit) return false;
+  const CrScalars& c = *S.crs;
+  const double tol = (double)S.imp_tol;
+  return c.rr[k - 1] > tol * tol * c.bb;
+}
+
+// G = sum_j u_j (grad w_j)^T over the particle's stencil, u from the staged
+// tile (3 floats per node) when the stencil lies in it, else from cru.
+__device__ __forceinline__ void hess_gather(const ItemShared& sh, const SceneDev& S, int bx, int by, int bz,
+                                            const int base[3], const AxisW& w, float Gm[3][3]) {
+#pragma unroll
+  for (int r = 0; r < 3; r++) Gm[r][0] = Gm[r][1] = Gm[r][2] = 0.0f;
+  const int tx = base[0] - 1 - (4 * bx - 2), ty = base[1] - 1 - (4 * by - 2), tz = base[2] - 1 - (4 * bz - 2);
+  const bool in_tile = tx >= 0 && ty >= 0 && tz >= 0 && tx <= kTile - 4 && ty <= kTile - 4 && tz <= kTile - 4;
+  int X[4], Y[4], Z[4];
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+    const int t = tx + a, q = ty + a, r = tz + a;
+    X[a] = ((t + 2) >> 2) * kOutBlockFloats + 3 * ((t + 2) & 3);
+    Y[a] = ((q + 2) >> 2) * 3 * kOutBlockFloats + 3 * 4 * ((q + 2) & 3);
+    Z[a] = ((r + 2) >> 2) * 9 * kOutBlockFloats + 3 * 16 * ((r + 2) & 3);
+  }
+  const float* st = &sh.stage[0][0];
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+#pragma unroll
+    for (int b = 0; b < 4; b++) {
+      float S1[3] = {0.0f, 0.0f, 0.0f}, S2[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+      for (int a = 0; a < 4; a++) {
+        float u[3];
+        if (in_tile) {
+          const float* o = st + X[a] + Y[b] + Z[c];
+          u[0] = o[0];
+          u[1] = o[1];
+          u[2] = o[2];
+        } else {
+          const int g0 = base[0] - 1 + a, g1 = base[1] - 1 + b, g2 = base[2] - 1 + c;
+          u[0] = u[1] = u[2] = 0.0f;
+          if (node_in_grid(S, g0, g1, g2)) {
+            const int sl = __ldg(&S.blk_slot[block_id(S, g0 >> 2, g1 >> 2, g2 >> 2)]);
+            if (sl >= 0) {
+              const float* o = S.cru + (size_t)sl * kImpBlockFloats + 3 * ((g0 & 3) + 4 * (g1 & 3) + 16 * (g2 & 3));
+              u[0] = __ldg(o);
+              u[1] = __ldg(o + 1);
+              u[2] = __ldg(o + 2);
+            }
+          }
+        }
+#pragma unroll
+        for (int r = 0; r < 3; r++) {
+          S1[r] += w.wx[a] * u[r];
+          S2[r] += w.gx[a] * u[r];
+        }
+      }
+      const float t1 = w.wy[b] * w.wz[c], t2 = w.gy[b] * w.wz[c], t3 = w.wy[b] * w.gz[c];
+#pragma unroll
+      for (int r = 0; r < 3; r++) {
+        Gm[r][0] += t1 * S2[r];
+        Gm[r][1] += t2 * S1[r];
+        Gm[r][2] += t3 * S1[r];
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void cross3(const float a[3], const float b[3], float o[3]) {
+  o[0] = a[1] * b[2] - a[2] * b[1];
+  o[1] = a[2] * b[0] - a[0] * b[2];
+  o[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+// q.A = V0 dP(F; G F) F^T for particle p (false: the particle carries no
+// stress force, p2gTransfer.glsl:126). dP = 2 mu (dF - dR) + lambda dJ C +
+// lambda (J - 1) dC with C = J F^-T the cofactor matrix; with F^T F = V
+// diag(s^2) V^T (warm-started Jacobi from the particle's stored frame),
+// W = F V diag(1/s) and G' = W^T dF V, the rotation's differential is
+// dR = W X V^T, X skew with X_ij = (G'_ij - G'_ji) / (s_i + s_j).
+__device__ __forceinline__ bool hess_particle(const SceneDev& S, int p, const float Gm[3][3], P2GParticle& q) {
+  const float vol = S.vv[p].w;
+  if (!(vol > 0.0f)) return false;
+  M3 F;
+  float jp;
+  load_fe(S, p, F, jp);
+  const float4 f4 = S.vq[p];
+  float qv[4] = {f4.x, f4.y, f4.z, f4.w};
+  M3 V;
+  float lam[3];
+  eigen_warm(F, qv, V, lam);
+  const M3 B = m3_mul(F, V);  // W diag(s)
+  float sig[3];
+  M3 W;
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const float inv = rsqrt_nr(fmaxf(lam[c], 1e-30f));
+    sig[c] = lam[c] * inv;
+#pragma unroll
+    for (int r = 0; r < 3; r++) W.m[c][r] = B.m[c][r] * inv;
+  }
+  M3 dF;  // G F
+#pragma unroll
+  for (int c = 0; c < 3; c++)
+#pragma unroll
+    for (int r = 0; r < 3; r++) dF.m[c][r] = Gm[r][0] * F.m[c][0] + Gm[r][1] * F.m[c][1] + Gm[r][2] * F.m[c][2];
+  const M3 Gw = m3_mul_at(W, m3_mul(dF, V));  // W^T dF V; Gw.m[c][r] is row r, column c
+  const float x01 = (Gw.m[1][0] - Gw.m[0][1]) / (sig[0] + sig[1]);
+  const float x02 = (Gw.m[2][0] - Gw.m[0][2]) / (sig[0] + sig[2]);
+  const float x12 = (Gw.m[2][1] - Gw.m[1][2]) / (sig[1] + sig[2]);
+  M3 X;
+  X.m[0][0] = 0.0f; X.m[1][0] = x01;  X.m[2][0] = x02;
+  X.m[0][1] = -x01; X.m[1][1] = 0.0f; X.m[2][1] = x12;
+  X.m[0][2] = -x02; X.m[1][2] = -x12; X.m[2][2] = 0.0f;
+  const M3 dR = m3_mul_bt(m3_mul(W, X), V);
+  // cofactor C (columns f1 x f2, f2 x f0, f0 x f1) and its differential
+  M3 C, dC;
+  cross3(F.m[1], F.m[2], C.m[0]);
+  cross3(F.m[2], F.m[0], C.m[1]);
+  cross3(F.m[0], F.m[1], C.m[2]);
+  float dJ = 0.0f;
+#pragma unroll
+  for (int c = 0; c < 3; c++)
+#pragma unroll
+    for (int r = 0; r < 3; r++) dJ += C.m[c][r] * dF.m[c][r];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const int c1 = (c + 1) % 3, c2 = (c + 2) % 3;
+    float t0[3], t1[3];
+    cross3(dF.m[c1], F.m[c2], t0);
+    cross3(F.m[c1], dF.m[c2], t1);
+#pragma unroll
+    for (int r = 0; r < 3; r++) dC.m[c][r] = t0[r] + t1[r];
+  }
+  const float J = m3_det(F);
+  const float e = expf(S.hardening * (1.0f - jp));
+  const float mu2 = 2.0f * S.mu0 * e, la = S.lambda0 * e;
+  const float la_dj = la * dJ, la_j1 = la * (J - 1.0f);
+  M3 dP;
+#pragma unroll
+  for (int c = 0; c < 3; c++)
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+      dP.m[c][r] = mu2 * (dF.m[c][r] - dR.m[c][r]) + la_dj * C.m[c][r] + la_j1 * dC.m[c][r];
+  const M3 A = m3_mul_bt(dP, F);
+#pragma unroll
+  for (int r = 0; r < 3; r++)
+#pragma unroll
+    for (int c = 0; c < 3; c++) q.A[r][c] = vol * A.m[c][r];
+  q.force = true;
+  return true;
+}
+
+// K u for the items of every scene whose iteration k runs, into acc's force
+// slots (iteration 0: u = v*).
+__global__ void __launch_bounds__(kItemMax, 2) k_hess(const SceneDev* __restrict__ scenes,
+                                                      const int* __restrict__ item_prefix, int nscenes, int k) {
+  extern __shared__ float4 smem_raw[];
+  ItemShared& sh = *reinterpret_cast<ItemShared*>(smem_raw);
+  tile_init(sh);
+  const int total = item_prefix[nscenes];
+  uint32_t phase = 0;
+  for (int u = blockIdx.x; u < total; u += gridDim.x) {
+    const int s = find_scene(item_prefix, nscenes, u);
+    const SceneDev& S = scenes[s];
+    if (!cr_running(S, k)) continue;  // uniform across the CTA
+    const int4 it = S.items[u - item_prefix[s]];
+    tile_zero(sh, 3);
+    int bx, by, bz;
+    home_coords(S, it.x, bx, by, bz);
+    if (threadIdx.x < 32) stage_issue(sh, S.cru, kImpBlockFloats, tile_slot(S, it, threadIdx.x));
+    __syncthreads();  // zero-filled stage blocks are visible
+    stage_wait(sh, S, phase);
+    const int i = threadIdx.x;
+    bool have = false;
+    P2GParticle q;
+    q.force = false;
+    AxisW w;
+    int base[3] = {0, 0, 0};
+    if (i < min(it.z, kItemMax)) {
+      const int p = it.y + i;
+      const float4 xm = S.xm[p];
+      if (fabsf(xm.w) <= 100.0f) {  // p2gTransfer.glsl:64-66
+        float pg[3];
+        grid_coords(S, xm, pg, base);
+        all_weights(pg, base, w);
+        float Gm[3][3];
+        hess_gather(sh, S, bx, by, bz, base, w, Gm);
+        have = hess_particle(S, p, Gm, q);
+      }
+    }
+    p2g_tile_pass<kP2gForce>(sh, S, bx, by, bz, have, q, w, base, [] {});
+    __syncthreads();
+  }
+}
+
+// Per-warp FP64 sum added to *dst. All 32 lanes call it together.
+__device__ __forceinline__ void warp_sum_add(double* dst, double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(dst, v);
+}
+
+// Runs body(S, slot, node) -> (d0, d1) over the active nodes of the scenes for
+// which run(S) holds (one 64-thread group per active block) and adds the two
+// per-scene sums to the doubles that target(S) names. A warp lies inside one
+// group, so its scene changes only between blocks and the sums flush per warp.
+template <class Run, class Body, class Target>
+__device__ __forceinline__ void for_active_nodes(const SceneDev* __restrict__ scenes,
+                                                 const int* __restrict__ active_prefix, int nscenes, Run run,
+                                                 Body body, Target target) {
+  const int groups = blockDim.x / kBlockNodes;
+  const int node = threadIdx.x % kBlockNodes;
+  const long long total = active_prefix[nscenes];
+  int cur = -1;
+  double s0 = 0.0, s1 = 0.0;
+  for (long long u = (long long)blockIdx.x * groups + threadIdx.x / kBlockNodes; u < total;
+       u += (long long)gridDim.x * groups) {
+    const int s = find_scene(active_prefix, nscenes, u);
+    const SceneDev& S = scenes[s];
+    if (!run(S)) continue;
+    if (s != cur) {
+      if (cur >= 0) {
+        double *d0, *d1;
+        target(scenes[cur], d0, d1);
+        warp_sum_add(d0, s0);
+        if (d1) warp_sum_add(d1, s1);
+      }
+      cur = s;
+      s0 = s1 = 0.0;
+    }
+    const int slot = (int)(u - active_prefix[s]);
+    double a = 0.0, b = 0.0;
+    body(S, slot, node, a, b);
+    s0 += a;
+    s1 += b;
+  }
+  if (cur >= 0) {
+    double *d0, *d1;
+    target(scenes[cur], d0, d1);
+    warp_sum_add(d0, s0);
+    if (d1) warp_sum_add(d1, s1);
+  }
+}
+
+// K u of block `slot` at `node` from acc's force slots (cleared when `take`).
+__device__ __forceinline__ void take_ku(const SceneDev& S, int slot, int node, bool take, float ku[3]) {
+  float* acc = S.acc + (size_t)S.active[slot] * kAccBlockFloats + node;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    ku[k] = acc[(4 + k) * kBlockNodes];
+    if (take) acc[(4 + k) * kBlockNodes] = 0.0f;
+  }
+}
+
+__device__ __forceinline__ float dot3f(const float a[3], const float b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+// M^1/2 and M^-1/2 at a node (both 0 without mass).
+__device__ __forceinline__ void mass_scales(float m, float& sq, float& isq) {
+  isq = m > 0.0f ? rsqrt_nr(m) : 0.0f;
+  sq = m * isq;
+}
+
+// r_0 = M^1/2 v* - (I + c M^-1/2 K M^-1/2) M^1/2 v* = -c M^-1/2 K v*
+// (c = beta dt^2), u = M^-1/2 r_0; |M^1/2 v*|^2 and |r_0|^2.
+__global__ void __launch_bounds__(256) k_cr_begin(const SceneDev* __restrict__ scenes,
+                                                  const int* __restrict__ active_prefix, int nscenes) {
+  for_active_nodes(
+      scenes, active_prefix, nscenes, [](const SceneDev& S) { return cr_running(S, 0); },
+      [](const SceneDev& S, int slot, int node, double& bb, double& rr) {
+        const size_t i = (size_t)slot * kBlockNodes + node;
+        float ku[3];
+        take_ku(S, slot, node, true, ku);
+        const float4 vm = S.crv[i];
+        float sq, isq;
+        mass_scales(vm.w, sq, isq);
+        const float ci = -S.imp_beta * S.dt * S.dt * isq;
+        const float r[3] = {ci * ku[0], ci * ku[1], ci * ku[2]};
+        float* u = S.cru + (size_t)slot * kImpBlockFloats + 3 * node;
+        u[0] = isq * r[0];
+        u[1] = isq * r[1];
+        u[2] = isq * r[2];
+        const float b[3] = {sq * vm.x, sq * vm.y, sq * vm.z};
+        bb = (double)dot3f(b, b);
+        rr = (double)dot3f(r, r);
+      },
+      [](const SceneDev& S, double*& d0, double*& d1) {
+        d0 = &S.crs->bb;
+        d1 = &S.crs->rr[0];
+      });
+}
+
+// The residual r = M^1/2 u at one node and A r = r + c M^-1/2 K u (zero
+// where the node has no mass).
+__device__ __forceinline__ void residual_and_ar(const SceneDev& S, int slot, int node, bool take, float r[3],
+                                                float ar[3]) {
+  float ku[3];
+  take_ku(S, slot, node, take, ku);
+  float sq, isq;
+  mass_scales(S.crv[(size_t)slot * kBlockNodes + node].w, sq, isq);
+  const float ci = S.imp_beta * S.dt * S.dt * isq;
+  const float* u = S.cru + (size_t)slot * kImpBlockFloats + 3 * node;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    r[k] = sq * u[k];
+    ar[k] = r[k] + ci * ku[k];
+  }
+}
+
+// Iteration k: (r_{k-1}, A r_{k-1}).
+__global__ void __launch_bounds__(256) k_cr_rar(const SceneDev* __restrict__ scenes,
+                                                const int* __restrict__ active_prefix, int nscenes, int k) {
+  for_active_nodes(
+      scenes, active_prefix, nscenes, [k](const SceneDev& S) { return cr_running(S, k); },
+      [](const SceneDev& S, int slot, int node, double& rar, double&) {
+        float r[3], ar[3];
+        residual_and_ar(S, slot, node, false, r, ar);
+        rar = (double)dot3f(r, ar);
+      },
+      [k](const SceneDev& S, double*& d0, double*& d1) {
+        d0 = &S.crs->rAr[k];
+        d1 = nullptr;
+      });
+}
+
+// Iteration k: beta = rAr[k] / rAr[k-1]; p = r + beta p, A p = A r + beta A p
+// (k = 1: p = r, A p = A r); |A p|^2. K r is consumed here.
+__global__ void __launch_bounds__(256) k_cr_dir(const SceneDev* __restrict__ scenes,
+                                                const int* __restrict__ active_prefix, int nscenes, int k) {
+  for_active_nodes(
+      scenes, active_prefix, nscenes, [k](const SceneDev& S) { return cr_running(S, k); },
+      [k](const SceneDev& S, int slot, int node, double& apap, double&) {
+        const size_t i = (size_t)slot * kBlockNodes + node;
+        const size_t plane = (size_t)S.pool_cap * kBlockNodes;
+        float r[3], ar[3];
+        residual_and_ar(S, slot, node, true, r, ar);
+        const CrScalars& c = *S.crs;
+        float beta = 0.0f;
+        if (k > 1 && c.rAr[k - 1] != 0.0) beta = (float)(c.rAr[k] / c.rAr[k - 1]);
+        float p[3] = {r[0], r[1], r[2]}, ap[3] = {ar[0], ar[1], ar[2]};
+        if (k > 1) {
+          const float4 p0 = S.crv[plane + i], a0 = S.crv[2 * plane + i];
+          p[0] += beta * p0.x;
+          p[1] += beta * p0.y;
+          p[2] += beta * p0.z;
+          ap[0] += beta * a0.x;
+          ap[1] += beta * a0.y;
+          ap[2] += beta * a0.z;
+        }
+        S.crv[plane + i] = make_float4(p[0], p[1], p[2], 0.0f);
+        S.crv[2 * plane + i] = make_float4(ap[0], ap[1], ap[2], 0.0f);
+        apap = (double)dot3f(ap, ap);
+      },
+      [k](const SceneDev& S, double*& d0, double*& d1) {
+        d0 = &S.crs->ApAp[k];
+        d1 = nullptr;
+      });
+}
+
+// Iteration k: alpha = rAr[k] / ApAp[k]; y += alpha p (v += alpha M^-1/2 p),
+// r -= alpha A p (u = M^-1/2 r); |r|^2.
+__global__ void __launch_bounds__(256) k_cr_update(const SceneDev* __restrict__ scenes,
+                                                   const int* __restrict__ active_prefix, int nscenes, int k) {
+  for_active_nodes(
+      scenes, active_prefix, nscenes, [k](const SceneDev& S) { return cr_running(S, k); },
+      [k](const SceneDev& S, int slot, int node, double& rr, double&) {
+        const size_t i = (size_t)slot * kBlockNodes + node;
+        const size_t plane = (size_t)S.pool_cap * kBlockNodes;
+        const CrScalars& c = *S.crs;
+        const float alpha = c.ApAp[k] > 0.0 ? (float)(c.rAr[k] / c.ApAp[k]) : 0.0f;
+        float4 vm = S.crv[i];
+        float sq, isq;
+        mass_scales(vm.w, sq, isq);
+        const float4 p = S.crv[plane + i], ap = S.crv[2 * plane + i];
+        const float ai = alpha * isq;
+        vm.x += ai * p.x;
+        vm.y += ai * p.y;
+        vm.z += ai * p.z;
+        S.crv[i] = vm;
+        float* u = S.cru + (size_t)slot * kImpBlockFloats + 3 * node;
+        const float r[3] = {sq * u[0] - alpha * ap.x, sq * u[1] - alpha * ap.y, sq * u[2] - alpha * ap.z};
+        u[0] = isq * r[0];
+        u[1] = isq * r[1];
+        u[2] = isq * r[2];
+        if (slot == 0 && node == 0) S.crs->iters = k;
+        rr = (double)dot3f(r, r);
+      },
+      [k](const SceneDev& S, double*& d0, double*& d1) {
+        d0 = &S.crs->rr[k];
+        d1 = nullptr;
+      });
+}
+
+// The colliders on the solved v (gForceCompute.glsl:72-93 at the node), then
+// gout's (v*, d) becomes (v, d + v - v*) so that d = v - alpha p/m.
+__global__ void __launch_bounds__(256) k_cr_end(const SceneDev* __restrict__ scenes,
+                                                const int* __restrict__ active_prefix, int nscenes) {
+  for_active_nodes(
+      scenes, active_prefix, nscenes, [](const SceneDev& S) { return S.crs != nullptr; },
+      [](const SceneDev& S, int slot, int node, double&, double&) {
+        const float4 xm = S.crv[(size_t)slot * kBlockNodes + node];
+        if (!(xm.w > 0.0f)) return;
+        const int b = S.active[slot];
+        const int bx = b % S.bdim[0], by = (b / S.bdim[0]) % S.bdim[1], bz = b / (S.bdim[0] * S.bdim[1]);
+        const int gi = 4 * bx + (node & 3), gj = 4 * by + ((node >> 2) & 3), gk = 4 * bz + (node >> 4);
+        const float xi[3] = {__fadd_rn(S.gpos[0], __fmul_rn(S.h, (float)gi)),
+                             __fadd_rn(S.gpos[1], __fmul_rn(S.h, (float)gj)),
+                             __fadd_rn(S.gpos[2], __fmul_rn(S.h, (float)gk))};
+        float v[3] = {xm.x, xm.y, xm.z};
+        collide(S.coll, S.ncoll, xi, v);
+        float* o = S.gout + (size_t)slot * kOutBlockFloats + kOutFields * node;
+        const float vs[3] = {o[0], o[1], o[2]};
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          o[3 + k] += v[k] - vs[k];
+          o[k] = v[k];
+        }
+      },
+      [](const SceneDev& S, double*& d0, double*& d1) {
+        d0 = &S.crs->bb;  // nothing is added (both sums are zero)
+        d1 = nullptr;
+      });
+}
+
+int hess_smem() {
+  static bool configured = false;
+  const int bytes = (int)sizeof(ItemShared);
+  if (!configured) {
+    cudaFuncSetAttribute(k_hess, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    configured = true;
+  }
+  return bytes;
+}
+
+}  // namespace
+
+void fast_implicit_setup() { hess_smem(); }
+
+void fast_implicit_solve(const SceneDev* scenes, const int* item_prefix, const int* active_prefix, int nscenes,
+                         int max_iters, int item_ctas, int grid_ctas, cudaStream_t st) {
+  const int smem = hess_smem();
+  k_hess<<<item_ctas, kItemMax, smem, st>>>(scenes, item_prefix, nscenes, 0);
+  k_cr_begin<<<grid_ctas, 256, 0, st>>>(scenes, active_prefix, nscenes);
+  for (int k = 1; k <= max_iters && k <= kCrMaxIters; k++) {
+    k_hess<<<item_ctas, kItemMax, smem, st>>>(scenes, item_prefix, nscenes, k);
+    k_cr_rar<<<grid_ctas, 256, 0, st>>>(scenes, active_prefix, nscenes, k);
+    k_cr_dir<<<grid_ctas, 256, 0, st>>>(scenes, active_prefix, nscenes, k);
+    k_cr_update<<<grid_ctas, 256, 0, st>>>(scenes, active_prefix, nscenes, k);
+  }
+  k_cr_end<<<grid_ctas, 256, 0, st>>>(scenes, active_prefix, nscenes);
+}
+
+}  // namespace snow

@@ -188,8 +188,16 @@ bool valid_params(const snow_params* p) {
   if (!(p->grid_spacing > 0.0f)) return false;
   if ((double)p->grid_dim[0] * p->grid_dim[1] * p->grid_dim[2] > 2.0e9) return false;
   if (p->mode != SNOW_MODE_REFERENCE && p->mode != SNOW_MODE_FAST) return false;
+  if (!(p->implicit_beta >= 0.0f && p->implicit_beta <= 1.0f)) return false;
+  if (!(p->implicit_tolerance >= 0.0f) || !std::isfinite(p->implicit_tolerance)) return false;
+  if (p->implicit_max_iters < 0 || p->implicit_max_iters > kCrMaxIters) return false;
   return true;
 }
+
+// The semi-implicit solve's settings with the library defaults filled in.
+bool is_implicit(const snow_params& p) { return p.implicit_beta > 0.0f; }
+int implicit_iters(const snow_params& p) { return p.implicit_max_iters > 0 ? p.implicit_max_iters : 50; }
+float implicit_tol(const snow_params& p) { return p.implicit_tolerance > 0.0f ? p.implicit_tolerance : 1e-5f; }
 
 void fill_sd_params(snow_scene* s) {
   SceneDev& d = s->sd;
@@ -217,6 +225,9 @@ void fill_sd_params(snow_scene* s) {
   d.alpha = s->p.alpha;
   d.ncoll = s->ncoll;
   d.coll = s->coll_d;
+  d.imp_beta = s->p.implicit_beta;
+  d.imp_tol = implicit_tol(s->p);
+  d.imp_maxit = implicit_iters(s->p);
 }
 
 snow_status push_sd(snow_scene* s) {
@@ -262,6 +273,7 @@ snow_status fast_alloc_grid(snow_scene* s) {
       (st = salloc(s, (size_t)kCounterStride, &d.counters)) || (st = salloc(s, (size_t)8, &s->d_prefix)) ||
       (st = salloc(s, (size_t)1, &s->sd_dev)))
     return st;
+  if (is_implicit(s->p) && (st = salloc(s, (size_t)1, &d.crs))) return st;
   snow_ctx* ctx = s->ctx;
   CK(cudaMemsetAsync(d.blk_flag, 0, nb * sizeof(int), ctx->stream));
   CK(cudaMemsetAsync(d.blk_slot, 0xff, nb * sizeof(int), ctx->stream));
@@ -276,10 +288,17 @@ snow_status fast_alloc_pool(snow_scene* s, int cap_blocks) {
   snow_ctx* ctx = s->ctx;
   if (d.gout) dfree_one(ctx, s, d.gout);
   if (d.active) dfree_one(ctx, s, d.active);
+  if (d.crv) dfree_one(ctx, s, d.crv);
+  if (d.cru) dfree_one(ctx, s, d.cru);
   d.gout = nullptr;
   d.active = nullptr;
+  d.crv = nullptr;
+  d.cru = nullptr;
   snow_status st;
   if ((st = salloc(s, (size_t)cap_blocks * kOutBlockFloats, &d.gout)) || (st = salloc(s, (size_t)cap_blocks, &d.active)))
+    return st;
+  if (d.crs && ((st = salloc(s, (size_t)cap_blocks * kBlockNodes * 3, &d.crv)) ||
+                (st = salloc(s, (size_t)cap_blocks * kImpBlockFloats, &d.cru))))
     return st;
   d.pool_cap = cap_blocks;
   return SNOW_OK;
@@ -316,6 +335,12 @@ void fast_enqueue_p2g(snow_scene* s, bool mass_only, cudaStream_t st) {
 void fast_enqueue_grid(snow_scene* s, bool clear_only, cudaStream_t st) {
   fast_grid(s->sd_dev, s->d_prefix + 2, 1, grid_ctas(), clear_only, st);
 }
+// The semi-implicit solve after the grid update (explicit scenes: nothing).
+void fast_enqueue_solve(snow_scene* s, cudaStream_t st) {
+  if (s->sd.crs)
+    fast_implicit_solve(s->sd_dev, s->d_prefix + 0, s->d_prefix + 2, 1, s->sd.imp_maxit, item_ctas(s->tune),
+                        grid_ctas(), st);
+}
 // One step of a scene whose P2G sums of the current state are pending in
 // acc: rigid advance, [binning], grid update, G2P + advance + next P2G.
 void fast_enqueue_step(snow_scene* s, bool bin, cudaStream_t st) {
@@ -323,6 +348,7 @@ void fast_enqueue_step(snow_scene* s, bool bin, cudaStream_t st) {
   if (bin) fast_bin(s, st);
   fast_enqueue_compact(s, st, true);
   fast_enqueue_grid(s, false, st);
+  fast_enqueue_solve(s, st);
   fast_g2p2g(s->sd_dev, s->d_prefix + 0, 1, item_ctas(s->tune), st);
 }
 
@@ -363,6 +389,7 @@ snow_status fast_init(snow_scene* s) {
   cudaStream_t st = ctx->stream;
   snow_status r;
   s->sd.n = (int)s->n;
+  if (s->sd.crs) fast_implicit_setup();
   if ((r = fast_single_prefix(s))) return r;
   if ((r = push_sd(s))) return r;
   fast_bin(s, st);
@@ -615,14 +642,19 @@ size_t snow_scene_footprint(const snow_params* p, size_t n) {
   // staging copy of the caller's arrays (x, v, m, F_E, F_P: 100 B).
   const double tiles = (double)radix_tiles(n);
   const double items = (double)n / kMinItemMax + std::min((double)n, nb) + 1;
+  // A semi-implicit scene adds per pool block its solver planes (64 nodes x
+  // (3 float4 + 3 floats)) and one scalar record.
+  const double solver = is_implicit(*p) ? nb * (64 * (48.0 + 12.0)) + sizeof(CrScalars) : 0.0;
   return (size_t)(n * (92.0 + 108.0 + 100.0) + tiles * 256 * 4.0 + 4096.0 + items * 16.0 + nb * (448 * 4.0 + 5 * 4.0) +
-                  nb * (384 * 4.0 + 4.0) + 1024.0);
+                  nb * (384 * 4.0 + 4.0) + solver + 1024.0);
 }
 
 snow_status snow_scene_create(snow_ctx* ctx, const snow_params* p, const snow_collider* colliders, int n_colliders,
                               size_t capacity, snow_scene** out) {
   if (!ctx || !out || !valid_params(p) || n_colliders < 0 || (n_colliders > 0 && !colliders))
     return fail(ctx, SNOW_EINVAL, "snow_scene_create: invalid argument");
+  if (p->mode == SNOW_MODE_REFERENCE && is_implicit(*p))
+    return fail(ctx, SNOW_EUNSUPPORTED, "the semi-implicit update has no shader counterpart: FAST mode only");
   *out = nullptr;
   CK(cudaSetDevice(ctx->device));
   snow_scene* s = new snow_scene();
@@ -878,6 +910,7 @@ snow_status snow_dispatch(snow_scene* s, int kernel, double dt) {
     case SNOW_K_G_FORCE:
       fast_enqueue_compact(s, st);
       fast_enqueue_grid(s, false, st);
+      fast_enqueue_solve(s, st);
       s->p2g_ready = false;
       break;
     case SNOW_K_G2P:
@@ -940,15 +973,18 @@ snow_status snow_scene_step(snow_scene* s, double dt, int n_steps) {
       fast_enqueue_compact(s, st, true);
       fast_enqueue_grid(s, false, st);
       CK(cudaEventRecord(ev[2], st));
-      fast_g2p2g(s->sd_dev, s->d_prefix + 0, 1, item_ctas(s->tune), st);
+      fast_enqueue_solve(s, st);
       CK(cudaEventRecord(ev[3], st));
-      CK(cudaEventSynchronize(ev[3]));
-      float t[3];
-      for (int k = 0; k < 3; k++) cudaEventElapsedTime(&t[k], ev[k], ev[k + 1]);
+      fast_g2p2g(s->sd_dev, s->d_prefix + 0, 1, item_ctas(s->tune), st);
+      CK(cudaEventRecord(ev[4], st));
+      CK(cudaEventSynchronize(ev[4]));
+      float t[4];
+      for (int k = 0; k < 4; k++) cudaEventElapsedTime(&t[k], ev[k], ev[k + 1]);
       s->times.sort_ms += t[0];
       s->times.grid_ms += t[1];
-      s->times.g2p_ms += t[2];
-      s->times.total_ms += t[0] + t[1] + t[2];
+      s->times.other_ms += t[2];  // the semi-implicit solve
+      s->times.g2p_ms += t[3];
+      s->times.total_ms += t[0] + t[1] + t[2] + t[3];
       s->times.steps++;
     } else if (!ctx->graphs) {
       fast_enqueue_step(s, bin, st);
@@ -1221,6 +1257,20 @@ snow_status snow_scene_phase_times(snow_scene* s, snow_phase_times* out, int res
   return SNOW_OK;
 }
 
+snow_status snow_scene_solver_report(snow_scene* s, snow_solver_report* out) {
+  if (!s || !out) return SNOW_EINVAL;
+  snow_ctx* ctx = s->ctx;
+  if (!s->sd.crs) return fail(ctx, SNOW_EUNSUPPORTED, "the scene steps explicitly");
+  CrScalars c;
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(&c, s->sd.crs, sizeof c, cudaMemcpyDeviceToHost));
+  out->iterations = c.iters;
+  out->max_iters = s->sd.imp_maxit;
+  out->initial_residual = c.bb > 0.0 ? std::sqrt(c.rr[0] / c.bb) : 0.0;
+  out->residual = c.bb > 0.0 ? std::sqrt(c.rr[c.iters] / c.bb) : 0.0;
+  return SNOW_OK;
+}
+
 // ---- batches ----------------------------------------------------------------
 snow_status snow_batch_create(snow_ctx* ctx, snow_scene* const* scenes, int n, snow_batch** out) {
   if (!ctx || !scenes || n <= 0 || !out) return fail(ctx, SNOW_EINVAL, "snow_batch_create: invalid argument");
@@ -1323,6 +1373,10 @@ void batch_enqueue_step(snow_batch* b, int phase, int interval, cudaStream_t st)
   }
   fast_compact(b->d_scenes, blocks, n, b->total_blocks, items, active, st);
   fast_grid(b->d_scenes, active, n, grid_ctas(), false, st);
+  int iters = 0;  // the solve runs while any semi-implicit scene still iterates
+  for (snow_scene* s : b->scenes)
+    if (s->sd.crs) iters = std::max(iters, s->sd.imp_maxit);
+  if (iters > 0) fast_implicit_solve(b->d_scenes, items, active, n, iters, item_ctas(b->scenes[0]->tune), grid_ctas(), st);
   fast_g2p2g(b->d_scenes, items, n, item_ctas(b->scenes[0]->tune), st);
 }
 

@@ -64,6 +64,21 @@ enum {
   kCounterStride = 8
 };
 
+// Semi-implicit velocity solve: conjugate residuals on the mass-scaled form
+// of (M + beta dt^2 K) v = M v* over the active nodes, one record per scene,
+// cleared at the start of each step. Iteration k (1-based) forms
+// rAr[k] = (r_{k-1}, A r_{k-1}), ApAp[k] = |A p_{k-1}|^2 and rr[k] = |r_k|^2.
+constexpr int kCrMaxIters = 128;
+struct CrScalars {
+  double bb;                   // |M^1/2 v*|^2
+  double rr[kCrMaxIters + 1];  // rr[0]: the initial residual
+  double rAr[kCrMaxIters + 1];
+  double ApAp[kCrMaxIters + 1];
+  int iters;                   // iterations taken
+  int pad;
+};
+constexpr int kImpBlockFloats = 3 * kBlockNodes;  // 192: one 3-vector per node
+
 // Device-resident description of one FAST scene (read by every kernel).
 struct SceneDev {
   float gpos[3];
@@ -100,6 +115,13 @@ struct SceneDev {
   int4* items;
   int item_cap;
   int* counters;    // kCounterStride ints
+  // semi-implicit velocity solve (crs == nullptr: the scene steps explicitly)
+  float imp_beta;   // beta of (M + beta dt^2 K) v = M v*
+  float imp_tol;    // stop once |r| <= imp_tol |M^1/2 v*| (r of the mass-scaled system)
+  int imp_maxit;    // at most this many iterations per step
+  float4* crv;      // 3 planes of pool_cap x 64 float4 per node: (v, m), (p, 0), (A p, 0)
+  float* cru;       // pool_cap x 192: u = M^-1/2 r (the vector K is applied to), 3 floats per node
+  CrScalars* crs;
 };
 
 struct FastTuning {
@@ -131,6 +153,16 @@ void fast_grid(const SceneDev* scenes, const int* active_prefix, int nscenes, in
 void fast_volume(const SceneDev* sd_dev, int n, cudaStream_t st);
 void fast_g2p_advance(const SceneDev* scenes, const int* item_prefix, int nscenes, int grid_ctas, cudaStream_t st);
 void fast_g2p2g(const SceneDev* scenes, const int* item_prefix, int nscenes, int grid_ctas, cudaStream_t st);
+// The semi-implicit velocity solve between the grid update (which leaves
+// v*, m and u = v* in the solver planes) and G2P: max_iters iterations of
+// conjugate residuals (each a K u pass over the items and three passes over
+// the active nodes; a scene that has converged skips the rest), then the
+// colliders on v and v, d written back into gout. Scenes without a solver
+// record are left alone.
+void fast_implicit_solve(const SceneDev* scenes, const int* item_prefix, const int* active_prefix, int nscenes,
+                         int max_iters, int item_ctas, int grid_ctas, cudaStream_t st);
+// Kernel attributes of the solve (outside any stream capture).
+void fast_implicit_setup();
 
 // Binning of one scene (host-side sizes known): keys -> radix sort ->
 // permutation of the particle streams -> P2G work items.

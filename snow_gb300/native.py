@@ -30,7 +30,7 @@ EXPORTS = [
     "snow_batch_step", "snow_batch_autotune", "snow_sort_keys_static", "snow_server_create", "snow_server_destroy",
     "snow_server_submit", "snow_server_poll", "snow_server_fetch", "snow_server_stats", "snow_server_drain",
     "snow_scene_set_tuning", "snow_batch_set_tuning", "snow_ctx_set_graphs", "snow_scene_stats_enqueue",
-    "snow_ctx_stats_read",
+    "snow_ctx_stats_read", "snow_scene_solver_report",
 ]
 SORT_STATIC_MAX_KEYS = 262144  # SNOW_SORT_STATIC_MAX_KEYS
 
@@ -39,7 +39,8 @@ class SnowParams(C.Structure):
     _fields_ = [("grid_pos", C.c_float * 3), ("grid_dim", C.c_int * 3), ("grid_spacing", C.c_float),
                 ("young", C.c_float), ("poisson", C.c_float), ("hardening", C.c_float),
                 ("crit_compression", C.c_float), ("crit_stretch", C.c_float), ("alpha", C.c_float),
-                ("gravity", C.c_float * 3), ("mode", C.c_int), ("sort_interval", C.c_int)]
+                ("gravity", C.c_float * 3), ("mode", C.c_int), ("sort_interval", C.c_int),
+                ("implicit_beta", C.c_float), ("implicit_tolerance", C.c_float), ("implicit_max_iters", C.c_int)]
 
 
 class SnowCollider(C.Structure):
@@ -56,6 +57,11 @@ class SnowStats(C.Structure):
 class SnowPhaseTimes(C.Structure):
     _fields_ = [("sort_ms", C.c_double), ("p2g_ms", C.c_double), ("grid_ms", C.c_double), ("g2p_ms", C.c_double),
                 ("other_ms", C.c_double), ("total_ms", C.c_double), ("steps", C.c_uint64)]
+
+
+class SnowSolverReport(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("max_iters", C.c_int), ("residual", C.c_double),
+                ("initial_residual", C.c_double)]
 
 
 class SnowTuning(C.Structure):
@@ -146,6 +152,7 @@ def load(path: str = LIB_PATH):
     L.snow_scene_size.restype = sz
     L.snow_scene_cell_keys.argtypes = [vp, up, up]
     L.snow_scene_phase_times.argtypes = [vp, C.POINTER(SnowPhaseTimes), C.c_int]
+    L.snow_scene_solver_report.argtypes = [vp, C.POINTER(SnowSolverReport)]
     L.snow_batch_create.argtypes = [vp, C.POINTER(vp), C.c_int, C.POINTER(vp)]
     L.snow_batch_destroy.argtypes = [vp]
     L.snow_batch_destroy.restype = None

@@ -68,6 +68,11 @@ class Scene:
     dt: float = PHYSIC_DT
     steps: int = 1
     colliders: List[Collider] = dataclasses.field(default_factory=list)
+    # semi-implicit velocity update: beta > 0 solves (M + beta dt^2 K) v = M v*
+    # each step (0 = the explicit step; tolerance / iterations 0 = defaults)
+    implicit_beta: float = 0.0
+    implicit_tolerance: float = 0.0
+    implicit_max_iters: int = 0
     x: Optional[np.ndarray] = None   # N x 3 float32
     v: Optional[np.ndarray] = None   # N x 3 float32
     m: Optional[np.ndarray] = None   # N float32

@@ -48,7 +48,7 @@ def test_struct_layouts_match_the_header():
     from snow_gb300 import native
     # snow_collider is the reference's cx, cv, cn vec4 triple: 48 bytes
     assert ctypes.sizeof(native.SnowCollider) == 48
-    assert ctypes.sizeof(native.SnowParams) == 4 * (3 + 3 + 1 + 6 + 3 + 2)
+    assert ctypes.sizeof(native.SnowParams) == 4 * (3 + 3 + 1 + 6 + 3 + 2 + 3)
 
 
 def test_ctypes_structs_match_the_c_compiler_layout(tmp_path):
@@ -61,7 +61,8 @@ def test_ctypes_structs_match_the_c_compiler_layout(tmp_path):
     pairs = {"snow_params": N.SnowParams, "snow_collider": N.SnowCollider, "snow_stats": N.SnowStats,
              "snow_phase_times": N.SnowPhaseTimes, "snow_tuning": N.SnowTuning,
              "snow_server_config": N.SnowServerConfig, "snow_job_desc": N.SnowJobDesc,
-             "snow_job_result": N.SnowJobResult, "snow_server_report": N.SnowServerStats}
+             "snow_job_result": N.SnowJobResult, "snow_server_report": N.SnowServerStats,
+             "snow_solver_report": N.SnowSolverReport}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "snow_mpm.h"', "int main(void) {"]
     for cname, ct in pairs.items():
         lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')

@@ -1,0 +1,157 @@
+"""GPU tests of the semi-implicit velocity update (FAST mode) against the
+oracle's FP64 restatement (the reference's SemiImplicitTimeUpdate is an
+empty stub, semiimplicittimeupdate.cpp:3-5).
+
+The scenes are snowballs with random particle velocities: a rough v* on which
+the implicit term (M + beta dt^2 K) acts strongly. Velocities are compared in
+the kinetic-energy norm |M^1/2 v|, the norm the solve's residual is measured
+in."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from snow_gb300 import scenes
+
+gpu = pytest.mark.gpu
+
+DT = 5e-3
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from snow_gb300 import api
+    return api.Context(0)
+
+
+def _rough_scene(seed=5, n=3000, edge=32, young=1.4e7, beta=1.0, tol=1e-6, iters=100):
+    s = scenes.small_scene(n=n, grid_edge=edge, seed=seed, young=young)
+    s.v = np.random.default_rng(seed + 100).normal(size=(s.n, 3)).astype(np.float32)
+    s.dt = DT
+    s.implicit_beta, s.implicit_tolerance, s.implicit_max_iters = beta, tol, iters
+    return s
+
+
+def _oracle_grid(s, tol=1e-10):
+    o = O.OracleSim(s, O.EXACT64, vround=False).upload().init()
+    o.phase(O.PH_RESET)
+    o.phase(O.PH_P2G)
+    o.phase(O.PH_GRID, s.dt)
+    g = o.grid()
+    vstar, m = g["vstar"].copy(), g["mass"]
+    o.set_implicit(s.implicit_beta, tol, 200)
+    o.phase(O.PH_IMPLICIT, s.dt)
+    return m, vstar, o.grid()["vstar"], o.solver_report()
+
+
+def _energy(m, a):
+    return float(np.sqrt(np.sum(m[:, None] * a * a)))
+
+
+@gpu
+@pytest.mark.parametrize("seed,young", [(5, 1.4e7), (6, 1.4e6), (7, 1.4e8)])
+def test_solved_grid_velocity_matches_the_oracle(ctx, seed, young):
+    from snow_gb300 import api, native as N
+    s = _rough_scene(seed=seed, young=young)
+    g = api.SimScene(ctx, s).upload().init()
+    g.dispatch(N.K_P2G, s.dt)
+    g.dispatch(N.K_G_FORCE, s.dt)  # grid update + solve
+    v_gpu = g.grid()["vstar"].astype(np.float64)
+    rep = g.solver_report()
+    m, vstar, v_ref, orep = _oracle_grid(s)
+    scale = _energy(m, vstar)
+    corr = _energy(m, v_ref - vstar)
+    print(rep, orep, _energy(m, v_gpu - v_ref) / scale, _energy(m, v_gpu - v_ref) / corr)
+    assert orep["initial_residual"] > 1e-3  # the implicit term is not negligible
+    assert 0 < rep["iterations"] <= rep["max_iters"]
+    assert rep["residual"] <= s.implicit_tolerance
+    assert abs(rep["initial_residual"] - orep["initial_residual"]) <= 1e-3 * orep["initial_residual"] + 1e-6
+    # the solution: within a few tolerances of the exact solve in the energy
+    # norm, plus FP32 rounding of the operator, which grows with |c K| (of the
+    # order of the initial residual)
+    tol = 5 * s.implicit_tolerance + 5e-6 * (1.0 + orep["initial_residual"])
+    assert _energy(m, v_gpu - v_ref) <= tol * scale
+    live = m > 0
+    assert np.all(v_gpu[~live] == 0)
+
+
+@gpu
+def test_one_semi_implicit_step_matches_the_oracle(ctx):
+    from snow_gb300 import api
+    s = _rough_scene(seed=8, tol=1e-7)
+    a = api.SimScene(ctx, s).upload().init().step(s.dt, 1).download()
+    o = O.OracleSim(s, O.EXACT64, vround=False).upload().init().set_implicit(1.0, 1e-10, 200).step(s.dt, 1)
+    b = o.state()
+    vscale = np.abs(b["v"]).max()
+    assert np.abs(a["x"] - b["x"]).max() <= 1e-5 * 1.0 + 2e-6 * vscale * s.dt
+    assert np.abs(a["v"] - b["v"]).max() <= 1e-4 * vscale
+    assert np.abs(a["FE"] - b["FE"]).max() <= 1e-4
+    assert np.abs(a["Jp"] - b["Jp"]).max() <= 1e-4
+    # and the step differs from the explicit one: the solve did something
+    e = O.OracleSim(s, O.EXACT64, vround=False).upload().init().step(s.dt, 1).state()
+    assert np.abs(e["v"] - b["v"]).max() > 100 * np.abs(a["v"] - b["v"]).max()
+
+
+@gpu
+def test_batch_with_implicit_and_explicit_scenes_matches_each_alone(ctx):
+    from snow_gb300 import api, native as N
+    scs = [_rough_scene(seed=9, n=2500, edge=32), _rough_scene(seed=10, n=4000, edge=40, beta=0.0),
+           _rough_scene(seed=11, n=1500, edge=24, beta=0.5, iters=30)]
+    for sc in scs:
+        sc.v *= 0.2
+    steps = 4
+    alone = []
+    for sc in scs:
+        sm = api.SimScene(ctx, sc).upload().init().step(sc.dt, steps)
+        alone.append(sm.download())
+    sims = [api.SimScene(ctx, sc).upload().init() for sc in scs]
+    api.Batch(ctx, sims).step(steps, dt=[sc.dt for sc in scs])
+    for a, sm in zip(alone, sims):
+        b = sm.download()
+        assert np.abs(a["x"] - b["x"]).max() <= 1e-4
+        assert np.abs(a["v"] - b["v"]).max() <= 1e-3 * max(1.0, np.abs(a["v"]).max())
+    assert sims[0].solver_report()["iterations"] > 0
+    with pytest.raises(N.SnowError) as e:
+        sims[1].solver_report()
+    assert e.value.status == -8  # SNOW_EUNSUPPORTED: the scene steps explicitly
+
+
+@gpu
+def test_semi_implicit_steps_stay_finite_and_conserve_mass(ctx):
+    from snow_gb300 import api
+    s = _rough_scene(seed=12, n=4000, edge=32, young=1.4e8)
+    s.v *= 0.1
+    sim = api.SimScene(ctx, s).upload().init()
+    m0 = sim.stats()["mass"]
+    for _ in range(10):
+        sim.step(s.dt, 1)
+        rep = sim.solver_report()
+        assert rep["residual"] <= s.implicit_tolerance or rep["iterations"] == rep["max_iters"]
+    st = sim.stats()
+    assert st["nonfinite"] == 0
+    assert abs(st["mass"] - m0) <= 1e-6 * m0
+
+
+@gpu
+def test_reference_mode_has_no_semi_implicit_update(ctx):
+    from snow_gb300 import api, native as N
+    s = _rough_scene(seed=13, n=500, edge=16)
+    with pytest.raises(N.SnowError) as e:
+        api.SimScene(ctx, s, mode=N.MODE_REFERENCE)
+    assert e.value.status == -8
+    bad = _rough_scene(seed=13, n=500, edge=16, beta=1.5)
+    with pytest.raises(N.SnowError) as e:
+        api.SimScene(ctx, bad)
+    assert e.value.status == -1
+
+
+@gpu
+def test_engine_classes_drive_the_semi_implicit_update(ctx):
+    from snow_gb300 import api
+    s = scenes.small_scene(n=2000, grid_edge=32, seed=14)
+    engine = api.MPMPhysicEngine(api.SemiImplicitTimeUpdate(s, ctx=ctx, beta=1.0, tolerance=1e-6))
+    assert engine.init()
+    for _ in range(3):
+        engine.update(s.dt)
+    sim = engine.integration.sim
+    assert sim.stats()["nonfinite"] == 0
+    assert sim.solver_report()["max_iters"] == 50
