@@ -46,6 +46,14 @@ __device__ __forceinline__ bool cr_running(const SceneDev& S, int k) {
   return c.rr[k - 1] > tol * tol * c.bb;
 }
 
+// Whether any scene of the launch runs iteration k (a launch of an iteration
+// that every scene has finished returns at once).
+__device__ __forceinline__ bool any_running(const SceneDev* __restrict__ scenes, int nscenes, int k) {
+  for (int s = 0; s < nscenes; s++)
+    if (cr_running(scenes[s], k)) return true;
+  return false;
+}
+
 // G = sum_j u_j (grad w_j)^T over the particle's stencil, u from the staged
 // tile (3 floats per node) when the stencil lies in it, else from cru.
 __device__ __forceinline__ void hess_gather(const ItemShared& sh, const SceneDev& S, int bx, int by, int bz,
@@ -195,6 +203,7 @@ __device__ __forceinline__ bool hess_particle(const SceneDev& S, int p, const fl
 // slots (iteration 0: u = v*).
 __global__ void __launch_bounds__(kItemMax, 2) k_hess(const SceneDev* __restrict__ scenes,
                                                       const int* __restrict__ item_prefix, int nscenes, int k) {
+  if (!any_running(scenes, nscenes, k)) return;
   extern __shared__ float4 smem_raw[];
   ItemShared& sh = *reinterpret_cast<ItemShared*>(smem_raw);
   tile_init(sh);
@@ -249,6 +258,9 @@ template <class Run, class Body, class Target>
 __device__ __forceinline__ void for_active_nodes(const SceneDev* __restrict__ scenes,
                                                  const int* __restrict__ active_prefix, int nscenes, Run run,
                                                  Body body, Target target) {
+  bool any = false;
+  for (int s = 0; s < nscenes && !any; s++) any = run(scenes[s]);
+  if (!any) return;
   const int groups = blockDim.x / kBlockNodes;
   const int node = threadIdx.x % kBlockNodes;
   const long long total = active_prefix[nscenes];

@@ -43,6 +43,11 @@ def _oracle_grid(s, tol=1e-10):
     return m, vstar, o.grid()["vstar"], o.solver_report()
 
 
+def orep_at(s, tol):
+    """Iterations the oracle's solve takes at tolerance `tol`."""
+    return _oracle_grid(s, tol)[3]["iterations"]
+
+
 def _energy(m, a):
     return float(np.sqrt(np.sum(m[:, None] * a * a)))
 
@@ -58,18 +63,27 @@ def test_solved_grid_velocity_matches_the_oracle(ctx, seed, young):
     v_gpu = g.grid()["vstar"].astype(np.float64)
     rep = g.solver_report()
     m, vstar, v_ref, orep = _oracle_grid(s)
+    # the explicit v* of the same state on the GPU (FP32 inputs of the solve)
+    s0 = _rough_scene(seed=seed, young=young, beta=0.0)
+    g0 = api.SimScene(ctx, s0).upload().init()
+    g0.dispatch(N.K_P2G, s0.dt)
+    g0.dispatch(N.K_G_FORCE, s0.dt)
+    vstar_gpu = g0.grid()["vstar"].astype(np.float64)
     scale = _energy(m, vstar)
-    corr = _energy(m, v_ref - vstar)
-    print(rep, orep, _energy(m, v_gpu - v_ref) / scale, _energy(m, v_gpu - v_ref) / corr)
+    err_in, err_out = _energy(m, vstar_gpu - vstar) / scale, _energy(m, v_gpu - v_ref) / scale
+    print(rep, orep, "v* error", err_in, "v error", err_out, "correction", _energy(m, v_ref - vstar) / scale)
     assert orep["initial_residual"] > 1e-3  # the implicit term is not negligible
     assert 0 < rep["iterations"] <= rep["max_iters"]
+    assert abs(rep["iterations"] - orep_at(s, s.implicit_tolerance)) <= 3
     assert rep["residual"] <= s.implicit_tolerance
     assert abs(rep["initial_residual"] - orep["initial_residual"]) <= 1e-3 * orep["initial_residual"] + 1e-6
-    # the solution: within a few tolerances of the exact solve in the energy
-    # norm, plus FP32 rounding of the operator, which grows with |c K| (of the
-    # order of the initial residual)
-    tol = 5 * s.implicit_tolerance + 5e-6 * (1.0 + orep["initial_residual"])
-    assert _energy(m, v_gpu - v_ref) <= tol * scale
+    # The solve's input v* carries the FP32 step's rounding: at F_E = I the
+    # FP32 polar rotation is I to ~1e-7, so the explicit force is noise of
+    # order 2 mu 1e-7, which grows with E (measured: 5e-6, 5e-5, 5e-4 of
+    # |M^1/2 v*| at E = 1.4e6, 1.4e7, 1.4e8). The solve must not amplify it:
+    # the solved v is as close to the exact FP64 solve as v* is to the FP64 v*.
+    assert err_in <= 1e-3
+    assert err_out <= max(err_in, 1e-6) + 5 * s.implicit_tolerance
     live = m > 0
     assert np.all(v_gpu[~live] == 0)
 
