@@ -29,7 +29,11 @@
 //   crs  per scene: |M^1/2 v*|^2 and per iteration (r, A r), |A p|^2, |r|^2 in FP64
 // Kernels of one iteration k: K u over the work items (k_hess), then three
 // passes over the active nodes: (r, A r); the directions p, A p and |A p|^2;
-// v, r and |r|^2. A scene whose residual met the tolerance skips the rest.
+// v, r and |r|^2; then k_cr_cond advances k (a device counter) and decides
+// whether iteration k runs. Inside a captured step graph the iterations are
+// the body of a conditional WHILE node that k_cr_cond sets, so the loop ends
+// on the device as soon as every scene has converged; without a graph the
+// host launches max_iters iterations and the finished ones return at once.
 #include "fast_item.cuh"
 
 namespace snow {
@@ -202,7 +206,9 @@ __device__ __forceinline__ bool hess_particle(const SceneDev& S, int p, const fl
 // K u for the items of every scene whose iteration k runs, into acc's force
 // slots (iteration 0: u = v*).
 __global__ void __launch_bounds__(kItemMax, 2) k_hess(const SceneDev* __restrict__ scenes,
-                                                      const int* __restrict__ item_prefix, int nscenes, int k) {
+                                                      const int* __restrict__ item_prefix, int nscenes,
+                                                      const int* __restrict__ iter) {
+  const int k = iter ? *iter : 0;  // iteration 0: K v*
   if (!any_running(scenes, nscenes, k)) return;
   extern __shared__ float4 smem_raw[];
   ItemShared& sh = *reinterpret_cast<ItemShared*>(smem_raw);
@@ -361,7 +367,9 @@ __device__ __forceinline__ void residual_and_ar(const SceneDev& S, int slot, int
 
 // Iteration k: (r_{k-1}, A r_{k-1}).
 __global__ void __launch_bounds__(256) k_cr_rar(const SceneDev* __restrict__ scenes,
-                                                const int* __restrict__ active_prefix, int nscenes, int k) {
+                                                const int* __restrict__ active_prefix, int nscenes,
+                                                const int* __restrict__ iter) {
+  const int k = *iter;
   for_active_nodes(
       scenes, active_prefix, nscenes, [k](const SceneDev& S) { return cr_running(S, k); },
       [](const SceneDev& S, int slot, int node, double& rar, double&) {
@@ -378,7 +386,9 @@ __global__ void __launch_bounds__(256) k_cr_rar(const SceneDev* __restrict__ sce
 // Iteration k: beta = rAr[k] / rAr[k-1]; p = r + beta p, A p = A r + beta A p
 // (k = 1: p = r, A p = A r); |A p|^2. K r is consumed here.
 __global__ void __launch_bounds__(256) k_cr_dir(const SceneDev* __restrict__ scenes,
-                                                const int* __restrict__ active_prefix, int nscenes, int k) {
+                                                const int* __restrict__ active_prefix, int nscenes,
+                                                const int* __restrict__ iter) {
+  const int k = *iter;
   for_active_nodes(
       scenes, active_prefix, nscenes, [k](const SceneDev& S) { return cr_running(S, k); },
       [k](const SceneDev& S, int slot, int node, double& apap, double&) {
@@ -412,7 +422,9 @@ __global__ void __launch_bounds__(256) k_cr_dir(const SceneDev* __restrict__ sce
 // Iteration k: alpha = rAr[k] / ApAp[k]; y += alpha p (v += alpha M^-1/2 p),
 // r -= alpha A p (u = M^-1/2 r); |r|^2.
 __global__ void __launch_bounds__(256) k_cr_update(const SceneDev* __restrict__ scenes,
-                                                   const int* __restrict__ active_prefix, int nscenes, int k) {
+                                                   const int* __restrict__ active_prefix, int nscenes,
+                                                   const int* __restrict__ iter) {
+  const int k = *iter;
   for_active_nodes(
       scenes, active_prefix, nscenes, [k](const SceneDev& S) { return cr_running(S, k); },
       [k](const SceneDev& S, int slot, int node, double& rr, double&) {
@@ -474,6 +486,16 @@ __global__ void __launch_bounds__(256) k_cr_end(const SceneDev* __restrict__ sce
       });
 }
 
+// Advances the iteration counter (first: to 1) and, inside a graph, sets the
+// WHILE node's condition: whether any scene runs the new iteration.
+__global__ void k_cr_cond(const SceneDev* __restrict__ scenes, int nscenes, int* iter, int first,
+                          cudaGraphConditionalHandle cond, int use_cond) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int k = first ? 1 : *iter + 1;
+  *iter = k;
+  if (use_cond) cudaGraphSetConditional(cond, any_running(scenes, nscenes, k) ? 1u : 0u);
+}
+
 int hess_smem() {
   static bool configured = false;
   const int bytes = (int)sizeof(ItemShared);
@@ -489,15 +511,51 @@ int hess_smem() {
 void fast_implicit_setup() { hess_smem(); }
 
 void fast_implicit_solve(const SceneDev* scenes, const int* item_prefix, const int* active_prefix, int nscenes,
-                         int max_iters, int item_ctas, int grid_ctas, cudaStream_t st) {
+                         int max_iters, int item_ctas, int grid_ctas, int* d_iter, cudaStream_t body,
+                         cudaStream_t st) {
   const int smem = hess_smem();
-  k_hess<<<item_ctas, kItemMax, smem, st>>>(scenes, item_prefix, nscenes, 0);
+  auto iteration = [&](cudaStream_t s) {
+    k_hess<<<item_ctas, kItemMax, smem, s>>>(scenes, item_prefix, nscenes, d_iter);
+    k_cr_rar<<<grid_ctas, 256, 0, s>>>(scenes, active_prefix, nscenes, d_iter);
+    k_cr_dir<<<grid_ctas, 256, 0, s>>>(scenes, active_prefix, nscenes, d_iter);
+    k_cr_update<<<grid_ctas, 256, 0, s>>>(scenes, active_prefix, nscenes, d_iter);
+  };
+  k_hess<<<item_ctas, kItemMax, smem, st>>>(scenes, item_prefix, nscenes, nullptr);
   k_cr_begin<<<grid_ctas, 256, 0, st>>>(scenes, active_prefix, nscenes);
-  for (int k = 1; k <= max_iters && k <= kCrMaxIters; k++) {
-    k_hess<<<item_ctas, kItemMax, smem, st>>>(scenes, item_prefix, nscenes, k);
-    k_cr_rar<<<grid_ctas, 256, 0, st>>>(scenes, active_prefix, nscenes, k);
-    k_cr_dir<<<grid_ctas, 256, 0, st>>>(scenes, active_prefix, nscenes, k);
-    k_cr_update<<<grid_ctas, 256, 0, st>>>(scenes, active_prefix, nscenes, k);
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaGraph_t g = nullptr;
+  cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, nullptr, nullptr, nullptr);
+  if (cs == cudaStreamCaptureStatusActive) {
+    // conditional WHILE node in the graph being captured; its body is
+    // captured from a second stream into the node's own graph. Errors of
+    // these calls invalidate the capture and surface at its end.
+    cudaGraphConditionalHandle cond;
+    cudaGraphConditionalHandleCreate(&cond, g, 0, cudaGraphCondAssignDefault);
+    k_cr_cond<<<1, 32, 0, st>>>(scenes, nscenes, d_iter, 1, cond, 1);
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &ndeps);
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = cond;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &p) == cudaSuccess &&
+        cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies) == cudaSuccess &&
+        cudaStreamBeginCaptureToGraph(body, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      iteration(body);
+      k_cr_cond<<<1, 32, 0, body>>>(scenes, nscenes, d_iter, 0, cond, 1);
+      cudaGraph_t out = nullptr;
+      cudaStreamEndCapture(body, &out);
+    }
+  } else {
+    k_cr_cond<<<1, 32, 0, st>>>(scenes, nscenes, d_iter, 1, cudaGraphConditionalHandle(), 0);
+    for (int k = 1; k <= max_iters && k <= kCrMaxIters; k++) {
+      iteration(st);
+      k_cr_cond<<<1, 32, 0, st>>>(scenes, nscenes, d_iter, 0, cudaGraphConditionalHandle(), 0);
+    }
   }
   k_cr_end<<<grid_ctas, 256, 0, st>>>(scenes, active_prefix, nscenes);
 }

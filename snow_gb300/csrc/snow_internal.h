@@ -154,13 +154,17 @@ void fast_volume(const SceneDev* sd_dev, int n, cudaStream_t st);
 void fast_g2p_advance(const SceneDev* scenes, const int* item_prefix, int nscenes, int grid_ctas, cudaStream_t st);
 void fast_g2p2g(const SceneDev* scenes, const int* item_prefix, int nscenes, int grid_ctas, cudaStream_t st);
 // The semi-implicit velocity solve between the grid update (which leaves
-// v*, m and u = v* in the solver planes) and G2P: max_iters iterations of
-// conjugate residuals (each a K u pass over the items and three passes over
-// the active nodes; a scene that has converged skips the rest), then the
+// v*, m and u = v* in the solver planes) and G2P: iterations of conjugate
+// residuals (each a K u pass over the items and three passes over the active
+// nodes) until every scene has converged or reached its cap, then the
 // colliders on v and v, d written back into gout. Scenes without a solver
-// record are left alone.
+// record are left alone. d_iter is a device int (the iteration counter).
+// When `st` is capturing a graph the iterations become a conditional WHILE
+// node whose body is captured on `body` (a stream not otherwise in use);
+// otherwise max_iters iterations are launched.
 void fast_implicit_solve(const SceneDev* scenes, const int* item_prefix, const int* active_prefix, int nscenes,
-                         int max_iters, int item_ctas, int grid_ctas, cudaStream_t st);
+                         int max_iters, int item_ctas, int grid_ctas, int* d_iter, cudaStream_t body,
+                         cudaStream_t st);
 // Kernel attributes of the solve (outside any stream capture).
 void fast_implicit_setup();
 

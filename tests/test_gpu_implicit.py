@@ -169,3 +169,27 @@ def test_engine_classes_drive_the_semi_implicit_update(ctx):
     sim = engine.integration.sim
     assert sim.stats()["nonfinite"] == 0
     assert sim.solver_report()["max_iters"] == 50
+
+
+@gpu
+def test_graph_loop_and_host_loop_agree(ctx):
+    """With graphs the iterations run as a conditional WHILE node that stops on
+    the device; without, the host launches every iteration up to the cap and
+    the finished ones return at once. Both give the same state and report."""
+    from snow_gb300 import api
+    s = _rough_scene(seed=15, n=3000, edge=32, tol=1e-6, iters=60)
+    s.v *= 0.3
+    out = []
+    for graphs in (True, False):
+        c = api.Context(0)
+        c.set_graphs(graphs)
+        sim = api.SimScene(c, s).upload().init().step(s.dt, 3)
+        out.append((sim.download(), sim.solver_report()))
+        sim.close()
+        c.close()
+    (a, ra), (b, rb) = out
+    assert ra["iterations"] == rb["iterations"] and 0 < ra["iterations"] < 60
+    assert abs(ra["residual"] - rb["residual"]) <= 1e-3 * rb["residual"] + 1e-12
+    assert np.abs(a["x"] - b["x"]).max() <= 1e-6
+    # FP64 atomics sum the dot products in a varying order: last-bit differences
+    assert np.abs(a["v"] - b["v"]).max() <= 1e-4 * max(1.0, np.abs(b["v"]).max())
