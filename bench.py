@@ -531,6 +531,91 @@ def bench_reference(args):
     return dict(value=value, unit=UNIT, cores=threads, kind=kind, sample=sample_desc, t_sample=t_sample)
 
 
+def bench_implicit(args, local_rank):
+    """The semi-implicit update (absent from the reference, whose
+    SemiImplicitTimeUpdate is empty) on the headline's geometry with a stiff
+    material, a long step and a rough velocity field (seeded 1 m/s jitter on
+    top of the +-5 m/s collision), where the CR solve iterates. The same scene
+    stepped explicitly is timed beside it. L2 flushed before every timed step."""
+    import torch
+
+    from snow_gb300 import api, scenes
+
+    torch.cuda.set_device(local_rank)
+    young, dt, jitter = 1.4e7, 5e-4, 1.0
+
+    def scene(beta):
+        s = scenes.cfg2_two_snowballs(n=args.particles, grid_edge=args.grid)
+        s.young, s.dt = young, dt
+        rng = np.random.default_rng(0x5EED0006)
+        s.v = (s.v + rng.normal(scale=jitter, size=s.v.shape)).astype(np.float32)
+        s.implicit_beta, s.implicit_tolerance, s.implicit_max_iters = beta, 1e-5, 50
+        return s
+
+    ctx = api.Context(local_rank)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local_rank}")
+    out = {}
+    for beta in (1.0, 0.0):
+        s = scene(beta)
+        sim = api.SimScene(ctx, s).upload().init().set_tuning(2, 256, 2)
+        for _ in range(args.warmup):
+            sim.step(dt, 1)
+        ctx.synchronize()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        with ClockSampler(local_rank) as clocks:
+            torch.cuda.synchronize()
+            for i in range(args.steps):
+                with torch.cuda.stream(stream):
+                    flush.zero_()
+                    starts[i].record(stream)
+                sim.step(dt, 1)
+                with torch.cuda.stream(stream):
+                    ends[i].record(stream)
+            torch.cuda.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends)) / args.steps
+        r = dict(ms_per_step=ms, value=s.n / (ms * 1e-3), clocks=clocks.summary())
+        if beta > 0:
+            # CR iterations of the steps that follow (per-kernel times of the
+            # solve: profiles/implicit_solve_two_snowballs_1M_256.md)
+            its = []
+            for _ in range(4):
+                sim.step(dt, 1)
+                rep = sim.solver_report()
+                its.append(rep["iterations"])
+            r.update(iterations=its, residual=rep["residual"], initial_residual=rep["initial_residual"])
+            # the same steps launched kernel by kernel (no graph): the host
+            # launches every CR iteration up to the cap, the finished ones
+            # return at once; this is also the pass in which a profiler sees
+            # the solve's kernels (a graph runs them inside a conditional node)
+            ctx.set_profiling(True)
+            sim.phase_times(reset=True)
+            sim.step(dt, 4)
+            ph = sim.phase_times(reset=True)
+            ctx.set_profiling(False)
+            r.update(eager_ms=ph["total_ms"] / ph["steps"])
+        st = sim.stats()
+        if st["nonfinite"]:
+            raise RuntimeError("non-finite particle state in the semi-implicit run")
+        out[beta] = r
+        sim.close()
+    ctx.close()
+    imp, exp = out[1.0], out[0.0]
+    return {"metric": METRIC, "value": imp["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": imp["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered lattice)",
+            "config": {"workload": f"semi-implicit update (beta 1, CR tolerance 1e-5, cap 50): two snowballs "
+                                   f"at +-5 m/s plus seeded {jitter} m/s velocity jitter, {args.particles} "
+                                   f"particles, {args.grid}^3 grid, E={young:g}, dt={dt:g}, FAST mode",
+                       "particles": args.particles, "grid": f"{args.grid}^3", "dt": dt,
+                       "l2": "flushed (256 MB write) before every timed step", "tuning": "2,256,2"},
+            "cr_iterations_per_step": imp["iterations"], "cr_residual": imp["residual"],
+            "cr_initial_residual": imp["initial_residual"], "eager_ms_per_step": imp["eager_ms"],
+            "explicit_same_scene": {"value": exp["value"], "ms_per_step": exp["ms_per_step"]},
+            "clocks": imp["clocks"]}
+
+
 def workload_config(args):
     return {"workload": f"two snowballs colliding head-on at +-5 m/s, {args.particles} particles (8 per cell), "
                         f"{args.grid}^3 grid, h=1/{args.grid}, dt=2e-5, FAST mode",
@@ -560,8 +645,9 @@ def main():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--serve-policy", default="srpt", choices=["fifo", "srpt"])
     ap.add_argument("--serve-cap", type=int, default=4 << 20, help="particles stepped together (0 = all)")
-    ap.add_argument("--workload", default="default", choices=["default", "batch16"],
-                    help="batch16: only the 16-scene batch at scale (2M-8M particles each), one JSON line")
+    ap.add_argument("--workload", default="default", choices=["default", "batch16", "implicit"],
+                    help="batch16: only the 16-scene batch at scale (2M-8M particles each); implicit: the "
+                         "semi-implicit update on the headline geometry; one JSON line each")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local_rank = rank_info()
@@ -578,6 +664,14 @@ def main():
                                  "sample": r["sample"]},
                 "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
+        return 0
+
+    if args.workload == "implicit":
+        if rank != 0:
+            return 0
+        if "--steps" not in sys.argv:
+            args.steps = 16
+        print(json.dumps(bench_implicit(args, local_rank)))
         return 0
 
     if args.workload == "batch16":
