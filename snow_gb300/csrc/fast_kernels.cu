@@ -375,28 +375,43 @@ __global__ void __launch_bounds__(256) k_stats(const SceneDev* __restrict__ sd, 
   float acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   StatsPartial t;
   stats_init(t);
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
-    const float4 xm = S.xm[p];
-    const float4 vv = S.vv[p];
-    const float jp = S.fc[p].y;
-    const float m = xm.w;
-    const bool ok = isfinite(xm.x) && isfinite(xm.y) && isfinite(xm.z) && isfinite(vv.x) && isfinite(vv.y) &&
-                    isfinite(vv.z) && isfinite(jp);
-    if (!ok) {
-      t.bad++;
-      continue;
+  // four particles per thread and pass, their loads issued together
+  constexpr int U = 4;
+  const int stride = gridDim.x * blockDim.x;
+  for (int p0 = blockIdx.x * blockDim.x + threadIdx.x; p0 < n; p0 += U * stride) {
+    float4 xm[U], vv[U];
+    float jp[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int p = p0 + u * stride;
+      if (p < n) {
+        xm[u] = S.xm[p];
+        vv[u] = S.vv[p];
+        jp[u] = S.fc[p].y;
+      }
     }
-    acc[0] += m;
-    acc[1] += m * vv.x;
-    acc[2] += m * vv.y;
-    acc[3] += m * vv.z;
-    acc[4] += 0.5f * m * (vv.x * vv.x + vv.y * vv.y + vv.z * vv.z);
-    acc[5] += m * xm.x;
-    acc[6] += m * xm.y;
-    acc[7] += m * xm.z;
-    acc[8] += jp;
-    t.bmin[0] = fminf(t.bmin[0], xm.x); t.bmin[1] = fminf(t.bmin[1], xm.y); t.bmin[2] = fminf(t.bmin[2], xm.z);
-    t.bmax[0] = fmaxf(t.bmax[0], xm.x); t.bmax[1] = fmaxf(t.bmax[1], xm.y); t.bmax[2] = fmaxf(t.bmax[2], xm.z);
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      if (p0 + u * stride >= n) break;
+      const float m = xm[u].w;
+      const bool ok = isfinite(xm[u].x) && isfinite(xm[u].y) && isfinite(xm[u].z) && isfinite(vv[u].x) &&
+                      isfinite(vv[u].y) && isfinite(vv[u].z) && isfinite(jp[u]);
+      if (!ok) {
+        t.bad++;
+        continue;
+      }
+      acc[0] += m;
+      acc[1] += m * vv[u].x;
+      acc[2] += m * vv[u].y;
+      acc[3] += m * vv[u].z;
+      acc[4] += 0.5f * m * (vv[u].x * vv[u].x + vv[u].y * vv[u].y + vv[u].z * vv[u].z);
+      acc[5] += m * xm[u].x;
+      acc[6] += m * xm[u].y;
+      acc[7] += m * xm[u].z;
+      acc[8] += jp[u];
+      t.bmin[0] = fminf(t.bmin[0], xm[u].x); t.bmin[1] = fminf(t.bmin[1], xm[u].y); t.bmin[2] = fminf(t.bmin[2], xm[u].z);
+      t.bmax[0] = fmaxf(t.bmax[0], xm[u].x); t.bmax[1] = fmaxf(t.bmax[1], xm[u].y); t.bmax[2] = fmaxf(t.bmax[2], xm[u].z);
+    }
   }
 #pragma unroll
   for (int k = 0; k < 9; k++) t.acc[k] = acc[k];
@@ -586,7 +601,7 @@ void fast_g2p2g(const SceneDev* scenes, const int* item_prefix, int nscenes, int
 void fast_stats(const SceneDev* sd_dev, int n, StatsAccum* out_dev, cudaStream_t st) {
   if (n <= 0) return;
   int g = (n + 255) / 256;
-  if (g > num_sms() * 2) g = num_sms() * 2;
+  if (g > num_sms() * 4) g = num_sms() * 4;
   k_stats<<<g, 256, 0, st>>>(sd_dev, n, out_dev);
 }
 
