@@ -370,7 +370,8 @@ __global__ void __launch_bounds__(kItemMax, 2) k_g2p2g(const SceneDev* __restric
 // Bulk statistics: per-thread sums in FP32 over a dozen particles, then FP64
 // across threads (FP64 arithmetic is slow on this part: the per-particle work
 // stays in FP32).
-__global__ void __launch_bounds__(256) k_stats(const SceneDev* __restrict__ sd, int n, StatsAccum* out) {
+__global__ void __launch_bounds__(256) k_stats(const SceneDev* __restrict__ sd, int n, StatsSlot* slot,
+                                               StatsAccum* host) {
   const SceneDev& S = *sd;
   float acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   StatsPartial t;
@@ -415,7 +416,7 @@ __global__ void __launch_bounds__(256) k_stats(const SceneDev* __restrict__ sd, 
   }
 #pragma unroll
   for (int k = 0; k < 9; k++) t.acc[k] = acc[k];
-  stats_commit(t, out);
+  stats_commit(t, slot, host);
 }
 
 // Upload: the caller's arrays (x, v: N x 3; m: N; FE, FP: N x 9 row-major or
@@ -598,12 +599,14 @@ void fast_g2p2g(const SceneDev* scenes, const int* item_prefix, int nscenes, int
   k_g2p2g<<<grid_ctas, kItemMax, item_smem(), st>>>(scenes, item_prefix, nscenes);
 }
 
-void fast_stats(const SceneDev* sd_dev, int n, StatsAccum* out_dev, cudaStream_t st) {
-  if (n <= 0) return;
-  int g = (n + 255) / 256;
-  if (g > num_sms() * 4) g = num_sms() * 4;
-  k_stats<<<g, 256, 0, st>>>(sd_dev, n, out_dev);
+void fast_stats(const SceneDev* sd_dev, int n, StatsSlot* slot, StatsAccum* host, cudaStream_t st) {
+  int g = (n + 255) / 256;  // at least one block: it publishes the empty sums
+  if (g > num_sms()) g = num_sms();  // one block per SM: measured fastest (fixed costs dominate)
+  if (g > kStatsMaxBlocks) g = kStatsMaxBlocks;
+  if (g < 1) g = 1;
+  k_stats<<<g, 256, 0, st>>>(sd_dev, n < 0 ? 0 : n, slot, host);
 }
+
 
 void fast_pack(const float* x, const float* v, const float* m, const float* FE, const float* FP, size_t n,
                const SceneDev& sd, cudaStream_t st) {

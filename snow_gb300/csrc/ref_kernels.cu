@@ -315,7 +315,7 @@ __global__ void __launch_bounds__(kThreads) k_advance(RefArgs a, float dt) {
   }
 }
 
-__global__ void __launch_bounds__(kThreads) k_stats(RefArgs a, StatsAccum* out) {
+__global__ void __launch_bounds__(kThreads) k_stats(RefArgs a, StatsSlot* slot, StatsAccum* host) {
   StatsPartial t;
   stats_init(t);
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += gridDim.x * blockDim.x) {
@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(kThreads) k_stats(RefArgs a, StatsAccum* out) 
     t.bmin[0] = fminf(t.bmin[0], xm.x); t.bmin[1] = fminf(t.bmin[1], xm.y); t.bmin[2] = fminf(t.bmin[2], xm.z);
     t.bmax[0] = fmaxf(t.bmax[0], xm.x); t.bmax[1] = fmaxf(t.bmax[1], xm.y); t.bmax[2] = fmaxf(t.bmax[2], xm.z);
   }
-  stats_commit(t, out);
+  stats_commit(t, slot, host);
 }
 
 int grid_for(long long n) {
@@ -372,8 +372,10 @@ void ref_grid(const RefArgs& a, float dt, cudaStream_t st) { k_grid<<<grid_for(a
 void ref_g2p(const RefArgs& a, cudaStream_t st) {
   if (a.n > 0) k_g2p<<<grid_for(a.n), kThreads, 0, st>>>(a);
 }
-void ref_stats(const RefArgs& a, StatsAccum* out_dev, cudaStream_t st) {
-  if (a.n > 0) k_stats<<<grid_for(a.n), kThreads, 0, st>>>(a, out_dev);
+void ref_stats(const RefArgs& a, StatsSlot* slot, StatsAccum* host, cudaStream_t st) {
+  // at least one block (it publishes empty sums), at most one partial per slot entry
+  const int g = a.n > 0 ? grid_for(a.n) : 1;
+  k_stats<<<g < kStatsMaxBlocks ? g : kStatsMaxBlocks, kThreads, 0, st>>>(a, slot, host);
 }
 void ref_advance(const RefArgs& a, float dt, cudaStream_t st) {
   if (a.n > 0) k_advance<<<grid_for(a.n), kThreads, 0, st>>>(a, dt);

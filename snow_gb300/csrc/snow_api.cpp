@@ -31,9 +31,12 @@ struct snow_ctx {
   // freed blocks for reuse (scenes of a serving loop come and go)
   cudaMemPool_t pool = nullptr;
   // statistics: slot 0 for snow_scene_stats, slots 1..SNOW_STATS_SLOTS for
-  // the queued reads; the pinned init record resets an accumulator
-  StatsAccum* d_stats = nullptr;   // 1 + SNOW_STATS_SLOTS accumulators
-  StatsAccum* h_stats = nullptr;   // pinned, 1 + SNOW_STATS_SLOTS + 1 (init)
+  // the queued reads. The kernel's last block writes the totals into h_stats
+  // (mapped pinned memory; d_hstats is its device address) and empties the
+  // device slot, so a read is one launch and an event, no copies.
+  StatsSlot* d_stats = nullptr;    // 1 + SNOW_STATS_SLOTS accumulators
+  StatsAccum* h_stats = nullptr;   // mapped pinned, 1 + SNOW_STATS_SLOTS
+  StatsAccum* d_hstats = nullptr;
   cudaEvent_t stat_ev[SNOW_STATS_SLOTS] = {};
   size_t stat_n[SNOW_STATS_SLOTS] = {};
   bool stat_pending[SNOW_STATS_SLOTS] = {};
@@ -557,16 +560,11 @@ snow_status snow_ctx_create(int device, size_t hbm_budget_bytes, snow_ctx** out)
     uint64_t keep = hbm_budget_bytes ? (uint64_t)hbm_budget_bytes : UINT64_MAX;
     e = cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep);
   }
-  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_stats, sizeof(StatsAccum) * (1 + SNOW_STATS_SLOTS));
-  if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_stats, sizeof(StatsAccum) * (2 + SNOW_STATS_SLOTS));
-  if (e == cudaSuccess) {
-    StatsAccum& init = ctx->h_stats[1 + SNOW_STATS_SLOTS];
-    std::memset(&init, 0, sizeof init);
-    for (int k = 0; k < 3; k++) {
-      init.bmin_key[k] = 0x7fffffff;
-      init.bmax_key[k] = (int)0x80000000;
-    }
-  }
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_stats, sizeof(StatsSlot) * (1 + SNOW_STATS_SLOTS));
+  if (e == cudaSuccess)
+    e = cudaHostAlloc(&ctx->h_stats, sizeof(StatsAccum) * (1 + SNOW_STATS_SLOTS), cudaHostAllocMapped);
+  if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&ctx->d_hstats, ctx->h_stats, 0);
+  if (e == cudaSuccess) e = cudaMemset(ctx->d_stats, 0, sizeof(StatsSlot) * (1 + SNOW_STATS_SLOTS));
   for (int i = 0; i < SNOW_STATS_SLOTS && e == cudaSuccess; i++)
     e = cudaEventCreateWithFlags(&ctx->stat_ev[i], cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_counters, kCounterStride * sizeof(int));
@@ -1166,14 +1164,11 @@ snow_status snow_scene_download_colliders(snow_scene* s, snow_collider* out) {
 
 static snow_status stats_enqueue(snow_scene* s, int k) {
   snow_ctx* ctx = s->ctx;
-  StatsAccum* d = ctx->d_stats + k;
-  CK(cudaMemcpyAsync(d, ctx->h_stats + 1 + SNOW_STATS_SLOTS, sizeof(StatsAccum), cudaMemcpyHostToDevice,
-                     ctx->stream));
   if (s->mode == SNOW_MODE_REFERENCE)
-    ref_stats(ref_args(s), d, ctx->stream);
+    ref_stats(ref_args(s), ctx->d_stats + k, ctx->d_hstats + k, ctx->stream);
   else
-    fast_stats(s->sd_dev, (int)s->n, d, ctx->stream);
-  CK(cudaMemcpyAsync(ctx->h_stats + k, d, sizeof(StatsAccum), cudaMemcpyDeviceToHost, ctx->stream));
+    fast_stats(s->sd_dev, (int)s->n, ctx->d_stats + k, ctx->d_hstats + k, ctx->stream);
+  CK(cudaGetLastError());
   return SNOW_OK;
 }
 

@@ -200,8 +200,24 @@ struct StatsAccum {
   int bmin_key[3], bmax_key[3];  // order-preserving int keys of the bbox floats
   unsigned long long nonfinite;
 };
-void fast_stats(const SceneDev* sd_dev, int n, StatsAccum* out_dev, cudaStream_t st);
-void ref_stats(const RefArgs& a, StatsAccum* out_dev, cudaStream_t st);
+// Per-block partial sums of one statistics read and the counter of blocks
+// that have written theirs. The kernel's last block sums the partials in
+// block order (the result does not depend on which block finished when),
+// writes the totals to `host` (mapped pinned memory, read after the stream
+// passes the kernel) and resets the counter, so a read needs no copy in
+// either direction.
+constexpr int kStatsMaxBlocks = 1024;
+struct StatsBlockSum {
+  double acc[9];  // mass, momentum x3, kinetic energy, mass-weighted position x3, sum J_p
+  float bmin[3], bmax[3];
+  unsigned long long bad;
+};
+struct StatsSlot {
+  StatsBlockSum part[kStatsMaxBlocks];
+  unsigned int done;
+};
+void fast_stats(const SceneDev* sd_dev, int n, StatsSlot* slot, StatsAccum* host, cudaStream_t st);
+void ref_stats(const RefArgs& a, StatsSlot* slot, StatsAccum* host, cudaStream_t st);
 void fast_download_grid(const SceneDev* sd_dev, float* mass, float* mom, float* force, float* vstar, cudaStream_t st);
 void fast_pack(const float* x, const float* v, const float* m, const float* FE, const float* FP, size_t n,
                const SceneDev& sd, cudaStream_t st);
