@@ -217,3 +217,23 @@ def test_tiny_scenes_step_in_both_modes(ctx, n):
         if n:
             assert np.all(np.isfinite(out["x"])) and out["x"][:, 1].max() < s.x[:, 1].max()  # falling
         sim.close()
+
+
+@gpu
+def test_statistics_do_not_depend_on_block_scheduling(ctx):
+    """The statistics kernel sums its per-block records in block order: reads
+    of the same state agree to the bit, and with a sum over the downloaded
+    particles in FP64."""
+    from snow_gb300 import api
+    s = scenes.small_scene(n=50000, grid_edge=48, seed=96, v0=(0.5, -1.5, 0.25))
+    sim = api.SimScene(ctx, s).upload().init().step(s.dt, 3)
+    a, b = sim.stats(), sim.stats()
+    for key in ("mass", "kinetic_energy", "mean_jp"):
+        assert a[key] == b[key]
+    assert np.array_equal(a["momentum"], b["momentum"]) and np.array_equal(a["bbox_min"], b["bbox_min"])
+    d = sim.download()
+    m = s.m.astype(np.float64)
+    assert abs(a["mass"] - m.sum()) <= 1e-6 * m.sum()
+    mom = (m[:, None] * d["v"].astype(np.float64)).sum(0)
+    assert np.abs(np.asarray(a["momentum"]) - mom).max() <= 1e-5 * np.abs(mom).max()
+    assert np.allclose(a["bbox_min"], d["x"].min(0)) and np.allclose(a["bbox_max"], d["x"].max(0))

@@ -131,3 +131,27 @@ def test_particle_cap_and_policy_order_the_jobs(policy):
         _close(_alone(long_job, 200), srv.fetch(a, long_job.n), tol=5e-4)
     finally:
         srv.close()
+
+
+@gpu
+def test_semi_implicit_jobs_serve_beside_explicit_ones():
+    """A semi-implicit job (the solve's conditional loop inside the batch
+    graph) and explicit jobs in one batch: each matches the same scene stepped
+    alone."""
+    from snow_gb300 import api
+    stiff = scenes.small_scene(n=4000, grid_edge=32, seed=205, v0=(0.0, -1.0, 0.0), young=1.4e7)
+    stiff.v = stiff.v + np.random.default_rng(7).normal(scale=0.2, size=stiff.v.shape).astype(np.float32)
+    stiff.dt = 5e-4
+    stiff.implicit_beta, stiff.implicit_tolerance, stiff.implicit_max_iters = 1.0, 1e-6, 40
+    jobs = [stiff, _jobs()[0], _jobs()[3]]
+    steps = [12, 9, 6]
+    srv = api.Server(0, chunk_steps=4)
+    try:
+        ids = [srv.submit(s, steps=k, keep_state=True) for s, k in zip(jobs, steps)]
+        srv.drain(120.0)
+        res = {r["id"]: r for r in srv.poll()}
+        for jid, s, k in zip(ids, jobs, steps):
+            assert res[jid]["status"] == 0 and res[jid]["stats"]["nonfinite"] == 0
+            _close(_alone(s, k), srv.fetch(jid, s.n), tol=2e-4)
+    finally:
+        srv.close()
