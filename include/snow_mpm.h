@@ -86,7 +86,10 @@ typedef struct snow_params {
   float alpha;            /* PIC/FLIP blend, 0.95 in the shaders  */
   float gravity[3];       /* (0, -9.81, 0) in gForceCompute.glsl  */
   int mode;               /* snow_mode                            */
-  int sort_interval;      /* FAST: re-bin particles every k steps (0 = library default) */
+  int sort_interval;      /* FAST: re-bin particles at least every k steps (0 = library
+                           * default). snow_scene_step re-bins every step while particles
+                           * leave their work items' tiles between binnings (fast particles,
+                           * long steps) and returns to k once they stay put */
   /* Semi-implicit velocity update (the reference's SemiImplicitTimeUpdate,
    * an empty stub in semiimplicittimeupdate.cpp:3-5; Stomakhin et al. 2013,
    * eq. 9): with implicit_beta > 0 each step solves
@@ -352,7 +355,7 @@ snow_status snow_scene_set_tuning(snow_scene* s, const snow_tuning* t);
 /* Applies a tuning to every scene of the batch (e.g. one kept from an
  * earlier autotune); takes effect at each scene's next re-binning. */
 snow_status snow_batch_set_tuning(snow_batch* b, const snow_tuning* t);
-/* Times candidate tunings (sort interval 4/8/12/16 x 128/256 particles per work
+/* Times candidate tunings (sort interval 1/2/4/8/12/16 x 128/256 particles per work
  * item x 1/2 CTAs per SM) on real steps of the batch and keeps the fastest.
  * The steps advance the scenes like snow_batch_step (out->steps_taken says
  * how many); dt as for snow_batch_step. */

@@ -522,34 +522,16 @@ void fast_implicit_solve(const SceneDev* scenes, const int* item_prefix, const i
   };
   k_hess<<<item_ctas, kItemMax, smem, st>>>(scenes, item_prefix, nscenes, nullptr);
   k_cr_begin<<<grid_ctas, 256, 0, st>>>(scenes, active_prefix, nscenes);
-  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-  cudaGraph_t g = nullptr;
-  cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, nullptr, nullptr, nullptr);
-  if (cs == cudaStreamCaptureStatusActive) {
-    // conditional WHILE node in the graph being captured; its body is
-    // captured from a second stream into the node's own graph. Errors of
-    // these calls invalidate the capture and surface at its end.
-    cudaGraphConditionalHandle cond;
-    cudaGraphConditionalHandleCreate(&cond, g, 0, cudaGraphCondAssignDefault);
+  cudaGraphConditionalHandle cond;
+  if (capture_handle(st, &cond)) {
+    // a conditional WHILE node in the graph being captured (its body is
+    // captured from the second stream); errors invalidate the capture and
+    // surface at its end
     k_cr_cond<<<1, 32, 0, st>>>(scenes, nscenes, d_iter, 1, cond, 1);
-    const cudaGraphNode_t* deps = nullptr;
-    size_t ndeps = 0;
-    cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &ndeps);
-    cudaGraphNodeParams p = {};
-    p.type = cudaGraphNodeTypeConditional;
-    p.conditional.handle = cond;
-    p.conditional.type = cudaGraphCondTypeWhile;
-    p.conditional.size = 1;
-    cudaGraphNode_t node;
-    if (cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &p) == cudaSuccess &&
-        cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies) == cudaSuccess &&
-        cudaStreamBeginCaptureToGraph(body, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
-                                      cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-      iteration(body);
-      k_cr_cond<<<1, 32, 0, body>>>(scenes, nscenes, d_iter, 0, cond, 1);
-      cudaGraph_t out = nullptr;
-      cudaStreamEndCapture(body, &out);
-    }
+    capture_conditional(st, cond, cudaGraphCondTypeWhile, body, [&](cudaStream_t b) {
+      iteration(b);
+      k_cr_cond<<<1, 32, 0, b>>>(scenes, nscenes, d_iter, 0, cond, 1);
+    });
   } else {
     k_cr_cond<<<1, 32, 0, st>>>(scenes, nscenes, d_iter, 1, cudaGraphConditionalHandle(), 0);
     for (int k = 1; k <= max_iters && k <= kCrMaxIters; k++) {

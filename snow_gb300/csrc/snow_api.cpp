@@ -81,12 +81,24 @@ struct snow_scene {
   int key_bits = 0;
   int* d_prefix = nullptr;  // [0,2) items, [2,4) active, [6,8) blocks
   int steps_since_sort = 1 << 30;
+  // re-binning interval in use (1 .. tune.sort_interval): dropped to 1 when
+  // particles leave their work items' tiles between binnings, doubled back
+  // after a run of clean checks
+  int bin_interval = 8;
+  int clean_checks = 0;
+  // the device counters as copied (without a wait) at the last binning point
+  // and read at the next one
+  int* h_cnt = nullptr;
+  cudaEvent_t cnt_ev = nullptr;
+  bool cnt_pending = false;
+  long long fallbacks_seen = 0;
+  int steps_at_snapshot = 0;  // steps between the last two snapshots
   int version = 0;
   bool volume_given = false;
   // FAST: acc holds the P2G sums of the current particle state (the next
   // step's grid update consumes them)
   bool p2g_ready = false;
-  // graphs of one step, keyed by (dt, with sort)
+  // graphs of one step, keyed by (dt, with binning)
   cudaGraphExec_t g_plain = nullptr, g_sort = nullptr;
   float g_dt = NAN;
   snow_phase_times times{};
@@ -367,25 +379,65 @@ snow_status set_dt(snow_scene* s, float dt) {
   return SNOW_OK;
 }
 
-// Checks device-side error counters; grows the output pool when it runs full.
-snow_status fast_check(snow_scene* s) {
+// Checks a copy of the device-side counters: errors, the output pool's fill
+// (grown when it runs three quarters full).
+snow_status check_counters(snow_scene* s, const int* h) {
   snow_ctx* ctx = s->ctx;
-  CK(cudaMemcpyAsync(ctx->h_counters, s->sd.counters, kCounterStride * sizeof(int), cudaMemcpyDeviceToHost,
-                     ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
-  const int active = ctx->h_counters[CNT_ACTIVE];
-  const int overflow = ctx->h_counters[CNT_OVERFLOW];
-  const int nonfinite = ctx->h_counters[CNT_NONFINITE];
-  if (ctx->h_counters[CNT_TIMEOUT] > 0) return fail(ctx, SNOW_ETIMEDOUT, "a bounded device wait ran out");
-  if (overflow > 0) return fail(ctx, SNOW_ECAPACITY, "grid block pool overflowed");
-  if (nonfinite > 0) return fail(ctx, SNOW_ENUMERIC, "non-finite particle state");
+  if (h[CNT_TIMEOUT] > 0) return fail(ctx, SNOW_ETIMEDOUT, "a bounded device wait ran out");
+  if (h[CNT_OVERFLOW] > 0) return fail(ctx, SNOW_ECAPACITY, "grid block pool overflowed");
+  if (h[CNT_NONFINITE] > 0) return fail(ctx, SNOW_ENUMERIC, "non-finite particle state");
+  const int active = h[CNT_ACTIVE];
   if (active > (s->sd.pool_cap * 3) / 4 && s->sd.pool_cap < s->sd.nblocks) {
+    // the old pool is freed in stream order, after the queued steps that use it
     const int want = std::min(s->sd.nblocks, std::max(2 * active, s->sd.pool_cap + 1024));
     snow_status st = fast_alloc_pool(s, want);
     if (st) return st;
     return push_sd(s);
   }
   return SNOW_OK;
+}
+
+// At a binning point of snow_scene_step: checks the counters copied at the
+// previous binning point (that copy has long landed, so there is no wait for
+// the queued steps), adapts the re-binning interval to the share of
+// particle-steps that left their work item's tile since then (above 1/256:
+// re-bin every step; below 1/4096 eight times in a row: double the interval,
+// up to the tuned one), and copies the counters again for the next point.
+snow_status fast_check_async(snow_scene* s, int steps_since_last) {
+  snow_ctx* ctx = s->ctx;
+  if (s->cnt_pending) {
+    CK(cudaEventSynchronize(s->cnt_ev));
+    s->cnt_pending = false;
+    const int* h = s->h_cnt;
+    const long long fb = (long long)(unsigned)h[CNT_FALLBACK];
+    const long long delta = fb - s->fallbacks_seen;
+    s->fallbacks_seen = fb;
+    const double work = (double)s->steps_at_snapshot * (double)std::max<size_t>(s->n, 1);
+    if (s->steps_at_snapshot > 0 && delta > work / 256.0) {
+      s->bin_interval = 1;
+      s->clean_checks = 0;
+    } else if (delta <= work / 4096.0 && ++s->clean_checks >= 8) {
+      s->bin_interval = std::min(s->tune.sort_interval, 2 * s->bin_interval);
+      s->clean_checks = 0;
+    }
+    snow_status r = check_counters(s, h);
+    if (r) return r;
+  }
+  CK(cudaMemcpyAsync(s->h_cnt, s->sd.counters, kCounterStride * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaEventRecord(s->cnt_ev, ctx->stream));
+  s->cnt_pending = true;
+  s->steps_at_snapshot = steps_since_last;
+  return SNOW_OK;
+}
+
+// Checks device-side error counters now (waits for the stream); grows the
+// output pool when it runs full.
+snow_status fast_check(snow_scene* s) {
+  snow_ctx* ctx = s->ctx;
+  CK(cudaMemcpyAsync(ctx->h_counters, s->sd.counters, kCounterStride * sizeof(int), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return check_counters(s, ctx->h_counters);
 }
 
 // ExplicitTimeUpdate::init (explicittimeupdate.cpp:29-33) -- grid mass and
@@ -671,11 +723,17 @@ snow_status snow_scene_create(snow_ctx* ctx, const snow_params* p, const snow_co
   s->coll_h.assign(colliders, colliders + n_colliders);
   s->ncoll = n_colliders;
   if (p->sort_interval > 0) s->tune.sort_interval = p->sort_interval;
+  s->bin_interval = s->tune.sort_interval;
   snow_status st = SNOW_OK;
   if (n_colliders > 0) st = salloc(s, (size_t)n_colliders, &s->coll_d);
   if (!st && n_colliders > 0)
     if (cudaMemcpy(s->coll_d, colliders, sizeof(snow_collider) * n_colliders, cudaMemcpyHostToDevice) != cudaSuccess)
       st = cuda_fail(ctx, cudaGetLastError(), "collider upload");
+  if (!st && s->mode == SNOW_MODE_FAST) {
+    if (cudaMallocHost(&s->h_cnt, kCounterStride * sizeof(int)) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->cnt_ev, cudaEventDisableTiming) != cudaSuccess)
+      st = cuda_fail(ctx, cudaGetLastError(), "counter snapshot");
+  }
   if (!st && s->mode == SNOW_MODE_FAST) {
     fill_sd_params(s);
     s->sd.dt = 1e-3f;
@@ -703,6 +761,8 @@ void snow_scene_destroy(snow_scene* s) {
   for (snow_batch* b : holders) snow_batch_destroy(b);
   drop_graphs(s);
   dfree_all(ctx, s->allocs, s->bytes);
+  if (s->h_cnt) cudaFreeHost(s->h_cnt);
+  if (s->cnt_ev) cudaEventDestroy(s->cnt_ev);
   ctx->scenes.erase(s);
   delete s;
 }
@@ -906,7 +966,7 @@ snow_status snow_dispatch(snow_scene* s, int kernel, double dt) {
         fast_enqueue_compact(s, st);
         fast_enqueue_grid(s, true, st);
       }
-      if (s->steps_since_sort >= s->tune.sort_interval) {
+      if (s->steps_since_sort >= s->bin_interval) {
         fast_bin(s, st);
         s->steps_since_sort = 0;
       }
@@ -964,10 +1024,10 @@ snow_status snow_scene_step(snow_scene* s, double dt, int n_steps) {
     s->p2g_ready = true;
   }
   for (int i = 0; i < n_steps; i++) {
-    const bool bin = s->steps_since_sort >= s->tune.sort_interval;
+    const bool bin = s->steps_since_sort >= s->bin_interval;
     if (bin) {
       // binning points are where the host looks at the device counters
-      r = fast_check(s);
+      r = fast_check_async(s, std::min(s->steps_since_sort, 1 << 20));
       if (r) return r;
     }
     if (ctx->profiling) {
@@ -1449,6 +1509,7 @@ snow_status snow_scene_set_tuning(snow_scene* s, const snow_tuning* t) {
   s->tune.sort_interval = t->sort_interval;
   s->tune.items_max = t->items_max;
   s->tune.ctas_per_sm = t->ctas_per_sm;
+  s->bin_interval = t->sort_interval;
   drop_graphs(s);
   return SNOW_OK;
 }
@@ -1461,6 +1522,7 @@ snow_status snow_batch_set_tuning(snow_batch* b, const snow_tuning* t) {
     s->tune.sort_interval = t->sort_interval;
     s->tune.items_max = t->items_max;
     s->tune.ctas_per_sm = t->ctas_per_sm;
+    s->bin_interval = t->sort_interval;
     drop_graphs(s);
   }
   for (auto& g : b->graphs) cudaGraphExecDestroy(g.second);
@@ -1476,7 +1538,7 @@ snow_status snow_batch_set_tuning(snow_batch* b, const snow_tuning* t) {
 snow_status snow_batch_autotune(snow_batch* b, const double* dt, snow_tuning* out) {
   if (!b) return SNOW_EINVAL;
   snow_ctx* ctx = b->ctx;
-  static const int kIntervals[] = {4, 8, 12, 16};
+  static const int kIntervals[] = {1, 2, 4, 8, 12, 16};  // 1, 2: particles that cross cells in a step or two
   static const int kItems[] = {128, 256};
   static const int kCtas[] = {1, 2};
   snow_tuning best{};

@@ -135,7 +135,6 @@ constexpr int kMinItemMax = 64;
 // (P2G work items, active blocks, grid blocks). Item and active-block counts
 // are only known on the device; fast_prefix() forms both prefixes there.
 void fast_prefix(const SceneDev* scenes, int nscenes, int* items_prefix, int* active_prefix, cudaStream_t st);
-// Zeroes the per-step counters (active blocks, overflow) of every scene.
 // Start of a step: resets the per-step counters and, with `rigid`, moves the
 // colliders by dt * velocity (rigidAdvance.glsl:14-18).
 void fast_begin_step(const SceneDev* scenes, int nscenes, bool rigid, cudaStream_t st);
@@ -167,6 +166,46 @@ void fast_implicit_solve(const SceneDev* scenes, const int* item_prefix, const i
                          cudaStream_t st);
 // Kernel attributes of the solve (outside any stream capture).
 void fast_implicit_setup();
+
+// While `st` captures a graph: appends a conditional node (IF or WHILE) on
+// `cond` after the work captured so far, and captures `fill`'s launches on
+// `body` (a stream not otherwise capturing) as the node's body. Returns
+// false when `st` is not capturing or a call failed (a failure also
+// invalidates the capture, which then fails at its end).
+template <class Fill>
+bool capture_conditional(cudaStream_t st, cudaGraphConditionalHandle cond, cudaGraphConditionalNodeType type,
+                         cudaStream_t body, Fill fill) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t ndeps = 0;
+  if (cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &ndeps) != cudaSuccess ||
+      cs != cudaStreamCaptureStatusActive)
+    return false;
+  cudaGraphNodeParams p = {};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = cond;
+  p.conditional.type = type;
+  p.conditional.size = 1;
+  cudaGraphNode_t node;
+  if (cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &p) != cudaSuccess ||
+      cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies) != cudaSuccess ||
+      cudaStreamBeginCaptureToGraph(body, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                    cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+    return false;
+  fill(body);
+  cudaGraph_t out = nullptr;
+  return cudaStreamEndCapture(body, &out) == cudaSuccess;
+}
+// A conditional handle on the graph `st` is capturing (false if none).
+inline bool capture_handle(cudaStream_t st, cudaGraphConditionalHandle* cond) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaGraph_t g = nullptr;
+  if (cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, nullptr, nullptr, nullptr) != cudaSuccess ||
+      cs != cudaStreamCaptureStatusActive)
+    return false;
+  return cudaGraphConditionalHandleCreate(cond, g, 0, cudaGraphCondAssignDefault) == cudaSuccess;
+}
 
 // Binning of one scene (host-side sizes known): keys -> radix sort ->
 // permutation of the particle streams -> P2G work items.
