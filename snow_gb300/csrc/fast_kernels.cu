@@ -69,6 +69,12 @@ __global__ void k_begin_step(const SceneDev* __restrict__ scenes, int nscenes, i
   }
 }
 
+__global__ void k_gather_counters(const SceneDev* __restrict__ scenes, int nscenes, int* out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nscenes * kCounterStride; i += gridDim.x * blockDim.x)
+    out[i] = scenes[i / kCounterStride].counters[i % kCounterStride];
+  __threadfence_system();
+}
+
 __global__ void k_count_flags(const SceneDev* __restrict__ sd, int nblocks) {
   int c = 0;
   for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nblocks; b += gridDim.x * blockDim.x)
@@ -554,6 +560,11 @@ void fast_prefix(const SceneDev* scenes, int nscenes, int* items_prefix, int* ac
 
 void fast_begin_step(const SceneDev* scenes, int nscenes, bool rigid, cudaStream_t st) {
   if (nscenes > 0) k_begin_step<<<nscenes, 32, 0, st>>>(scenes, nscenes, rigid ? 1 : 0);
+}
+
+void fast_gather_counters(const SceneDev* scenes, int nscenes, int* out, cudaStream_t st) {
+  const int n = nscenes * kCounterStride;
+  k_gather_counters<<<(n + 255) / 256, 256, 0, st>>>(scenes, nscenes, out);
 }
 
 void fast_count_flags(const SceneDev* sd_dev, int nblocks, cudaStream_t st) {

@@ -118,6 +118,12 @@ struct snow_batch {
   int g_threads = 0;
   size_t bytes = 0;
   std::vector<std::pair<void*, size_t>> allocs;
+  // every scene's counters, written by a kernel into mapped pinned memory at
+  // one checking point and read at the next
+  int* h_cnt = nullptr;
+  int* d_hcnt = nullptr;
+  cudaEvent_t cnt_ev = nullptr;
+  bool cnt_pending = false;
 };
 
 // ---------------------------------------------------------------------------
@@ -1350,6 +1356,13 @@ snow_status snow_batch_create(snow_ctx* ctx, snow_scene* const* scenes, int n, s
     snow_batch_destroy(b);
     return st;
   }
+  if (cudaHostAlloc(&b->h_cnt, sizeof(int) * kCounterStride * n, cudaHostAllocMapped) != cudaSuccess ||
+      cudaHostGetDevicePointer((void**)&b->d_hcnt, b->h_cnt, 0) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->cnt_ev, cudaEventDisableTiming) != cudaSuccess) {
+    st = cuda_fail(ctx, cudaGetLastError(), "batch counter snapshot");
+    snow_batch_destroy(b);
+    return st;
+  }
   ctx->batches.insert(b);
   *out = b;
   return SNOW_OK;
@@ -1360,6 +1373,8 @@ void snow_batch_destroy(snow_batch* b) {
   cudaStreamSynchronize(b->ctx->stream);
   for (auto& g : b->graphs) cudaGraphExecDestroy(g.second);
   dfree_all(b->ctx, b->allocs, b->bytes);
+  if (b->h_cnt) cudaFreeHost(b->h_cnt);
+  if (b->cnt_ev) cudaEventDestroy(b->cnt_ev);
   b->ctx->batches.erase(b);
   delete b;
 }
@@ -1470,10 +1485,19 @@ snow_status snow_batch_step(snow_batch* b, const double* dt, int n_steps) {
   for (int i = 0; i < n_steps; i++) {
     const int phase = b->step_count % interval;
     if (phase == 0 && b->step_count > 0) {
-      for (snow_scene* s : b->scenes) {
-        r = fast_check(s);
-        if (r) return r;
+      // the counters gathered at the previous checking point (long landed:
+      // no wait for the queued steps), then a new gather for the next one
+      if (b->cnt_pending) {
+        CK(cudaEventSynchronize(b->cnt_ev));
+        b->cnt_pending = false;
+        for (size_t k = 0; k < b->scenes.size(); k++) {
+          r = check_counters(b->scenes[k], b->h_cnt + k * kCounterStride);
+          if (r) return r;
+        }
       }
+      fast_gather_counters(b->d_scenes, (int)b->scenes.size(), b->d_hcnt, st);
+      CK(cudaEventRecord(b->cnt_ev, st));
+      b->cnt_pending = true;
       r = batch_refresh(b, dt);
       if (r) return r;
     }

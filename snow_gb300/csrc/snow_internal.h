@@ -138,6 +138,10 @@ void fast_prefix(const SceneDev* scenes, int nscenes, int* items_prefix, int* ac
 // Start of a step: resets the per-step counters and, with `rigid`, moves the
 // colliders by dt * velocity (rigidAdvance.glsl:14-18).
 void fast_begin_step(const SceneDev* scenes, int nscenes, bool rigid, cudaStream_t st);
+// Copies every scene's counters into out[s * kCounterStride ...] (mapped
+// pinned memory: a batch reads them one re-binning interval later, without
+// draining the stream).
+void fast_gather_counters(const SceneDev* scenes, int nscenes, int* out, cudaStream_t st);
 // Counts flagged blocks of one scene into counters[CNT_ACTIVE] (pool sizing).
 void fast_count_flags(const SceneDev* sd_dev, int nblocks, cudaStream_t st);
 // Flags -> active list and pool slots; its last CTA then forms the item and
