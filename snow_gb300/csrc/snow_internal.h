@@ -235,7 +235,7 @@ void fast_apply_bins(const SceneDev& sd, const SceneDev* sd_dev, BinScratch& b, 
 
 // Radix sort of arbitrary (key, value) pairs; the result lands in k[0]/v[0].
 void radix_sort_pairs(uint32_t* k[2], uint32_t* v[2], size_t n, int key_bits, uint32_t* hist, uint32_t* scan_tmp,
-                      cudaStream_t st);
+                      cudaStream_t st, int start = 0);  // start: the buffer holding the input
 
 // Bulk statistics of one scene.
 struct StatsAccum {

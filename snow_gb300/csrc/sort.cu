@@ -283,11 +283,11 @@ int grid_for(size_t n, int threads, int per_sm) {
 size_t radix_tiles(size_t n) { return (n + kRsTile - 1) / kRsTile; }
 
 void radix_sort_pairs(uint32_t* k[2], uint32_t* v[2], size_t n, int key_bits, uint32_t* hist, uint32_t* scan_tmp,
-                      cudaStream_t st) {
+                      cudaStream_t st, int start) {
   if (n == 0) return;
   const int ntiles = (int)radix_tiles(n);
   const int passes = (key_bits + 7) / 8;
-  int cur = 0;
+  int cur = start;
   const int g = grid_for((size_t)ntiles * kRsThreads, kRsThreads, 8);
   for (int pass = 0; pass < passes; pass++) {
     const int shift = 8 * pass;
@@ -304,8 +304,11 @@ void radix_sort_pairs(uint32_t* k[2], uint32_t* v[2], size_t n, int key_bits, ui
 
 void fast_sort_keys(const SceneDev& sd, const SceneDev* sd_dev, BinScratch& b, int key_bits, cudaStream_t st) {
   if (sd.n <= 0) return;
-  k_keys<<<grid_for(sd.n, 256, 8), 256, 0, st>>>(sd_dev, b.keys[0], b.vals[0]);
-  radix_sort_pairs(b.keys, b.vals, (size_t)sd.n, key_bits, b.hist, b.scan_tmp, st);
+  // an odd number of passes starts from the second buffer so that the
+  // result lands in the first without a copy
+  const int start = ((key_bits + 7) / 8) & 1;
+  k_keys<<<grid_for(sd.n, 256, 8), 256, 0, st>>>(sd_dev, b.keys[start], b.vals[start]);
+  radix_sort_pairs(b.keys, b.vals, (size_t)sd.n, key_bits, b.hist, b.scan_tmp, st, start);
 }
 
 void fast_apply_bins(const SceneDev& sd, const SceneDev* sd_dev, BinScratch& b, int items_max, cudaStream_t st) {
