@@ -123,8 +123,7 @@ __device__ __forceinline__ void stats_commit(StatsPartial& t, StatsSlot* slot, S
     r.ke = b.acc[4];
     r.jp = b.acc[8];
     r.nonfinite = b.bad;
-    *host = r;
-    __threadfence_system();
+    *host = r;  // visible to the host once it has waited for the kernel
     slot->done = 0u;
   }
 }
