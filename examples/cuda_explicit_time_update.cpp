@@ -6,13 +6,18 @@
 // fill snow_params / snow_collider from its PhysicalScene; here a snowball
 // in the reference's default world (defines.hpp) stands in for the scene.
 //
+// CudaSemiImplicitTimeUpdate does the same for the reference's
+// SemiImplicitTimeUpdate (semiimplicittimeupdate.hpp:6-12, empty there): the
+// scene's parameters ask for the semi-implicit velocity update.
+//
 //   g++ -std=c++17 -I include examples/cuda_explicit_time_update.cpp \
 //       -L snow_gb300/_build -lsnow_gb300 -Wl,-rpath,snow_gb300/_build -o explicit_step
-//   ./explicit_step [steps]
+//   ./explicit_step [steps] [--semi-implicit]
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <random>
+#include <string>
 #include <vector>
 
 #include "snow_mpm.h"
@@ -28,7 +33,7 @@ struct PhysicalScene {  // what the reference's PhysicalScene carries for the st
 class CudaExplicitTimeUpdate {
  public:
   explicit CudaExplicitTimeUpdate(PhysicalScene&& s) : scene_(std::move(s)) {}
-  ~CudaExplicitTimeUpdate() {
+  virtual ~CudaExplicitTimeUpdate() {
     snow_scene_destroy(sim_);
     snow_ctx_destroy(ctx_);
   }
@@ -51,7 +56,7 @@ class CudaExplicitTimeUpdate {
 
   bool stats(snow_stats* out) { return snow_scene_stats(sim_, out) == SNOW_OK || fail("snow_scene_stats"); }
 
- private:
+ protected:
   bool fail(const char* what) {
     std::fprintf(stderr, "%s failed: %s\n", what, ctx_ ? snow_last_error(ctx_) : "no context");
     return false;
@@ -59,6 +64,25 @@ class CudaExplicitTimeUpdate {
   PhysicalScene scene_;
   snow_ctx* ctx_ = nullptr;
   snow_scene* sim_ = nullptr;
+};
+
+// SemiImplicitTimeUpdate: each update solves (M + beta dt^2 K) v = M v* on
+// the grid (conjugate residuals) before G2P.
+class CudaSemiImplicitTimeUpdate : public CudaExplicitTimeUpdate {
+ public:
+  explicit CudaSemiImplicitTimeUpdate(PhysicalScene&& s, float beta = 1.0f)
+      : CudaExplicitTimeUpdate(with_beta(std::move(s), beta)) {}
+  bool report(snow_solver_report* out) {
+    return snow_scene_solver_report(sim_, out) == SNOW_OK || fail("snow_scene_solver_report");
+  }
+
+ private:
+  static PhysicalScene with_beta(PhysicalScene&& s, float beta) {
+    s.params.implicit_beta = beta;
+    s.params.implicit_tolerance = 1e-5f;
+    s.params.implicit_max_iters = 50;
+    return std::move(s);
+  }
 };
 
 // A snowball of radius 0.3 m above the ground of the default world, seeded
@@ -97,16 +121,27 @@ PhysicalScene snowball() {
 
 int main(int argc, char** argv) {
   const int steps = argc > 1 ? std::atoi(argv[1]) : 100;
+  const bool semi = argc > 2 && std::string(argv[2]) == "--semi-implicit";
   PhysicalScene scene = snowball();
   const size_t n = scene.m.size();
-  CudaExplicitTimeUpdate integration(std::move(scene));  // MPMPhysicEngine's member
-  if (!integration.init()) return 1;
+  // MPMPhysicEngine's member
+  CudaSemiImplicitTimeUpdate* si = semi ? new CudaSemiImplicitTimeUpdate(std::move(scene)) : nullptr;
+  CudaExplicitTimeUpdate* integration = si ? si : new CudaExplicitTimeUpdate(std::move(scene));
+  int rc = 0;
   snow_stats before{}, after{};
-  if (!integration.stats(&before)) return 1;
-  for (int i = 0; i < steps; i++)
-    if (!integration.update(1e-3)) return 1;
-  if (!integration.stats(&after)) return 1;
-  std::printf("particles %zu steps %d centre of mass y %.6f -> %.6f nonfinite %llu\n", n, steps,
-              before.center_of_mass[1], after.center_of_mass[1], (unsigned long long)after.nonfinite);
-  return after.nonfinite == 0 && after.center_of_mass[1] < before.center_of_mass[1] ? 0 : 2;
+  if (!integration->init() || !integration->stats(&before)) rc = 1;
+  for (int i = 0; i < steps && rc == 0; i++)
+    if (!integration->update(1e-3)) rc = 1;
+  if (rc == 0 && !integration->stats(&after)) rc = 1;
+  if (rc == 0) {
+    std::printf("%s particles %zu steps %d centre of mass y %.6f -> %.6f nonfinite %llu\n",
+                semi ? "semi-implicit" : "explicit", n, steps, before.center_of_mass[1], after.center_of_mass[1],
+                (unsigned long long)after.nonfinite);
+    snow_solver_report rep{};
+    if (si && si->report(&rep))
+      std::printf("last solve: %d iterations, residual %.3g\n", rep.iterations, rep.residual);
+    rc = after.nonfinite == 0 && after.center_of_mass[1] < before.center_of_mass[1] ? 0 : 2;
+  }
+  delete integration;
+  return rc;
 }

@@ -28,7 +28,11 @@ def test_example_compiles_and_links(tmp_path):
 
 
 @pytest.mark.gpu
-def test_example_runs_the_default_world(tmp_path):
-    out = subprocess.run([_build(tmp_path), "100"], capture_output=True, text=True, timeout=300)
+@pytest.mark.parametrize("mode", ["", "--semi-implicit"])
+def test_example_runs_the_default_world(tmp_path, mode):
+    out = subprocess.run([_build(tmp_path), "100"] + ([mode] if mode else []), capture_output=True, text=True,
+                         timeout=300)
     assert out.returncode == 0, out.stdout + out.stderr
     assert "nonfinite 0" in out.stdout
+    if mode:
+        assert "semi-implicit" in out.stdout and "last solve" in out.stdout
