@@ -132,6 +132,25 @@ def test_fast_single_step_from_rest_within_1e5(ctx, seed, n, edge, v0):
     assert max(e["x"], e["v"], e["FE"], e["Jp"]) <= REL_TOL, e
 
 
+@gpu
+def test_fast_single_step_with_sphere_and_moving_colliders_within_1e5(ctx):
+    """Grid and particle collider projection (gForceCompute.glsl:72-93,
+    particleAdvance.glsl:182-204) for a sphere (type 1) inside the snowball
+    and a moving half-plane under it, after the rigid advance of both
+    (rigidAdvance.glsl:14-18), against the FP64 oracle."""
+    from snow_gb300 import native as N
+    s = scenes.small_scene(n=5000, grid_edge=32, seed=34, v0=(0.5, -3.0, 0.2), center=(0.5, 0.3, 0.5))
+    s.colliders.append(scenes.Collider(pos=(0.52, 0.28, 0.49), type=1, radius=0.06, vel=(0.0, 0.5, 0.0),
+                                       friction=0.3))
+    s.colliders.append(scenes.Collider(pos=(0.0, 0.2, 0.0), type=0, normal=(0.0, 1.0, 0.0), vel=(0.0, 1.0, 0.0),
+                                       friction=0.1))
+    g = sim(ctx, s, N.MODE_FAST).upload().init().step(s.dt, 1)
+    o = _exact_oracle(s).upload().init().step()
+    e = field_errors(g.download(), o.state())
+    assert max(e["x"], e["v"], e["FE"], e["Jp"]) <= REL_TOL, e
+    assert np.abs(g.colliders() - o.colliders()).max() <= 1e-6
+
+
 def _deformed_restart(ctx, warm_steps, seed=41):
     """The FP64 oracle advanced `warm_steps` through an impact on the floor,
     then both the oracle and a FAST GPU scene restarted from its state
