@@ -182,8 +182,13 @@ snow_status snow_scene_set_volume(snow_scene* s, const float* volume, size_t n);
 /* ExplicitTimeUpdate::init: grid reset, grid mass, particle density. */
 snow_status snow_scene_init(snow_scene* s);
 /* n_steps x ExplicitTimeUpdate::update(dt). Asynchronous: returns once the
- * work is queued; errors found on the device surface at the next call that
- * synchronises (download, stats, snow_ctx_synchronize). */
+ * work is queued. Conditions counted on the device (non-finite particles:
+ * SNOW_ENUMERIC, grid block pool overflow: SNOW_ECAPACITY, an expired
+ * bounded wait: SNOW_ETIMEDOUT) are returned by a later step call, at the
+ * second re-binning point after they occurred (the counters are read there
+ * without waiting for the queued steps); snow_scene_stats counts non-finite
+ * particles at once. CUDA errors surface at the next call that synchronises
+ * (download, stats, snow_ctx_synchronize). */
 snow_status snow_scene_step(snow_scene* s, double dt, int n_steps);
 /* One kernel of the step (per-kernel parity checks). In SNOW_MODE_FAST the
  * gather and the particle update are one kernel: SNOW_K_G2P runs both and
