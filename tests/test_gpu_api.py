@@ -253,3 +253,24 @@ def test_fast_particles_rebin_every_step_with_the_same_physics(ctx):
     assert a.stats()["nonfinite"] == 0
     assert np.abs(da["x"] - db["x"]).max() <= 1e-4
     assert np.abs(da["v"] - db["v"]).max() <= 1e-3 * max(1.0, np.abs(db["v"]).max())
+
+
+@gpu
+def test_non_finite_particles_are_reported(ctx):
+    """A particle uploaded with a NaN velocity: the statistics count it at
+    once, and a later step call returns SNOW_ENUMERIC (the device counters are
+    read at re-binning points, one interval behind)."""
+    from snow_gb300 import api, native as N
+    s = scenes.small_scene(n=3000, grid_edge=32, seed=89)
+    s.v = s.v.copy()
+    s.v[17] = np.nan
+    sim = api.SimScene(ctx, s).upload().init()
+    assert sim.stats()["nonfinite"] == 1
+    status = 0
+    for _ in range(40):
+        try:
+            sim.step(s.dt, 1)
+        except N.SnowError as e:
+            status = e.status
+            break
+    assert status == -5  # SNOW_ENUMERIC
