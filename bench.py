@@ -51,6 +51,11 @@ TRAFFIC_MEASURED = {(1 << 20, 256): 145.4e6}
 INSTRUCTIONS_MEASURED = {(1 << 20, 256): 169.1e6}
 # warp-instruction issue peak: 152 SMs x 4 schedulers x 2.07 GHz
 ISSUE_PEAK = 152 * 4 * 2.07e9
+# FP32 peak: 152 SMs x 128 lanes x 2 flops per FMA x 2.07 GHz; the algorithmic
+# flops of one particle-step (axis weights and gradients ~150, P2G ~64 x 30,
+# G2P ~64 x 30, one 3x3 SVD ~1000, F_E algebra ~200) are an estimate
+FP32_PEAK = 152 * 128 * 2 * 2.07e9
+FLOPS_PER_PARTICLE_STEP = 4200
 
 
 def rank_info():
@@ -732,6 +737,11 @@ def main():
                             "kernel": "g2p2g", "instructions_per_launch": INSTRUCTIONS_MEASURED[
                                 (args.particles, args.grid)]}
                            if (args.particles, args.grid) in INSTRUCTIONS_MEASURED else None),
+        "flop_roofline": {"achieved": FLOPS_PER_PARTICLE_STEP * n / (res["per"]["g2p2g"] * 1e-3) / 1e12,
+                          "peak": FP32_PEAK / 1e12, "unit": "TFLOP/s (FP32)", "kernel": "g2p2g",
+                          "frac": FLOPS_PER_PARTICLE_STEP * n / (res["per"]["g2p2g"] * 1e-3) / FP32_PEAK,
+                          "flops_per_particle_step": FLOPS_PER_PARTICLE_STEP,
+                          "note": "algorithmic estimate of the flops, not counted ones"},
         "phase_ms": res["per"],
         "clocks": res["clocks"],
         "e2e": {"value": n * res["e2e_steps"] / res["e2e_s"], "unit": UNIT,
