@@ -11,6 +11,8 @@
  *     (src/snow/simulation/timeUpdate/explicittimeupdate.cpp:4-34)
  *   ExplicitTimeUpdate::update(double dt)               snow_scene_step(scene, dt, 1)
  *     (explicittimeupdate.cpp:36-63)
+ *   SemiImplicitTimeUpdate (empty in the reference:     snow_params.implicit_beta > 0
+ *     semiimplicittimeupdate.cpp:3-5)                      (FAST mode; snow_scene_solver_report)
  *   Technique::dispatch_with_barrier per kernel         snow_dispatch(scene, SNOW_K_*, dt)
  *     (src/snow/simulation/computingTechnique/*.cpp)
  *   ParticleSystem::initSSBO std140 buffers             snow_scene_upload_std140 /
