@@ -203,8 +203,25 @@ __device__ __forceinline__ bool hess_particle(const SceneDev& S, int p, const fl
   return true;
 }
 
+// The first item u' >= u of this CTA's round-robin share (u' = u mod the
+// grid) whose scene runs iteration k (total when none is left); s gets its
+// scene. The items of a finished scene are stepped over in one jump.
+__device__ __forceinline__ int next_running(const SceneDev* __restrict__ scenes, const int* __restrict__ item_prefix,
+                                            int nscenes, int k, int u, int total, int& s) {
+  const int g = gridDim.x;
+  while (u < total) {
+    s = find_scene(item_prefix, nscenes, u);
+    if (cr_running(scenes[s], k)) return u;
+    u += (item_prefix[s + 1] - u + g - 1) / g * g;
+  }
+  s = 0;
+  return total;
+}
+
 // K u for the items of every scene whose iteration k runs, into acc's force
-// slots (iteration 0: u = v*).
+// slots (iteration 0: u = v*). Persistent over the items like the fused
+// explicit kernel: the bulk copies of the CTA's next item are issued by the
+// last warp while the current item's per-cell sums are flushed.
 __global__ void __launch_bounds__(kItemMax, 2) k_hess(const SceneDev* __restrict__ scenes,
                                                       const int* __restrict__ item_prefix, int nscenes,
                                                       const int* __restrict__ iter) {
@@ -214,38 +231,53 @@ __global__ void __launch_bounds__(kItemMax, 2) k_hess(const SceneDev* __restrict
   ItemShared& sh = *reinterpret_cast<ItemShared*>(smem_raw);
   tile_init(sh);
   const int total = item_prefix[nscenes];
+  const int lane = threadIdx.x & 31;
+  const bool lastw = (threadIdx.x >> 5) == (blockDim.x >> 5) - 1;
+  int s = 0;
+  int u = next_running(scenes, item_prefix, nscenes, k, blockIdx.x, total, s);
+  if (u >= total) return;  // uniform across the CTA
+  int4 it = scenes[s].items[u - item_prefix[s]];
+  if (lastw) stage_issue(sh, scenes[s].cru, kImpBlockFloats, tile_slot(scenes[s], it, lane));
   uint32_t phase = 0;
-  for (int u = blockIdx.x; u < total; u += gridDim.x) {
-    const int s = find_scene(item_prefix, nscenes, u);
-    const SceneDev& S = scenes[s];
-    if (!cr_running(S, k)) continue;  // uniform across the CTA
-    const int4 it = S.items[u - item_prefix[s]];
+  while (u < total) {
+    __syncthreads();  // zero-filled stage blocks are visible; the last flush is done
     tile_zero(sh, 3);
+    const SceneDev& S = scenes[s];
+    // the next item and (last warp) its pool slots, loaded ahead of use
+    int sn = 0;
+    const int un = next_running(scenes, item_prefix, nscenes, k, u + gridDim.x, total, sn);
+    int4 itn = make_int4(0, 0, 0, 0);
+    int slot = -1;
+    if (un < total) {
+      itn = scenes[sn].items[un - item_prefix[sn]];
+      if (lastw) slot = tile_slot(scenes[sn], itn, lane);
+    }
     int bx, by, bz;
     home_coords(S, it.x, bx, by, bz);
-    if (threadIdx.x < 32) stage_issue(sh, S.cru, kImpBlockFloats, tile_slot(S, it, threadIdx.x));
-    __syncthreads();  // zero-filled stage blocks are visible
-    stage_wait(sh, S, phase);
     const int i = threadIdx.x;
+    const bool mine = i < min(it.z, kItemMax);
+    float4 xm = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (mine) xm = S.xm[it.y + i];
+    stage_wait(sh, S, phase);
     bool have = false;
     P2GParticle q;
     q.force = false;
     AxisW w;
     int base[3] = {0, 0, 0};
-    if (i < min(it.z, kItemMax)) {
-      const int p = it.y + i;
-      const float4 xm = S.xm[p];
-      if (fabsf(xm.w) <= 100.0f) {  // p2gTransfer.glsl:64-66
-        float pg[3];
-        grid_coords(S, xm, pg, base);
-        all_weights(pg, base, w);
-        float Gm[3][3];
-        hess_gather(sh, S, bx, by, bz, base, w, Gm);
-        have = hess_particle(S, p, Gm, q);
-      }
+    if (mine && fabsf(xm.w) <= 100.0f) {  // p2gTransfer.glsl:64-66
+      float pg[3];
+      grid_coords(S, xm, pg, base);
+      all_weights(pg, base, w);
+      float Gm[3][3];
+      hess_gather(sh, S, bx, by, bz, base, w, Gm);
+      have = hess_particle(S, it.y + i, Gm, q);
     }
-    p2g_tile_pass<kP2gForce>(sh, S, bx, by, bz, have, q, w, base, [] {});
-    __syncthreads();
+    p2g_tile_pass<kP2gForce>(sh, S, bx, by, bz, have, q, w, base, [&] {
+      if (lastw && un < total) stage_issue(sh, scenes[sn].cru, kImpBlockFloats, lane < 27 ? slot : -1);
+    });
+    u = un;
+    s = sn;
+    it = itn;
   }
 }
 
