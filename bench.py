@@ -225,6 +225,14 @@ def bench_ours(args, local_rank, barrier=lambda: None):
     sim.dispatch(N.K_G_FORCE, dt)
     sim.dispatch(N.K_G2P, dt)
     del g
+    # the scene's state after the timed steps and after one more step from
+    # it, for the oracle's check of that step at full size (outside every
+    # timed region)
+    check_states = None
+    if not args.no_cpu_baseline:
+        y0 = sim.download()
+        sim.step(dt, 1)
+        check_states = (y0, sim.download())
 
     # FAST phases: sort (rigid advance + binning), grid (compaction + grid
     # update), g2p2g (the fused particle kernel)
@@ -286,7 +294,7 @@ def bench_ours(args, local_rank, barrier=lambda: None):
     res = dict(total_ms=total_ms, step_ms=step_ms, n=n, A=A, per=per, dominant=dominant, alg_bytes=alg_bytes,
                achieved=achieved, peak=peak, peak_kind=peak_kind, clocks=clocks.summary(), e2e_s=e2e_s,
                e2e_steps=e2e_steps, e2e_split=split, h2d=h2d, d2h=d2h_stats + d2h_final / e2e_steps, launches=launches,
-               gen_s=gen_s, stats=st, scene=s, tuning=tuning)
+               gen_s=gen_s, stats=st, scene=s, tuning=tuning, check_states=check_states)
     ctx.close()
     return res
 
@@ -476,6 +484,54 @@ def cpu_baseline_port(scene, steps=2):
     return dict(value=scene.n * steps / el, unit=UNIT, cores=threads, kind="port",
                 sample=f"{steps} full steps of the same {scene.n}-particle scene, FP32 int32-fixed-point "
                        f"restatement of the shaders, OpenMP over {threads} threads")
+
+
+def oracle_check(scene, states, tol=1e-5):
+    """One step of the FP64 oracle (EXACT64: no fixed point, no V rounding;
+    OpenMP over the host cores), restarted from the GPU's state after the
+    timed steps, against the GPU's own next step: per-field relative errors
+    of the FAST path on the full workload, with the denominators of the
+    parity tests (x: max(|x|, 1e-3 m); v: max(|v|, 1e-3 m/s, 1e-2 max|v|);
+    F_E: max|F_E| per particle; J_p: |J_p|). The GPU's advance starts from
+    warm SVD frames; only det F_P enters a step, so F_P = diag(J_p, 1, 1)."""
+    from oracle import oracle as O
+    from snow_gb300 import scenes
+
+    if any(tuple(c.vel) != (0.0, 0.0, 0.0) for c in scene.colliders):
+        return None  # moving colliders: their positions after the run are not carried over
+    y0, y1 = states
+    n = len(y0["x"])
+    fp = np.zeros((n, 3, 3))
+    fp[:, 0, 0] = y0["Jp"]
+    fp[:, 1, 1] = fp[:, 2, 2] = 1.0
+    s3 = scenes.Scene(**{k: getattr(scene, k) for k in ("grid_pos", "grid_dim", "grid_spacing", "young", "poisson",
+                                                        "hardening", "crit_compression", "crit_stretch", "alpha",
+                                                        "gravity", "dt")})
+    s3.colliders = list(scene.colliders)
+    s3.x, s3.v, s3.m = y0["x"], y0["v"], scene.m.copy()
+    rho = np.where(y0["volume"] > 0, s3.m.astype(np.float64) / np.maximum(y0["volume"], 1e-30), 0.0)
+    threads = os.cpu_count() or 1
+    t = time.perf_counter()
+    o = O.OracleSim(s3, mode=O.EXACT64, vround=False, threads=threads)
+    o.upload(FE=y0["FE"].astype(np.float64), FP=fp).set_density(rho)
+    o.step()
+    ref = o.state()
+    oracle_s = time.perf_counter() - t
+    x, v = y1["x"].astype(np.float64), y1["v"].astype(np.float64)
+    speed = np.linalg.norm(ref["v"], axis=1)
+    err = {
+        "x": (np.abs(x - ref["x"]) / np.maximum(np.abs(ref["x"]), 1e-3)).max(1),
+        "v": np.linalg.norm(v - ref["v"], axis=1) / np.maximum(speed, max(1e-3, 1e-2 * speed.max())),
+        "FE": np.abs(y1["FE"].astype(np.float64) - ref["FE"]).max((1, 2)) / np.abs(ref["FE"]).max((1, 2)),
+        "Jp": np.abs(y1["Jp"].astype(np.float64) - ref["Jp"]) / np.abs(ref["Jp"]),
+    }
+    worst = max(float(e.max()) for e in err.values())
+    return {"oracle": "EXACT64 (FP64, OpenMP)", "particles": n, "steps": 1, "tolerance": tol,
+            "start": "the workload's state after the timed steps (GPU state, warm SVD frames)",
+            "max": {k: float(e.max()) for k, e in err.items()},
+            "p99": {k: float(np.percentile(e, 99)) for k, e in err.items()},
+            "median": {k: float(np.median(e)) for k, e in err.items()},
+            "within_tolerance": bool(worst <= tol), "oracle_s": oracle_s, "threads": threads}
 
 
 def bench_reference(args):
@@ -758,6 +814,9 @@ def main():
         line["serving"] = bench_serving(args, local_rank)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_port(res["scene"], steps=2)
+        # the same leg checks the timed workload's next step against the oracle
+        if res["check_states"] is not None:
+            line["oracle_check"] = oracle_check(res["scene"], res["check_states"])
     print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()

@@ -1,6 +1,6 @@
-"""Host-only entry points of the C ABI, called without a GPU: the defaults of
-defines.hpp, the reference world's walls, the device footprint bound the
-serving loop admits jobs by, and parameter validation."""
+"""Host-only logic, run without a GPU: the C ABI's defaults of defines.hpp,
+the reference world's walls, the device footprint bound the serving loop
+admits jobs by, parameter validation, and the bench's oracle check."""
 import ctypes
 
 import pytest
@@ -68,3 +68,29 @@ def test_invalid_parameters_have_no_footprint(L, field, value):
     p = _params(L)
     setattr(p, field, value)
     assert L.snow_scene_footprint(ctypes.byref(p), 1000) == 0
+
+
+def test_bench_oracle_check_on_an_oracle_state():
+    """The bench's full-size check (one FP64 oracle step restarted from a
+    state, against a given next state) on CPU, with the oracle's own FP32-
+    rounded steps standing in for the GPU's: within 1e-5, and the reported
+    fields are the parity tests' four."""
+    import numpy as np
+    import bench
+    from oracle import oracle as O
+    from snow_gb300 import scenes
+    s = scenes.small_scene(n=2000, grid_edge=24, seed=3, v0=(0.0, -2.0, 0.0))
+    o = O.OracleSim(s, mode=O.EXACT64).upload().init().step(n=3)
+
+    def f32(st, vol=None):
+        d = dict(x=st["x"].astype(np.float32), v=st["v"].astype(np.float32), FE=st["FE"].astype(np.float32),
+                 Jp=np.linalg.det(st["FP"]).astype(np.float32))
+        if vol:
+            d["volume"] = (s.m / st["rho"]).astype(np.float32)
+        return d
+
+    y0 = f32(o.state(), vol=True)
+    y1 = f32(o.step().state())
+    r = bench.oracle_check(s, (y0, y1))
+    assert set(r["max"]) == {"x", "v", "FE", "Jp"}
+    assert r["within_tolerance"] and max(r["max"].values()) < 1e-6, r["max"]
