@@ -285,8 +285,7 @@ __device__ __forceinline__ void scatter_global(const SceneDev& S, const P2GParti
 // ---- shared memory of one work item --------------------------------------
 struct ItemShared {
   float stage[27][kOutBlockFloats];  // G2P: the pool blocks around the home block
-  float4 pd[kItemMax][kPd];          // P2G: per-particle data
-  short plist[kItemMax];             // the item's particles in tile-cell order
+  float4 pd[kItemMax][kPd];          // P2G: per-particle data, in tile-cell order
   float tile[kAccFields * kTile3];   // P2G sums of the tile's nodes
   int cstart[kCells + 1];            // first pd slot of each tile cell
   int ccount[kCells];                // particles per tile cell (zero between items)
@@ -604,7 +603,7 @@ template <int KIND>
 __device__ __forceinline__ void cell_sums(const ItemShared& sh, int j0, int j1, int b, int c,
                                           float (&acc)[4][kAccFields]) {
   for (int j = j0; j < j1; j++) {
-    const float4* d = sh.pd[sh.plist[j]];
+    const float4* d = sh.pd[j];
     const float* df = reinterpret_cast<const float*>(d);
     const float4 w4 = d[4];
     const float wxa[4] = {w4.x, w4.y, w4.z, w4.w};
@@ -668,11 +667,11 @@ __device__ __forceinline__ int cell_row_node(int ci, int b, int c) {
 
 // P2G of the item's particles into acc (every thread of the CTA calls it;
 // thread i holds particle i of the item when `have`):
-//   1. each particle inside the tile counts itself in its base cell and
-//      stores its mass, momentum, A and axis weights (the others scatter
-//      straight to acc);
-//   2. a scan of the cell counts lists the particles in tile-cell order and
-//      the occupied cells;
+//   1. each particle inside the tile counts itself in its base cell (the
+//      others scatter straight to acc);
+//   2. a scan of the cell counts gives each cell's first slot and lists the
+//      occupied cells; each particle stores its mass, momentum, A and axis
+//      weights at its slot, so the particles lie in tile-cell order;
 //   3. each half-warp owns one occupied cell at a time: lane l sums the
 //      x-row (b, c) = (l & 3, l >> 2) of the cell's stencil over the cell's
 //      particles in registers and adds the row to the shared tile;
@@ -701,24 +700,7 @@ __device__ __forceinline__ void p2g_tile_pass(ItemShared& sh, const SceneDev& S,
       scatter_global<KIND>(S, q, w, base);
     }
   }
-  if (my_cell >= 0) {
-    float4* d = sh.pd[threadIdx.x];
-    const bool f = KIND != kP2gMass && q.force;
-    if (KIND == kP2gMass)
-      d[0] = make_float4(q.m, 0.0f, 0.0f, 0.0f);
-    else if (KIND == kP2gFull)
-      d[0] = make_float4(q.m, q.mv[0], q.mv[1], q.mv[2]);
-    d[1] = f ? make_float4(q.A[0][0], q.A[0][1], q.A[0][2], q.A[1][0]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    d[2] = f ? make_float4(q.A[1][1], q.A[1][2], q.A[2][0], q.A[2][1]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    d[3] = make_float4(f ? q.A[2][2] : 0.0f, __int_as_float(my_cell), 0.0f, 0.0f);
-    d[4] = make_float4(w.wx[0], w.wx[1], w.wx[2], w.wx[3]);
-    d[5] = make_float4(w.gx[0], w.gx[1], w.gx[2], w.gx[3]);
-    d[6] = make_float4(w.wy[0], w.wy[1], w.wy[2], w.wy[3]);
-    d[7] = make_float4(w.gy[0], w.gy[1], w.gy[2], w.gy[3]);
-    d[8] = make_float4(w.wz[0], w.wz[1], w.wz[2], w.wz[3]);
-    d[9] = make_float4(w.gz[0], w.gz[1], w.gz[2], w.gz[3]);
-  }
-  __syncthreads();  // counts and P2G data done
+  __syncthreads();  // counts done
   if (threadIdx.x == 32) sh.nrows = 0;  // the previous item's flush is long done
   // exclusive scan of the cell counts and list of the occupied cells, one
   // cell per thread
@@ -749,7 +731,24 @@ __device__ __forceinline__ void p2g_tile_pass(ItemShared& sh, const SceneDev& S,
   if (t == kCells - 1) sh.cstart[kCells] = off + incl;
   if (t == blockDim.x - 1) sh.ncells = ooff + __popc(occ);
   __syncthreads();
-  if (my_cell >= 0) sh.plist[sh.cstart[my_cell] + my_rank] = (short)threadIdx.x;
+  if (my_cell >= 0) {
+    // the particle's P2G data, stored in tile-cell order
+    float4* d = sh.pd[sh.cstart[my_cell] + my_rank];
+    const bool f = KIND != kP2gMass && q.force;
+    if (KIND == kP2gMass)
+      d[0] = make_float4(q.m, 0.0f, 0.0f, 0.0f);
+    else if (KIND == kP2gFull)
+      d[0] = make_float4(q.m, q.mv[0], q.mv[1], q.mv[2]);
+    d[1] = f ? make_float4(q.A[0][0], q.A[0][1], q.A[0][2], q.A[1][0]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    d[2] = f ? make_float4(q.A[1][1], q.A[1][2], q.A[2][0], q.A[2][1]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    d[3] = make_float4(f ? q.A[2][2] : 0.0f, __int_as_float(my_cell), 0.0f, 0.0f);
+    d[4] = make_float4(w.wx[0], w.wx[1], w.wx[2], w.wx[3]);
+    d[5] = make_float4(w.gx[0], w.gx[1], w.gx[2], w.gx[3]);
+    d[6] = make_float4(w.wy[0], w.wy[1], w.wy[2], w.wy[3]);
+    d[7] = make_float4(w.gy[0], w.gy[1], w.gy[2], w.gy[3]);
+    d[8] = make_float4(w.wz[0], w.wz[1], w.wz[2], w.wz[3]);
+    d[9] = make_float4(w.gz[0], w.gz[1], w.gz[2], w.gz[3]);
+  }
   __syncthreads();
   {
     // half-warp h takes a contiguous slice of the occupied-cell list (the
