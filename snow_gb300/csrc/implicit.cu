@@ -58,23 +58,13 @@ __device__ __forceinline__ bool any_running(const SceneDev* __restrict__ scenes,
   return false;
 }
 
-// G = sum_j u_j (grad w_j)^T over the particle's stencil, u from the staged
-// tile (3 floats per node) when the stencil lies in it, else from cru.
-__device__ __forceinline__ void hess_gather(const ItemShared& sh, const SceneDev& S, int bx, int by, int bz,
-                                            const int base[3], const AxisW& w, float Gm[3][3]) {
+// G = sum_j u_j (grad w_j)^T over the particle's stencil, contracted along x
+// first for each (y, z) row; node(a, b, c, u) fills u at stencil node
+// (a, b, c) (zero for a node that contributes nothing).
+template <class Node>
+__device__ __forceinline__ void hess_sums(const AxisW& w, Node node, float Gm[3][3]) {
 #pragma unroll
   for (int r = 0; r < 3; r++) Gm[r][0] = Gm[r][1] = Gm[r][2] = 0.0f;
-  const int tx = base[0] - 1 - (4 * bx - 2), ty = base[1] - 1 - (4 * by - 2), tz = base[2] - 1 - (4 * bz - 2);
-  const bool in_tile = tx >= 0 && ty >= 0 && tz >= 0 && tx <= kTile - 4 && ty <= kTile - 4 && tz <= kTile - 4;
-  int X[4], Y[4], Z[4];
-#pragma unroll
-  for (int a = 0; a < 4; a++) {
-    const int t = tx + a, q = ty + a, r = tz + a;
-    X[a] = ((t + 2) >> 2) * kOutBlockFloats + 3 * ((t + 2) & 3);
-    Y[a] = ((q + 2) >> 2) * 3 * kOutBlockFloats + 3 * 4 * ((q + 2) & 3);
-    Z[a] = ((r + 2) >> 2) * 9 * kOutBlockFloats + 3 * 16 * ((r + 2) & 3);
-  }
-  const float* st = &sh.stage[0][0];
 #pragma unroll
   for (int c = 0; c < 4; c++) {
 #pragma unroll
@@ -83,24 +73,7 @@ __device__ __forceinline__ void hess_gather(const ItemShared& sh, const SceneDev
 #pragma unroll
       for (int a = 0; a < 4; a++) {
         float u[3];
-        if (in_tile) {
-          const float* o = st + X[a] + Y[b] + Z[c];
-          u[0] = o[0];
-          u[1] = o[1];
-          u[2] = o[2];
-        } else {
-          const int g0 = base[0] - 1 + a, g1 = base[1] - 1 + b, g2 = base[2] - 1 + c;
-          u[0] = u[1] = u[2] = 0.0f;
-          if (node_in_grid(S, g0, g1, g2)) {
-            const int sl = __ldg(&S.blk_slot[block_id(S, g0 >> 2, g1 >> 2, g2 >> 2)]);
-            if (sl >= 0) {
-              const float* o = S.cru + (size_t)sl * kImpBlockFloats + 3 * ((g0 & 3) + 4 * (g1 & 3) + 16 * (g2 & 3));
-              u[0] = __ldg(o);
-              u[1] = __ldg(o + 1);
-              u[2] = __ldg(o + 2);
-            }
-          }
-        }
+        node(a, b, c, u);
 #pragma unroll
         for (int r = 0; r < 3; r++) {
           S1[r] += w.wx[a] * u[r];
@@ -115,6 +88,47 @@ __device__ __forceinline__ void hess_gather(const ItemShared& sh, const SceneDev
         Gm[r][2] += t3 * S1[r];
       }
     }
+  }
+}
+
+// The gather of u (3 floats per node) from the staged tile when the stencil
+// lies in it (decided once per particle), else from cru.
+__device__ __forceinline__ void hess_gather(const ItemShared& sh, const SceneDev& S, int bx, int by, int bz,
+                                            const int base[3], const AxisW& w, float Gm[3][3]) {
+  const int tx = base[0] - 1 - (4 * bx - 2), ty = base[1] - 1 - (4 * by - 2), tz = base[2] - 1 - (4 * bz - 2);
+  if (tx >= 0 && ty >= 0 && tz >= 0 && tx <= kTile - 4 && ty <= kTile - 4 && tz <= kTile - 4) {
+    // tile node t (0..8) lies in tile block floor((t + 2) / 4) at local (t + 2) & 3
+    int X[4], Y[4], Z[4];
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+      const int t = tx + a, q = ty + a, r = tz + a;
+      X[a] = ((t + 2) >> 2) * kOutBlockFloats + 3 * ((t + 2) & 3);
+      Y[a] = ((q + 2) >> 2) * 3 * kOutBlockFloats + 3 * 4 * ((q + 2) & 3);
+      Z[a] = ((r + 2) >> 2) * 9 * kOutBlockFloats + 3 * 16 * ((r + 2) & 3);
+    }
+    const float* st = &sh.stage[0][0];
+    hess_sums(w,
+              [&](int a, int b, int c, float u[3]) {
+                const float* o = st + X[a] + Y[b] + Z[c];
+                u[0] = o[0];
+                u[1] = o[1];
+                u[2] = o[2];
+              },
+              Gm);
+  } else {
+    hess_sums(w,
+              [&](int a, int b, int c, float u[3]) {
+                const int g0 = base[0] - 1 + a, g1 = base[1] - 1 + b, g2 = base[2] - 1 + c;
+                u[0] = u[1] = u[2] = 0.0f;
+                if (!node_in_grid(S, g0, g1, g2)) return;
+                const int sl = __ldg(&S.blk_slot[block_id(S, g0 >> 2, g1 >> 2, g2 >> 2)]);
+                if (sl < 0) return;
+                const float* o = S.cru + (size_t)sl * kImpBlockFloats + 3 * ((g0 & 3) + 4 * (g1 & 3) + 16 * (g2 & 3));
+                u[0] = __ldg(o);
+                u[1] = __ldg(o + 1);
+                u[2] = __ldg(o + 2);
+              },
+              Gm);
   }
 }
 
@@ -157,9 +171,11 @@ __device__ __forceinline__ bool hess_particle(const SceneDev& S, int p, const fl
 #pragma unroll
     for (int r = 0; r < 3; r++) dF.m[c][r] = Gm[r][0] * F.m[c][0] + Gm[r][1] * F.m[c][1] + Gm[r][2] * F.m[c][2];
   const M3 Gw = m3_mul_at(W, m3_mul(dF, V));  // W^T dF V; Gw.m[c][r] is row r, column c
-  const float x01 = (Gw.m[1][0] - Gw.m[0][1]) / (sig[0] + sig[1]);
-  const float x02 = (Gw.m[2][0] - Gw.m[0][2]) / (sig[0] + sig[2]);
-  const float x12 = (Gw.m[2][1] - Gw.m[1][2]) / (sig[1] + sig[2]);
+  // singular values of a deformation gradient are O(1): the fast divide's
+  // 2 ulp are far inside the solve's tolerance
+  const float x01 = __fdividef(Gw.m[1][0] - Gw.m[0][1], sig[0] + sig[1]);
+  const float x02 = __fdividef(Gw.m[2][0] - Gw.m[0][2], sig[0] + sig[2]);
+  const float x12 = __fdividef(Gw.m[2][1] - Gw.m[1][2], sig[1] + sig[2]);
   M3 X;
   X.m[0][0] = 0.0f; X.m[1][0] = x01;  X.m[2][0] = x02;
   X.m[0][1] = -x01; X.m[1][1] = 0.0f; X.m[2][1] = x12;
