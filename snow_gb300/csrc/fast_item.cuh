@@ -28,7 +28,9 @@ template <int KIND> struct P2gFields {
 };
 constexpr int kCellsPerAxis = kTile - 3;  // 6
 constexpr int kCells = kCellsPerAxis * kCellsPerAxis * kCellsPerAxis;
-constexpr int kPd = 10;           // float4 per particle of P2G data in shared memory
+constexpr int kPd = 11;  // float4 per particle of P2G data in shared memory: 10 used, the 11th pads
+                         // the stride to 44 words so the 8 threads of a 16-byte store phase hit 8
+                         // distinct groups of 4 banks
 constexpr int kShColliders = 16;  // colliders cached in shared memory
 constexpr uint32_t kWaitPolls = 1u << 24;
 
