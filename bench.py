@@ -47,8 +47,8 @@ BYTES_GRID = (0, 40)
 # (profiles/k_g2p2g_two_snowballs_1M_256.md), keyed by (particles, grid edge);
 # other workloads report null: DRAM bytes (read + write) per launch, and warp
 # instructions per launch for the issue roofline.
-TRAFFIC_MEASURED = {(1 << 20, 256): 145.4e6}
-INSTRUCTIONS_MEASURED = {(1 << 20, 256): 169.1e6}
+TRAFFIC_MEASURED = {(1 << 20, 256): 144.1e6}
+INSTRUCTIONS_MEASURED = {(1 << 20, 256): 167.1e6}
 # warp-instruction issue peak: 152 SMs x 4 schedulers x 2.07 GHz
 ISSUE_PEAK = 152 * 4 * 2.07e9
 # FP32 peak: 152 SMs x 128 lanes x 2 flops per FMA x 2.07 GHz; the algorithmic
