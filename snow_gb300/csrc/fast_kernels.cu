@@ -376,7 +376,7 @@ __global__ void __launch_bounds__(kItemMax, 2) k_g2p2g(const SceneDev* __restric
 // Bulk statistics: per-thread sums in FP32 over a dozen particles, then FP64
 // across threads (FP64 arithmetic is slow on this part: the per-particle work
 // stays in FP32).
-__global__ void __launch_bounds__(256) k_stats(const SceneDev* __restrict__ sd, int n, StatsSlot* slot,
+__global__ void __launch_bounds__(kStatsThreads) k_stats(const SceneDev* __restrict__ sd, int n, StatsSlot* slot,
                                                StatsAccum* host) {
   const SceneDev& S = *sd;
   float acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -611,11 +611,11 @@ void fast_g2p2g(const SceneDev* scenes, const int* item_prefix, int nscenes, int
 }
 
 void fast_stats(const SceneDev* sd_dev, int n, StatsSlot* slot, StatsAccum* host, cudaStream_t st) {
-  int g = (n + 255) / 256;  // at least one block: it publishes the empty sums
+  int g = (n + kStatsThreads - 1) / kStatsThreads;  // at least one block: it publishes the empty sums
   if (g > num_sms()) g = num_sms();  // one block per SM: measured fastest (fixed costs dominate)
   if (g > kStatsMaxBlocks) g = kStatsMaxBlocks;
   if (g < 1) g = 1;
-  k_stats<<<g, 256, 0, st>>>(sd_dev, n < 0 ? 0 : n, slot, host);
+  k_stats<<<g, kStatsThreads, 0, st>>>(sd_dev, n < 0 ? 0 : n, slot, host);
 }
 
 

@@ -315,6 +315,7 @@ __global__ void __launch_bounds__(kThreads) k_advance(RefArgs a, float dt) {
   }
 }
 
+static_assert(kThreads == kStatsThreads, "the statistics commit assumes this block size");
 __global__ void __launch_bounds__(kThreads) k_stats(RefArgs a, StatsSlot* slot, StatsAccum* host) {
   StatsPartial t;
   stats_init(t);

@@ -30,17 +30,13 @@ __device__ __forceinline__ void stats_init(StatsPartial& t) {
   t.bad = 0;
 }
 
-// Every thread of the block calls this once with its partials; blockDim.x is a
-// multiple of 32 and at most 1024, gridDim.x at most kStatsMaxBlocks. Each
-// block stores its sums in slot->part; the last block to do so adds them up
-// in block order, publishes the totals to `host` and re-arms the slot.
-__device__ __forceinline__ void stats_commit(StatsPartial& t, StatsSlot* slot, StatsAccum* host) {
-  __shared__ StatsPartial warp_sums[32];
-  __shared__ bool last;
+constexpr int kStatsThreads = 256;  // the block size of every statistics kernel
+
+// Bounds and the non-finite count of the calling warp, combined with
+// shuffles (FP32 min/max, integer sums: cheap), in lane 0.
+__device__ __forceinline__ void stats_warp_bounds(StatsPartial& t) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-#pragma unroll
-    for (int k = 0; k < 9; k++) t.acc[k] += __shfl_down_sync(0xffffffffu, t.acc[k], o);
 #pragma unroll
     for (int k = 0; k < 3; k++) {
       t.bmin[k] = fminf(t.bmin[k], __shfl_down_sync(0xffffffffu, t.bmin[k], o));
@@ -48,81 +44,124 @@ __device__ __forceinline__ void stats_commit(StatsPartial& t, StatsSlot* slot, S
     }
     t.bad += __shfl_down_sync(0xffffffffu, t.bad, o);
   }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  if (lane == 0) warp_sums[warp] = t;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    StatsPartial b = warp_sums[0];
-    for (int w = 1; w < nwarps; w++) {
-      for (int k = 0; k < 9; k++) b.acc[k] += warp_sums[w].acc[k];
-      for (int k = 0; k < 3; k++) {
-        b.bmin[k] = fminf(b.bmin[k], warp_sums[w].bmin[k]);
-        b.bmax[k] = fmaxf(b.bmax[k], warp_sums[w].bmax[k]);
-      }
-      b.bad += warp_sums[w].bad;
-    }
-    StatsBlockSum& mine = slot->part[blockIdx.x];
-    for (int k = 0; k < 9; k++) mine.acc[k] = b.acc[k];
+}
+
+// FP64 sum over 32 lanes (the result in lane 0).
+__device__ __forceinline__ double stats_warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Every thread of the block (kStatsThreads of them) calls this once with
+// its partials; gridDim.x is at most kStatsMaxBlocks. The nine FP64 sums
+// are transposed through shared memory: warp w sums fields w, w + 8 over
+// the block's threads (8 values per lane, then 5 shuffle steps), so each
+// field costs 31 + 32 * 7 additions instead of every lane reducing all nine
+// fields (FP64 arithmetic is slow on this part). Each block stores its sums
+// in slot->part; the last block to do so adds the records up the same way,
+// in block order, publishes the totals to `host` and re-arms the slot. The
+// order of every addition is fixed, so the totals do not depend on block
+// scheduling.
+__device__ __forceinline__ void stats_commit(StatsPartial& t, StatsSlot* slot, StatsAccum* host) {
+  __shared__ double sacc[9][kStatsThreads];
+  __shared__ double bsum[9];
+  __shared__ float wmin[kStatsThreads / 32][3], wmax[kStatsThreads / 32][3];
+  __shared__ unsigned long long wbad[kStatsThreads / 32];
+  __shared__ bool last;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  constexpr int nwarps = kStatsThreads / 32;
+#pragma unroll
+  for (int k = 0; k < 9; k++) sacc[k][tid] = t.acc[k];
+  stats_warp_bounds(t);
+  if (lane == 0) {
+#pragma unroll
     for (int k = 0; k < 3; k++) {
-      mine.bmin[k] = b.bmin[k];
-      mine.bmax[k] = b.bmax[k];
+      wmin[warp][k] = t.bmin[k];
+      wmax[warp][k] = t.bmax[k];
     }
-    mine.bad = b.bad;
+    wbad[warp] = t.bad;
+  }
+  __syncthreads();
+  for (int k = warp; k < 9; k += nwarps) {
+    double v = 0.0;
+#pragma unroll
+    for (int i = 0; i < kStatsThreads / 32; i++) v += sacc[k][lane + 32 * i];
+    v = stats_warp_sum(v);
+    if (lane == 0) bsum[k] = v;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    StatsBlockSum& mine = slot->part[blockIdx.x];
+    for (int k = 0; k < 9; k++) mine.acc[k] = bsum[k];
+    for (int k = 0; k < 3; k++) {
+      float lo = wmin[0][k], hi = wmax[0][k];
+      for (int w = 1; w < nwarps; w++) {
+        lo = fminf(lo, wmin[w][k]);
+        hi = fmaxf(hi, wmax[w][k]);
+      }
+      mine.bmin[k] = lo;
+      mine.bmax[k] = hi;
+    }
+    unsigned long long bad = 0;
+    for (int w = 0; w < nwarps; w++) bad += wbad[w];
+    mine.bad = bad;
     __threadfence();
     last = atomicAdd(&slot->done, 1u) == gridDim.x - 1;
   }
   __syncthreads();
   if (!last) return;
-  // the last block: thread i sums blocks i, i + blockDim.x, ... then the
-  // block's warps and threads combine in a fixed order
+  // the last block: warp w sums fields w, w + 8 over the records (lane l
+  // takes records l, l + 32, ...; L2 reads: other blocks wrote them before
+  // their fence), every thread the bounds of records tid, tid + 256, ...
   __threadfence();
-  StatsPartial s;
-  stats_init(s);
-  for (int q = threadIdx.x; q < (int)gridDim.x; q += blockDim.x) {
-    // L2 reads (the records were written by other blocks before their fence)
+  const int nb = (int)gridDim.x;
+  for (int k = warp; k < 9; k += nwarps) {
+    double v = 0.0;
+    for (int q = lane; q < nb; q += 32) v += __ldcg(&slot->part[q].acc[k]);
+    v = stats_warp_sum(v);
+    if (lane == 0) bsum[k] = v;
+  }
+  StatsPartial b;
+  stats_init(b);
+  for (int q = tid; q < nb; q += kStatsThreads) {
     const StatsBlockSum* p = &slot->part[q];
-    for (int k = 0; k < 9; k++) s.acc[k] += __ldcg(&p->acc[k]);
     for (int k = 0; k < 3; k++) {
-      s.bmin[k] = fminf(s.bmin[k], __ldcg(&p->bmin[k]));
-      s.bmax[k] = fmaxf(s.bmax[k], __ldcg(&p->bmax[k]));
+      b.bmin[k] = fminf(b.bmin[k], __ldcg(&p->bmin[k]));
+      b.bmax[k] = fmaxf(b.bmax[k], __ldcg(&p->bmax[k]));
     }
-    s.bad += __ldcg(&p->bad);
+    b.bad += __ldcg(&p->bad);
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-#pragma unroll
-    for (int k = 0; k < 9; k++) s.acc[k] += __shfl_down_sync(0xffffffffu, s.acc[k], o);
+  stats_warp_bounds(b);
+  __syncthreads();  // wmin / wmax / wbad are reused
+  if (lane == 0) {
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-      s.bmin[k] = fminf(s.bmin[k], __shfl_down_sync(0xffffffffu, s.bmin[k], o));
-      s.bmax[k] = fmaxf(s.bmax[k], __shfl_down_sync(0xffffffffu, s.bmax[k], o));
+      wmin[warp][k] = b.bmin[k];
+      wmax[warp][k] = b.bmax[k];
     }
-    s.bad += __shfl_down_sync(0xffffffffu, s.bad, o);
+    wbad[warp] = b.bad;
   }
-  __syncthreads();  // warp_sums is reused
-  if (lane == 0) warp_sums[warp] = s;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    StatsPartial b = warp_sums[0];
-    for (int w = 1; w < nwarps; w++) {
-      for (int k = 0; k < 9; k++) b.acc[k] += warp_sums[w].acc[k];
-      for (int k = 0; k < 3; k++) {
-        b.bmin[k] = fminf(b.bmin[k], warp_sums[w].bmin[k]);
-        b.bmax[k] = fmaxf(b.bmax[k], warp_sums[w].bmax[k]);
-      }
-      b.bad += warp_sums[w].bad;
-    }
+  if (tid == 0) {
     StatsAccum r;
-    r.mass = b.acc[0];
+    r.mass = bsum[0];
     for (int k = 0; k < 3; k++) {
-      r.mom[k] = b.acc[1 + k];
-      r.com[k] = b.acc[5 + k];
-      r.bmin_key[k] = stats_order_key(b.bmin[k]);
-      r.bmax_key[k] = stats_order_key(b.bmax[k]);
+      float lo = wmin[0][k], hi = wmax[0][k];
+      for (int w = 1; w < nwarps; w++) {
+        lo = fminf(lo, wmin[w][k]);
+        hi = fmaxf(hi, wmax[w][k]);
+      }
+      r.mom[k] = bsum[1 + k];
+      r.com[k] = bsum[5 + k];
+      r.bmin_key[k] = stats_order_key(lo);
+      r.bmax_key[k] = stats_order_key(hi);
     }
-    r.ke = b.acc[4];
-    r.jp = b.acc[8];
-    r.nonfinite = b.bad;
+    r.ke = bsum[4];
+    r.jp = bsum[8];
+    unsigned long long bad = 0;
+    for (int w = 0; w < nwarps; w++) bad += wbad[w];
+    r.nonfinite = bad;
     *host = r;  // visible to the host once it has waited for the kernel
     slot->done = 0u;
   }
