@@ -362,8 +362,10 @@ snow_status snow_scene_set_tuning(snow_scene* s, const snow_tuning* t);
 /* Applies a tuning to every scene of the batch (e.g. one kept from an
  * earlier autotune); takes effect at each scene's next re-binning. */
 snow_status snow_batch_set_tuning(snow_batch* b, const snow_tuning* t);
-/* Times candidate tunings (sort interval 1/2/4/8/12/16 x 128/256 particles per work
- * item x 1/2 CTAs per SM) on real steps of the batch and keeps the fastest.
+/* Times candidate tunings (sort interval 1/2/4/8/12/16/24/32 x 128/256 particles per work
+ * item x 1/2 CTAs per SM) on real steps of the batch and keeps the fastest;
+ * each candidate is timed in a forward and in a reversed pass over the list
+ * (the scenes evolve meanwhile, and the two passes cancel a linear drift).
  * The steps advance the scenes like snow_batch_step (out->steps_taken says
  * how many); dt as for snow_batch_step. */
 snow_status snow_batch_autotune(snow_batch* b, const double* dt, snow_tuning* out);

@@ -1558,13 +1558,23 @@ snow_status snow_batch_set_tuning(snow_batch* b, const snow_tuning* t) {
 // Times each candidate (sort interval x particles per work item x CTAs per
 // SM) over real steps of the batch -- one sort interval to re-bin every scene
 // with the candidate's work items and capture its graphs, then two intervals
-// (at least 32 steps) timed with events -- and keeps the fastest.
+// (at least 32 steps) timed with events -- and keeps the fastest. The scenes
+// evolve while the candidates run, so the cost of a step drifts; every
+// candidate is timed twice, once in a forward and once in a reversed pass
+// over the list, and the two times are averaged, which cancels a drift that
+// is linear in the steps taken.
 snow_status snow_batch_autotune(snow_batch* b, const double* dt, snow_tuning* out) {
   if (!b) return SNOW_EINVAL;
   snow_ctx* ctx = b->ctx;
-  static const int kIntervals[] = {1, 2, 4, 8, 12, 16};  // 1, 2: particles that cross cells in a step or two
+  // 1, 2: particles that cross cells in a step or two; 24, 32: slow particles, binning amortised further
+  static const int kIntervals[] = {1, 2, 4, 8, 12, 16, 24, 32};
   static const int kItems[] = {128, 256};
   static const int kCtas[] = {1, 2};
+  std::vector<snow_tuning> cand;
+  for (int si : kIntervals)
+    for (int im : kItems)
+      for (int cp : kCtas) cand.push_back(snow_tuning{si, im, cp, 0, 0.0});
+  const int nc = (int)cand.size();
   snow_tuning best{};
   best.ms_per_step = 1e30;
   int steps = 0;
@@ -1572,25 +1582,24 @@ snow_status snow_batch_autotune(snow_batch* b, const double* dt, snow_tuning* ou
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
   snow_status r = SNOW_OK;
-  for (int si : kIntervals)
-    for (int im : kItems)
-      for (int cp : kCtas) {
-        snow_tuning t{si, im, cp, 0, 0.0};
-        if ((r = snow_batch_set_tuning(b, &t))) goto done;
-        if ((r = snow_batch_step(b, dt, si))) goto done;
-        const int k = std::max(32, 2 * si);
-        if (cudaEventRecord(e0, ctx->stream) != cudaSuccess) { r = cuda_fail(ctx, cudaGetLastError(), "event"); goto done; }
-        if ((r = snow_batch_step(b, dt, k))) goto done;
-        if (cudaEventRecord(e1, ctx->stream) != cudaSuccess) { r = cuda_fail(ctx, cudaGetLastError(), "event"); goto done; }
-        if (cudaEventSynchronize(e1) != cudaSuccess) { r = cuda_fail(ctx, cudaGetLastError(), "event"); goto done; }
-        float ms = 0.0f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        steps += si + k;
-        if (ms / k < best.ms_per_step) {
-          best = t;
-          best.ms_per_step = ms / k;
-        }
-      }
+  for (int pass = 0; pass < 2; pass++)
+    for (int j = 0; j < nc; j++) {
+      snow_tuning& t = cand[pass == 0 ? j : nc - 1 - j];
+      const int si = t.sort_interval;
+      if ((r = snow_batch_set_tuning(b, &t))) goto done;
+      if ((r = snow_batch_step(b, dt, si))) goto done;
+      const int k = std::max(32, 2 * si);
+      if (cudaEventRecord(e0, ctx->stream) != cudaSuccess) { r = cuda_fail(ctx, cudaGetLastError(), "event"); goto done; }
+      if ((r = snow_batch_step(b, dt, k))) goto done;
+      if (cudaEventRecord(e1, ctx->stream) != cudaSuccess) { r = cuda_fail(ctx, cudaGetLastError(), "event"); goto done; }
+      if (cudaEventSynchronize(e1) != cudaSuccess) { r = cuda_fail(ctx, cudaGetLastError(), "event"); goto done; }
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      steps += si + k;
+      t.ms_per_step += 0.5 * ms / k;
+    }
+  for (const snow_tuning& t : cand)
+    if (t.ms_per_step < best.ms_per_step) best = t;
   r = snow_batch_set_tuning(b, &best);
 done:
   cudaEventDestroy(e0);

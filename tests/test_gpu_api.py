@@ -144,7 +144,7 @@ def test_autotune_picks_a_candidate_and_reuses_the_cache(ctx, tmp_path):
     cache = str(tmp_path / "tuning.json")
     c = b.autotune(dt=[s.dt for s in scs], cache=cache)
     assert not c["cached"] and c["steps_taken"] > 0 and c["ms_per_step"] > 0
-    assert c["sort_interval"] in (1, 2, 4, 8, 12, 16) and c["items_max"] in (128, 256) and c["ctas_per_sm"] in (1, 2)
+    assert c["sort_interval"] in (1, 2, 4, 8, 12, 16, 24, 32) and c["items_max"] in (128, 256) and c["ctas_per_sm"] in (1, 2)
     again = b.autotune(dt=[s.dt for s in scs], cache=cache)
     assert again["cached"] and again["steps_taken"] == 0
     assert {k: again[k] for k in ("sort_interval", "items_max", "ctas_per_sm")} == \
