@@ -109,10 +109,13 @@ __device__ __forceinline__ void all_weights(const float pg[3], const int base[3]
   axis_weights(pg[2], base[2], w.wz, w.gz);
 }
 
-__device__ __forceinline__ void load_fe(const SceneDev& S, int p, M3& F, float& jp) {
-  const float4 a = S.fa[p];
-  const float4 b = S.fb[p];
-  const float2 c = S.fc[p];
+// Whether this step's binning left the particles in the binned copies.
+__device__ __forceinline__ bool particles_binned(const SceneDev& S) { return S.counters[CNT_BINNED] != 0; }
+
+__device__ __forceinline__ void load_fe(const SceneDev& S, int p, M3& F, float& jp, bool binned = false) {
+  const float4 a = (binned ? S.bfa : S.fa)[p];
+  const float4 b = (binned ? S.bfb : S.fb)[p];
+  const float2 c = (binned ? S.bfc : S.fc)[p];
   F.m[0][0] = a.x; F.m[0][1] = a.y; F.m[0][2] = a.z;
   F.m[1][0] = a.w; F.m[1][1] = b.x; F.m[1][2] = b.y;
   F.m[2][0] = b.z; F.m[2][1] = b.w; F.m[2][2] = c.x;
@@ -494,10 +497,10 @@ struct PState {
   float4 xm, vv;
 };
 
-__device__ __forceinline__ PState load_state(const SceneDev& S, int p) {
+__device__ __forceinline__ PState load_state(const SceneDev& S, int p, bool binned) {
   PState t;
-  t.xm = S.xm[p];
-  t.vv = S.vv[p];
+  t.xm = (binned ? S.bxm : S.xm)[p];
+  t.vv = (binned ? S.bvv : S.vv)[p];
   return t;
 }
 
@@ -515,12 +518,12 @@ struct PDef {
   float2 fc;
 };
 
-__device__ __forceinline__ PDef load_def(const SceneDev& S, int p) {
+__device__ __forceinline__ PDef load_def(const SceneDev& S, int p, bool binned) {
   PDef d;
-  d.fa = S.fa[p];
-  d.fb = S.fb[p];
-  d.vq = S.vq[p];
-  d.fc = S.fc[p];
+  d.fa = (binned ? S.bfa : S.fa)[p];
+  d.fb = (binned ? S.bfb : S.fb)[p];
+  d.vq = (binned ? S.bvq : S.vq)[p];
+  d.fc = (binned ? S.bfc : S.fc)[p];
   return d;
 }
 

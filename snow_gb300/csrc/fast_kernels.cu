@@ -59,6 +59,7 @@ __global__ void k_begin_step(const SceneDev* __restrict__ scenes, int nscenes, i
   if (threadIdx.x == 0) {
     S.counters[CNT_ACTIVE] = 0;
     S.counters[CNT_OVERFLOW] = 0;
+    S.counters[CNT_BINNED] = 0;
   }
   if (rigid)  // rigidAdvance.glsl:14-18
     for (int i = threadIdx.x; i < S.ncoll; i += blockDim.x)
@@ -259,7 +260,7 @@ __global__ void __launch_bounds__(kItemMax) k_g2p_advance(const SceneDev* __rest
     stage_wait(sh, S, phase);
     for (int i = threadIdx.x; i < it.z; i += blockDim.x) {
       const int p = it.y + i;
-      const PState ps = load_state(S, p);
+      const PState ps = load_state(S, p, false);  // per-kernel dispatches: binned in place
       float pg[3];
       int base[3];
       grid_coords(S, ps.xm, pg, base);
@@ -268,7 +269,7 @@ __global__ void __launch_bounds__(kItemMax) k_g2p_advance(const SceneDev* __rest
       float dv[3], L[3][3];
       g2p_gather(sh, S, bx, by, bz, base, w, dv, L);
       Advanced adv;
-      advance_particle(S, p, ps, load_def(S, p), dv, L, sh, adv);
+      advance_particle(S, p, ps, load_def(S, p, false), dv, L, sh, adv);
     }
     __syncthreads();
   }
@@ -279,7 +280,10 @@ __global__ void __launch_bounds__(kItemMax) k_g2p_advance(const SceneDev* __rest
 // the rotation R = W V^T of the advance's SVD: F_E' = W S' V^T with S'
 // diagonal up to the Jacobi residual, whose polar rotation is W V^T.
 // The pool blocks of the CTA's next item are copied into shared memory while
-// this item's P2G runs.
+// this item's P2G runs. BINNED: a step that re-binned some scene; such a
+// scene's particles are read from its binned copies (CNT_BINNED) and, like
+// every scene's, written to its streams.
+template <bool BINNED>
 __global__ void __launch_bounds__(kItemMax, 2) k_g2p2g(const SceneDev* __restrict__ scenes,
                                                        const int* __restrict__ item_prefix, int nscenes) {
   extern __shared__ float4 smem_raw[];
@@ -330,7 +334,8 @@ __global__ void __launch_bounds__(kItemMax, 2) k_g2p2g(const SceneDev* __restric
     const bool mine = i < min(it.z, kItemMax);
     const int p = it.y + i;
     PState ps;
-    if (mine) ps = load_state(S, p);
+    const bool binned = BINNED && particles_binned(S);
+    if (mine) ps = load_state(S, p, binned);
     stage_wait(sh, S, phase);
     bool have = false;
     P2GParticle q;
@@ -344,7 +349,7 @@ __global__ void __launch_bounds__(kItemMax, 2) k_g2p2g(const SceneDev* __restric
       all_weights(pg, base, w);
       float dv[3], L[3][3];
       g2p_gather(sh, S, bx, by, bz, base, w, dv, L);
-      const PDef def = load_def(S, p);
+      const PDef def = load_def(S, p, binned);
       Advanced adv;
       advance_particle(S, p, ps, def, dv, L, sh, adv);
       // P2G quantities of the advanced particle
@@ -534,7 +539,8 @@ int item_smem() {
     smem_opt_in(k_p2g<true>, bytes);
     smem_opt_in(k_p2g<false>, bytes);
     smem_opt_in(k_g2p_advance, bytes);
-    smem_opt_in(k_g2p2g, bytes);
+    smem_opt_in(k_g2p2g<false>, bytes);
+    smem_opt_in(k_g2p2g<true>, bytes);
     configured = true;
   }
   return bytes;
@@ -606,8 +612,12 @@ void fast_g2p_advance(const SceneDev* scenes, const int* item_prefix, int nscene
   k_g2p_advance<<<grid_ctas, kItemMax, item_smem(), st>>>(scenes, item_prefix, nscenes);
 }
 
-void fast_g2p2g(const SceneDev* scenes, const int* item_prefix, int nscenes, int grid_ctas, cudaStream_t st) {
-  k_g2p2g<<<grid_ctas, kItemMax, item_smem(), st>>>(scenes, item_prefix, nscenes);
+void fast_g2p2g(const SceneDev* scenes, const int* item_prefix, int nscenes, int grid_ctas, bool binned,
+                cudaStream_t st) {
+  if (binned)
+    k_g2p2g<true><<<grid_ctas, kItemMax, item_smem(), st>>>(scenes, item_prefix, nscenes);
+  else
+    k_g2p2g<false><<<grid_ctas, kItemMax, item_smem(), st>>>(scenes, item_prefix, nscenes);
 }
 
 void fast_stats(const SceneDev* sd_dev, int n, StatsSlot* slot, StatsAccum* host, cudaStream_t st) {

@@ -144,13 +144,14 @@ __device__ __forceinline__ void cross3(const float a[3], const float b[3], float
 // diag(s^2) V^T (warm-started Jacobi from the particle's stored frame),
 // W = F V diag(1/s) and G' = W^T dF V, the rotation's differential is
 // dR = W X V^T, X skew with X_ij = (G'_ij - G'_ji) / (s_i + s_j).
-__device__ __forceinline__ bool hess_particle(const SceneDev& S, int p, const float Gm[3][3], P2GParticle& q) {
-  const float vol = S.vv[p].w;
+__device__ __forceinline__ bool hess_particle(const SceneDev& S, int p, bool binned, const float Gm[3][3],
+                                              P2GParticle& q) {
+  const float vol = (binned ? S.bvv : S.vv)[p].w;
   if (!(vol > 0.0f)) return false;
   M3 F;
   float jp;
-  load_fe(S, p, F, jp);
-  const float4 f4 = S.vq[p];
+  load_fe(S, p, F, jp, binned);
+  const float4 f4 = (binned ? S.bvq : S.vq)[p];
   float qv[4] = {f4.x, f4.y, f4.z, f4.w};
   M3 V;
   float lam[3];
@@ -273,7 +274,8 @@ __global__ void __launch_bounds__(kItemMax, 2) k_hess(const SceneDev* __restrict
     const int i = threadIdx.x;
     const bool mine = i < min(it.z, kItemMax);
     float4 xm = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    if (mine) xm = S.xm[it.y + i];
+    const bool binned = particles_binned(S);  // the solve runs before the step's fused kernel
+    if (mine) xm = (binned ? S.bxm : S.xm)[it.y + i];
     stage_wait(sh, S, phase);
     bool have = false;
     P2GParticle q;
@@ -286,7 +288,7 @@ __global__ void __launch_bounds__(kItemMax, 2) k_hess(const SceneDev* __restrict
       all_weights(pg, base, w);
       float Gm[3][3];
       hess_gather(sh, S, bx, by, bz, base, w, Gm);
-      have = hess_particle(S, it.y + i, Gm, q);
+      have = hess_particle(S, it.y + i, binned, Gm, q);
     }
     p2g_tile_pass<kP2gForce>(sh, S, bx, by, bz, have, q, w, base, [&] {
       if (lastw && un < total) stage_issue(sh, scenes[sn].cru, kImpBlockFloats, lane < 27 ? slot : -1);

@@ -283,6 +283,12 @@ snow_status fast_alloc_particles(snow_scene* s, size_t cap) {
       (st = salloc(s, cap, &b.tmp_pid)))
     return st;
   b.n_cap = cap;
+  d.bxm = b.tmp4[0];
+  d.bvv = b.tmp4[1];
+  d.bfa = b.tmp4[2];
+  d.bfb = b.tmp4[3];
+  d.bvq = b.tmp4[4];
+  d.bfc = b.tmp2;
   d.item_cap = (int)(cap / kMinItemMax + std::min<size_t>(cap, (size_t)d.nblocks) + 1);
   if ((st = salloc(s, (size_t)d.item_cap, &d.items))) return st;
   return SNOW_OK;
@@ -343,9 +349,12 @@ int item_ctas(const FastTuning& t) { return num_sms() * t.ctas_per_sm; }
 int grid_ctas() { return num_sms() * 8; }
 
 // Binning: keys, radix sort, permutation, work items, item prefix.
-void fast_bin(snow_scene* s, cudaStream_t st) {
+// in_step: the step's fused kernel follows in the same stream and reads the
+// particles from the binned copies (no copy back); else they are copied back
+// for the per-kernel P2G that follows.
+void fast_bin(snow_scene* s, cudaStream_t st, bool in_step) {
   fast_sort_keys(s->sd, s->sd_dev, s->bin, s->key_bits, st);
-  fast_apply_bins(s->sd, s->sd_dev, s->bin, s->tune.items_max, st);
+  fast_apply_bins(s->sd, s->sd_dev, s->bin, s->tune.items_max, !in_step, st);
   fast_prefix(s->sd_dev, 1, s->d_prefix + 0, s->d_prefix + 2, st);
 }
 
@@ -370,11 +379,11 @@ void fast_enqueue_solve(snow_scene* s, cudaStream_t st) {
 // acc: rigid advance, [binning], grid update, G2P + advance + next P2G.
 void fast_enqueue_step(snow_scene* s, bool bin, cudaStream_t st) {
   fast_begin_step(s->sd_dev, 1, s->ncoll > 0, st);
-  if (bin) fast_bin(s, st);
+  if (bin) fast_bin(s, st, true);
   fast_enqueue_compact(s, st, true);
   fast_enqueue_grid(s, false, st);
   fast_enqueue_solve(s, st);
-  fast_g2p2g(s->sd_dev, s->d_prefix + 0, 1, item_ctas(s->tune), st);
+  fast_g2p2g(s->sd_dev, s->d_prefix + 0, 1, item_ctas(s->tune), bin, st);
 }
 
 snow_status set_dt(snow_scene* s, float dt) {
@@ -457,7 +466,7 @@ snow_status fast_init(snow_scene* s) {
   if (s->sd.crs) fast_implicit_setup();
   if ((r = fast_single_prefix(s))) return r;
   if ((r = push_sd(s))) return r;
-  fast_bin(s, st);
+  fast_bin(s, st, false);
   fast_enqueue_p2g(s, true, st);  // gMassCompute
   // size the output pool from the blocks that received mass
   CK(cudaMemsetAsync(s->sd.counters + CNT_ACTIVE, 0, sizeof(int), st));
@@ -973,7 +982,7 @@ snow_status snow_dispatch(snow_scene* s, int kernel, double dt) {
         fast_enqueue_grid(s, true, st);
       }
       if (s->steps_since_sort >= s->bin_interval) {
-        fast_bin(s, st);
+        fast_bin(s, st, false);
         s->steps_since_sort = 0;
       }
       fast_enqueue_p2g(s, false, st);
@@ -1024,7 +1033,7 @@ snow_status snow_scene_step(snow_scene* s, double dt, int n_steps) {
   if (r) return r;
   if (!s->p2g_ready) {
     // after per-kernel dispatches: bin and scatter the current state first
-    fast_bin(s, st);
+    fast_bin(s, st, false);
     s->steps_since_sort = 0;
     fast_enqueue_p2g(s, false, st);
     s->p2g_ready = true;
@@ -1040,14 +1049,14 @@ snow_status snow_scene_step(snow_scene* s, double dt, int n_steps) {
       cudaEvent_t* ev = ctx->ev;
       CK(cudaEventRecord(ev[0], st));
       fast_begin_step(s->sd_dev, 1, s->ncoll > 0, st);
-      if (bin) fast_bin(s, st);
+      if (bin) fast_bin(s, st, true);
       CK(cudaEventRecord(ev[1], st));
       fast_enqueue_compact(s, st, true);
       fast_enqueue_grid(s, false, st);
       CK(cudaEventRecord(ev[2], st));
       fast_enqueue_solve(s, st);
       CK(cudaEventRecord(ev[3], st));
-      fast_g2p2g(s->sd_dev, s->d_prefix + 0, 1, item_ctas(s->tune), st);
+      fast_g2p2g(s->sd_dev, s->d_prefix + 0, 1, item_ctas(s->tune), bin, st);
       CK(cudaEventRecord(ev[4], st));
       CK(cudaEventSynchronize(ev[4]));
       float t[4];
@@ -1438,12 +1447,12 @@ void batch_enqueue_step(snow_batch* b, int phase, int interval, cudaStream_t st)
     if ((i % interval) == phase) bins.push_back(i);
   snow_ctx* ctx = b->ctx;
   if (bins.size() < 2) {
-    for (int i : bins) fast_bin(b->scenes[i], st);
+    for (int i : bins) fast_bin(b->scenes[i], st, true);
   } else {
     const int lanes = std::min((int)bins.size(), (int)snow_ctx::kAux);
     cudaEventRecord(ctx->fork_ev, st);
     for (int k = 0; k < lanes; k++) cudaStreamWaitEvent(ctx->aux[k], ctx->fork_ev, 0);
-    for (size_t k = 0; k < bins.size(); k++) fast_bin(b->scenes[bins[k]], ctx->aux[k % lanes]);
+    for (size_t k = 0; k < bins.size(); k++) fast_bin(b->scenes[bins[k]], ctx->aux[k % lanes], true);
     for (int k = 0; k < lanes; k++) {
       cudaEventRecord(ctx->join_ev[k], ctx->aux[k]);
       cudaStreamWaitEvent(st, ctx->join_ev[k], 0);
@@ -1457,7 +1466,7 @@ void batch_enqueue_step(snow_batch* b, int phase, int interval, cudaStream_t st)
   if (iters > 0)
     fast_implicit_solve(b->d_scenes, items, active, n, iters, item_ctas(b->scenes[0]->tune), grid_ctas(),
                         b->ctx->d_iter, b->ctx->body_stream, st);
-  fast_g2p2g(b->d_scenes, items, n, item_ctas(b->scenes[0]->tune), st);
+  fast_g2p2g(b->d_scenes, items, n, item_ctas(b->scenes[0]->tune), !bins.empty(), st);
 }
 
 }  // namespace
@@ -1474,7 +1483,7 @@ snow_status snow_batch_step(snow_batch* b, const double* dt, int n_steps) {
     if (s->p2g_ready) continue;  // left behind by per-kernel dispatches: scatter its state first
     snow_status r0 = set_dt(s, dt ? (float)dt[i] : s->last_dt);
     if (r0) return r0;
-    fast_bin(s, st);
+    fast_bin(s, st, false);
     s->steps_since_sort = 0;
     fast_enqueue_p2g(s, false, st);
     s->p2g_ready = true;

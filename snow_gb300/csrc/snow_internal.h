@@ -61,7 +61,8 @@ enum {
   CNT_FALLBACK = 5,   // particles that left their P2G tile (diagnostic, cumulative)
   CNT_TIMEOUT = 6,    // bounded waits that ran out (cumulative)
   CNT_DONE = 7,       // CTAs of the compaction finished (the last forms the prefixes)
-  kCounterStride = 8
+  CNT_BINNED = 8,     // 1: this step's binning left the particles in the binned copies
+  kCounterStride = 9
 };
 
 // Semi-implicit velocity solve: conjugate residuals on the mass-scaled form
@@ -104,6 +105,16 @@ struct SceneDev {
   float2* fc;
   float4* vq;       // FAST: the Jacobi frame (quaternion) of each particle's last SVD
   uint32_t* pid;    // upload index of the particle now stored at each slot
+  // the binning's permuted copies of xm, vv, fa, fb, fc, vq: a binning inside
+  // a step leaves the particles there (counters[CNT_BINNED] = 1), and the
+  // kernels of that step read them from there until the fused kernel, which
+  // writes every particle, has put them back into the streams above
+  const float4* bxm;
+  const float4* bvv;
+  const float4* bfa;
+  const float4* bfb;
+  const float2* bfc;
+  const float4* bvq;
   // blocked grid
   int* blk_slot;    // nblocks: pool slot of the block this step, -1 if inactive
   int* blk_flag;    // nblocks: block received P2G sums since the last compaction
@@ -155,7 +166,10 @@ void fast_grid(const SceneDev* scenes, const int* active_prefix, int nscenes, in
                cudaStream_t st);
 void fast_volume(const SceneDev* sd_dev, int n, cudaStream_t st);
 void fast_g2p_advance(const SceneDev* scenes, const int* item_prefix, int nscenes, int grid_ctas, cudaStream_t st);
-void fast_g2p2g(const SceneDev* scenes, const int* item_prefix, int nscenes, int grid_ctas, cudaStream_t st);
+// binned: some scene of the launch was re-binned in this step (its particles
+// are in its binned copies)
+void fast_g2p2g(const SceneDev* scenes, const int* item_prefix, int nscenes, int grid_ctas, bool binned,
+                cudaStream_t st);
 // The semi-implicit velocity solve between the grid update (which leaves
 // v*, m and u = v* in the solver planes) and G2P: iterations of conjugate
 // residuals (each a K u pass over the items and three passes over the active
@@ -231,7 +245,10 @@ size_t radix_tiles(size_t n);
 // copy of the device descriptor) and leaves the sorted keys in keys[0] and
 // the permutation in vals[0].
 void fast_sort_keys(const SceneDev& sd, const SceneDev* sd_dev, BinScratch& b, int key_bits, cudaStream_t st);
-void fast_apply_bins(const SceneDev& sd, const SceneDev* sd_dev, BinScratch& b, int items_max, cudaStream_t st);
+// copy_back false: the particles stay in the binned copies (CNT_BINNED) for the
+// step's fused kernel; only valid when that kernel follows in the same step.
+void fast_apply_bins(const SceneDev& sd, const SceneDev* sd_dev, BinScratch& b, int items_max, bool copy_back,
+                     cudaStream_t st);
 
 // Radix sort of arbitrary (key, value) pairs; the result lands in k[0]/v[0].
 void radix_sort_pairs(uint32_t* k[2], uint32_t* v[2], size_t n, int key_bits, uint32_t* hist, uint32_t* scan_tmp,

@@ -226,22 +226,27 @@ __global__ void k_permute(const SceneDev* __restrict__ sd, const uint32_t* __res
 }
 
 // Block ranges of the sorted keys and the list of home blocks; also copies
-// the permuted streams back from the scratch copies.
+// the permuted particle ids back, and with copy_back the permuted streams
+// (else the particles stay in the binned copies, flagged by CNT_BINNED, for
+// the step's fused kernel to read and write back).
 __global__ void k_heads(const SceneDev* __restrict__ sd, const uint32_t* __restrict__ keys, int* __restrict__ bstart,
                         int* __restrict__ bend, int* __restrict__ home, const float4* __restrict__ xm,
                         const float4* __restrict__ vv, const float4* __restrict__ fa, const float4* __restrict__ fb,
                         const float2* __restrict__ fc, const uint32_t* __restrict__ pid,
-                        const float4* __restrict__ vq) {
+                        const float4* __restrict__ vq, int copy_back) {
   const SceneDev& S = *sd;
   const int n = S.n;
+  if (!copy_back && blockIdx.x == 0 && threadIdx.x == 0) S.counters[CNT_BINNED] = 1;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    S.xm[i] = xm[i];
-    S.vv[i] = vv[i];
-    S.fa[i] = fa[i];
-    S.fb[i] = fb[i];
-    S.fc[i] = fc[i];
     S.pid[i] = pid[i];
-    S.vq[i] = vq[i];
+    if (copy_back) {
+      S.xm[i] = xm[i];
+      S.vv[i] = vv[i];
+      S.fa[i] = fa[i];
+      S.fb[i] = fb[i];
+      S.fc[i] = fc[i];
+      S.vq[i] = vq[i];
+    }
     const uint32_t b = keys[i] >> 6;
     if (i == 0 || (keys[i - 1] >> 6) != b) {
       bstart[b] = i;
@@ -311,13 +316,14 @@ void fast_sort_keys(const SceneDev& sd, const SceneDev* sd_dev, BinScratch& b, i
   radix_sort_pairs(b.keys, b.vals, (size_t)sd.n, key_bits, b.hist, b.scan_tmp, st, start);
 }
 
-void fast_apply_bins(const SceneDev& sd, const SceneDev* sd_dev, BinScratch& b, int items_max, cudaStream_t st) {
+void fast_apply_bins(const SceneDev& sd, const SceneDev* sd_dev, BinScratch& b, int items_max, bool copy_back,
+                     cudaStream_t st) {
   if (sd.n <= 0) return;
   const size_t n = (size_t)sd.n;
   k_permute<<<grid_for(n, 256, 8), 256, 0, st>>>(sd_dev, b.vals[0], b.tmp4[0], b.tmp4[1], b.tmp4[2], b.tmp4[3],
                                                   b.tmp2, b.tmp_pid, b.tmp4[4]);
   k_heads<<<grid_for(n, 256, 8), 256, 0, st>>>(sd_dev, b.keys[0], b.bstart, b.bend, b.home, b.tmp4[0], b.tmp4[1],
-                                                b.tmp4[2], b.tmp4[3], b.tmp2, b.tmp_pid, b.tmp4[4]);
+                                                b.tmp4[2], b.tmp4[3], b.tmp2, b.tmp_pid, b.tmp4[4], copy_back ? 1 : 0);
   const size_t maxhome = n < (size_t)sd.nblocks ? n : (size_t)sd.nblocks;
   k_items<<<grid_for(maxhome, 256, 4), 256, 0, st>>>(sd_dev, b.bstart, b.bend, b.home, items_max);
 }
