@@ -204,7 +204,8 @@ __global__ void k_keys(const SceneDev* __restrict__ sd, uint32_t* __restrict__ k
 }
 
 // Gathers the particle streams into key order (into the scratch copies;
-// k_heads copies them back) and zeroes the item and home counters.
+// k_heads copies them back, or the step's fused kernel reads them there)
+// and zeroes the item and home counters.
 __global__ void k_permute(const SceneDev* __restrict__ sd, const uint32_t* __restrict__ perm, float4* __restrict__ xm,
                           float4* __restrict__ vv, float4* __restrict__ fa, float4* __restrict__ fb,
                           float2* __restrict__ fc, uint32_t* __restrict__ pid, float4* __restrict__ vq) {
