@@ -166,18 +166,25 @@ __device__ __forceinline__ void collide_hit(const snow_collider& c, const float 
 }
 
 // All colliders in order (half-plane: dot(x - c, n) <= 0; sphere: |x - c| < r).
+// A record is three 16-byte words, (pos, type), (vel, radius), (normal,
+// friction): the test reads the first and the one it needs, the projection
+// the whole record, only for a hit.
 __device__ __forceinline__ void collide(const snow_collider* coll, int ncoll, const float x[3], float v[3]) {
+  static_assert(sizeof(snow_collider) == 48, "three 16-byte words per collider");
   for (int i = 0; i < ncoll; i++) {
-    const snow_collider c = coll[i];
+    const float4* c4 = reinterpret_cast<const float4*>(coll + i);
+    const float4 a = c4[0];
+    const int type = __float_as_int(a.w);
     bool hit = false;
-    if (c.type == 0) {
-      hit = (x[0] - c.pos[0]) * c.normal[0] + (x[1] - c.pos[1]) * c.normal[1] + (x[2] - c.pos[2]) * c.normal[2] <=
-            0.0f;
-    } else if (c.type == 1) {
-      const float d[3] = {x[0] - c.pos[0], x[1] - c.pos[1], x[2] - c.pos[2]};
-      hit = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) < c.radius;
+    if (type == 0) {
+      const float4 nf = c4[2];
+      hit = (x[0] - a.x) * nf.x + (x[1] - a.y) * nf.y + (x[2] - a.z) * nf.z <= 0.0f;
+    } else if (type == 1) {
+      const float r = c4[1].w;
+      const float d[3] = {x[0] - a.x, x[1] - a.y, x[2] - a.z};
+      hit = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) < r;
     }
-    if (hit) collide_hit(c, x, v);
+    if (hit) collide_hit(coll[i], x, v);
   }
 }
 
