@@ -43,12 +43,13 @@ L2_FLUSH_BYTES = 256 << 20
 BYTES_G2P2G = (72 + 128, 16 + 24)
 BYTES_GRID = (0, 40)
 
-# From an ncu capture of the fused kernel on this workload
-# (profiles/k_g2p2g_two_snowballs_1M_256.md), keyed by (particles, grid edge);
-# other workloads report null: DRAM bytes (read + write) per launch, and warp
+# From a one-launch ncu capture of the fused kernel on this workload at the
+# work split named in TRAFFIC_SOURCE, keyed by (particles, grid edge); other
+# workloads report null: DRAM bytes (read + write) per launch, and warp
 # instructions per launch for the issue roofline.
 TRAFFIC_MEASURED = {(1 << 20, 256): 144.1e6}
 INSTRUCTIONS_MEASURED = {(1 << 20, 256): 167.1e6}
+TRAFFIC_SOURCE = "ncu capture of one k_g2p2g launch (sort interval 8, 256 particles per item, 2 CTAs per SM)"
 # warp-instruction issue peak: 152 SMs x 4 schedulers x 2.07 GHz
 ISSUE_PEAK = 152 * 4 * 2.07e9
 # FP32 peak: 152 SMs x 128 lanes x 2 flops per FMA x 2.07 GHz; the algorithmic
@@ -182,13 +183,20 @@ def bench_ours(args, local_rank, barrier=lambda: None):
         tb.close()
         scratch.close()
         sim.set_tuning(tuning["sort_interval"], tuning["items_max"], tuning["ctas_per_sm"])
-    # active grid nodes (nodes with mass) after one step, for the roofline
-    sim.step(dt, 1)
-    ctx.synchronize()
+    # the warm-up starts with a binning step (set_tuning re-bins at the next
+    # step), so the step graphs with and without binning both exist before
+    # the clock starts
+    sim.set_tuning(tuning["sort_interval"], tuning["items_max"], tuning["ctas_per_sm"])
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local_rank}")
     for _ in range(args.warmup):
         sim.step(dt, 1)
     ctx.synchronize()
+    # the timed window starts at a binning point: its first step re-bins, and
+    # so does every sort_interval-th step after it (or every step while
+    # particles leave their tiles), so the window carries at least its share
+    # of the binning cost
+    sim.set_tuning(tuning["sort_interval"], tuning["items_max"], tuning["ctas_per_sm"])
+    binnings0 = sim.phase_times()["binnings"]
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     with ClockSampler(local_rank) as clocks:
@@ -205,6 +213,7 @@ def bench_ours(args, local_rank, barrier=lambda: None):
         barrier()
     step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
     total_ms = sum(step_ms)
+    binnings = sim.phase_times()["binnings"] - binnings0
     st = sim.stats()
     if st["nonfinite"]:
         raise RuntimeError("non-finite particle state in the timed run")
@@ -284,17 +293,14 @@ def bench_ours(args, local_rank, barrier=lambda: None):
     sim2.close()
     del out
 
-    sort_every = tuning["sort_interval"]
     key_bits = math.ceil(math.log2(((args.grid + 3) // 4) ** 3 * 64))
-    launches = 0
-    for i in range(args.steps):
-        launches += kernels_per_step(len(s.colliders), False, key_bits)
-    launches += (args.steps // sort_every) * (kernels_per_step(len(s.colliders), True, key_bits) -
-                                               kernels_per_step(len(s.colliders), False, key_bits))
+    plain_k = kernels_per_step(len(s.colliders), False, key_bits)
+    bin_k = kernels_per_step(len(s.colliders), True, key_bits)
+    launches = args.steps * plain_k + binnings * (bin_k - plain_k)
     res = dict(total_ms=total_ms, step_ms=step_ms, n=n, A=A, per=per, dominant=dominant, alg_bytes=alg_bytes,
                achieved=achieved, peak=peak, peak_kind=peak_kind, clocks=clocks.summary(), e2e_s=e2e_s,
                e2e_steps=e2e_steps, e2e_split=split, h2d=h2d, d2h=d2h_stats + d2h_final / e2e_steps, launches=launches,
-               gen_s=gen_s, stats=st, scene=s, tuning=tuning, check_states=check_states)
+               gen_s=gen_s, stats=st, scene=s, tuning=tuning, check_states=check_states, binnings=binnings)
     ctx.close()
     return res
 
@@ -486,87 +492,115 @@ def cpu_baseline_port(scene, steps=2):
                        f"restatement of the shaders, OpenMP over {threads} threads")
 
 
-def oracle_check(scene, states, tol=1e-5):
-    """One step of the FP64 oracle (EXACT64: no fixed point, no V rounding;
-    OpenMP over the host cores), restarted from the GPU's state after the
-    timed steps, against the GPU's own next step: per-field relative errors
-    of the FAST path on the full workload, with the denominators of the
-    parity tests (x: max(|x|, 1e-3 m); v: max(|v|, 1e-3 m/s, 1e-2 max|v|);
-    F_E: max|F_E| per particle; J_p: |J_p|). The GPU's advance starts from
-    warm SVD frames; only det F_P enters a step, so F_P = diag(J_p, 1, 1)."""
+def _oracle_from_state(scene, y, threads):
+    """The FP64 oracle (EXACT64: no fixed point, no V rounding; OpenMP)
+    restarted from a FAST scene's downloaded state y. Only det F_P enters a
+    step, so F_P = diag(J_p, 1, 1); densities come from the particles'
+    initial volumes. The colliders must be static (their advanced positions
+    are not downloaded)."""
     from oracle import oracle as O
     from snow_gb300 import scenes
 
-    if any(tuple(c.vel) != (0.0, 0.0, 0.0) for c in scene.colliders):
-        return None  # moving colliders: their positions after the run are not carried over
-    y0, y1 = states
-    n = len(y0["x"])
+    n = len(y["x"])
     fp = np.zeros((n, 3, 3))
-    fp[:, 0, 0] = y0["Jp"]
+    fp[:, 0, 0] = y["Jp"]
     fp[:, 1, 1] = fp[:, 2, 2] = 1.0
     s3 = scenes.Scene(**{k: getattr(scene, k) for k in ("grid_pos", "grid_dim", "grid_spacing", "young", "poisson",
                                                         "hardening", "crit_compression", "crit_stretch", "alpha",
                                                         "gravity", "dt")})
     s3.colliders = list(scene.colliders)
-    s3.x, s3.v, s3.m = y0["x"], y0["v"], scene.m.copy()
-    rho = np.where(y0["volume"] > 0, s3.m.astype(np.float64) / np.maximum(y0["volume"], 1e-30), 0.0)
+    s3.x, s3.v, s3.m = y["x"], y["v"], scene.m.copy()
+    rho = np.where(y["volume"] > 0, s3.m.astype(np.float64) / np.maximum(y["volume"], 1e-30), 0.0)
+    o = O.OracleSim(s3, mode=O.EXACT64, vround=False, threads=threads)
+    return o.upload(FE=y["FE"].astype(np.float64), FP=fp).set_density(rho)
+
+
+def _check_report(scene, y0, y1, tol, start):
+    """One FP64 oracle step from y0 against the GPU's next state y1, with the
+    errors of oracle.parity_errors (strict velocity floor 1e-3 m/s, and the
+    FLIP-scale bound for particles stopped within the step)."""
+    from oracle import oracle as O
+
     threads = os.cpu_count() or 1
     t = time.perf_counter()
-    o = O.OracleSim(s3, mode=O.EXACT64, vround=False, threads=threads)
-    o.upload(FE=y0["FE"].astype(np.float64), FP=fp).set_density(rho)
-    o.step()
+    o = _oracle_from_state(scene, y0, threads)
+    flip = o.step_with_flip_scale()
     ref = o.state()
     oracle_s = time.perf_counter() - t
-    x, v = y1["x"].astype(np.float64), y1["v"].astype(np.float64)
-    speed = np.linalg.norm(ref["v"], axis=1)
-    err = {
-        "x": (np.abs(x - ref["x"]) / np.maximum(np.abs(ref["x"]), 1e-3)).max(1),
-        "v": np.linalg.norm(v - ref["v"], axis=1) / np.maximum(speed, max(1e-3, 1e-2 * speed.max())),
-        "FE": np.abs(y1["FE"].astype(np.float64) - ref["FE"]).max((1, 2)) / np.abs(ref["FE"]).max((1, 2)),
-        "Jp": np.abs(y1["Jp"].astype(np.float64) - ref["Jp"]) / np.abs(ref["Jp"]),
-    }
-    worst = max(float(e.max()) for e in err.values())
-    return {"oracle": "EXACT64 (FP64, OpenMP)", "particles": n, "steps": 1, "tolerance": tol,
-            "start": "the workload's state after the timed steps (GPU state, warm SVD frames)",
-            "max": {k: float(e.max()) for k, e in err.items()},
-            "p99": {k: float(np.percentile(e, 99)) for k, e in err.items()},
-            "median": {k: float(np.median(e)) for k, e in err.items()},
-            "within_tolerance": bool(worst <= tol), "oracle_s": oracle_s, "threads": threads}
+    e = O.parity_errors(y1, ref, flip)
+    bound = max(e["max"][k] for k in ("x", "v_flip", "FE", "Jp"))
+    stopped = int(np.count_nonzero(np.linalg.norm(np.asarray(y1["v"], np.float64) - ref["v"], axis=1) >
+                                   tol * np.maximum(np.linalg.norm(ref["v"], axis=1), 1e-3)))
+    return {"oracle": "EXACT64 (FP64, OpenMP)", "particles": len(y0["x"]), "steps": 1, "tolerance": tol,
+            "start": start, "max": e["max"], "p99": e["p99"], "median": e["median"],
+            "within_tolerance": bool(bound <= tol), "strict_v_within_tolerance": bool(e["max"]["v"] <= tol),
+            "particles_above_strict_v": stopped, "v_worst": e["v_worst"], "oracle_s": oracle_s,
+            "threads": threads}
+
+
+def oracle_check(scene, states, tol=1e-5):
+    """The FAST path on the full timed workload: one FP64 oracle step,
+    restarted from the GPU's state after the timed steps, against the GPU's
+    own next step (per-field relative errors; the GPU's advance starts from
+    warm SVD frames)."""
+    if any(tuple(c.vel) != (0.0, 0.0, 0.0) for c in scene.colliders):
+        return None  # moving colliders: their positions after the run are not carried over
+    y0, y1 = states
+    return _check_report(scene, y0, y1, tol,
+                         "the workload's state after the timed steps (GPU state, warm SVD frames)")
+
+
+def oracle_check_batched_at_scale(local_rank, n=2_097_152, edge=384, warm=3, tol=1e-5):
+    """The batched path at the size of the 16-scene batch's scenes: a snow
+    block of n particles on a 384^3 grid, its bottom layer resting in a
+    static sphere collider and moving down at 2 m/s, stepped by
+    snow_batch_step together with a small scene, `warm` batched steps and
+    then one more, which the FP64 oracle repeats from the GPU's state."""
+    import torch
+
+    from snow_gb300 import api, scenes
+
+    torch.cuda.set_device(local_rank)
+    t0 = time.perf_counter()
+    big = scenes.snow_block_on_sphere(0x5EED0014, n, edge, gap=-0.01, v0=(0.0, -2.0, 0.0))
+    small = scenes.small_scene(n=20000, grid_edge=64, seed=0x5EED0015, v0=(1.0, -2.0, 0.5))
+    gen_s = time.perf_counter() - t0
+    ctx = api.Context(local_rank)
+    sims = [api.SimScene(ctx, s).upload().init() for s in (big, small)]
+    batch = api.Batch(ctx, sims)
+    dts = [big.dt, small.dt]
+    batch.step(warm, dts)
+    y0 = sims[0].download()
+    batch.step(1, dts)
+    y1 = sims[0].download()
+    batch.close()
+    for g in sims:
+        g.close()
+    ctx.close()
+    r = _check_report(big, y0, y1, tol, f"after {warm} batched steps (GPU state, warm SVD frames)")
+    r.update(workload=f"snow block of {big.n} particles on a {edge}^3 grid, bottom layer inside a static sphere "
+                      f"collider (radius {big.colliders[-1].radius:.4f}), moving at 2 m/s, stepped by "
+                      f"snow_batch_step beside a 20,000-particle scene", scene_generation_s=gen_s)
+    return r
 
 
 def bench_reference(args):
-    """The reference's compute shaders compiled as C++ on the host cores.
-    Each timed step advances a particle sample of the workload's scene; the
-    full-scene rate is extrapolated from the measured per-step grid sweep
-    (a step with no particles) and the per-particle cost."""
+    """The reference's compute shaders compiled as C++ (oracle/_ref), or the
+    oracle's FP32 restatement where they are not built, on all host cores:
+    every warm-up and timed step advances the workload's whole scene (all
+    particles, the dense grid), as ExplicitTimeUpdate::update does."""
     from oracle import oracle as O
     from snow_gb300 import scenes
 
     threads = os.cpu_count() or 1
     s = scenes.cfg2_two_snowballs(n=args.particles, grid_edge=args.grid)
-    rng = np.random.default_rng(7)
-    k = max(1, min(s.n, args.ref_sample))
-    idx = np.sort(rng.choice(s.n, size=k, replace=False))
-    sample = scenes.Scene(**{f: getattr(s, f) for f in ("grid_pos", "grid_dim", "grid_spacing", "young", "poisson",
-                                                        "hardening", "crit_compression", "crit_stretch", "alpha",
-                                                        "gravity", "dt", "colliders")})
-    sample.x, sample.v, sample.m = s.x[idx], s.v[idx], s.m[idx]
     kind = "reference" if O.ref_lib() is not None else "port"
     if kind == "reference":
-        sim = O.RefSim(sample, threads=threads).upload_std140(*sample.std140()).init()
+        sim = O.RefSim(s, threads=threads).upload_std140(*s.std140()).init()
         stepper = lambda: sim.update()
-        empty = scenes.Scene(**{f: getattr(sample, f) for f in ("grid_pos", "grid_dim", "grid_spacing", "young",
-                                                                 "poisson", "hardening", "crit_compression",
-                                                                 "crit_stretch", "alpha", "gravity", "dt",
-                                                                 "colliders")})
-        empty.x, empty.v, empty.m = sample.x[:1], sample.v[:1], sample.m[:1]
-        esim = O.RefSim(empty, threads=threads).upload_std140(*empty.std140()).init()
-        estep = lambda: esim.update()
     else:
-        sim = O.OracleSim(sample, mode=O.FAITHFUL32, threads=threads).upload_std140(*sample.std140()).init()
+        sim = O.OracleSim(s, mode=O.FAITHFUL32, threads=threads).upload_std140(*s.std140()).init()
         stepper = lambda: sim.step()
-        empty = None
-        estep = None
     for _ in range(args.warmup):
         stepper()
     times = []
@@ -574,22 +608,15 @@ def bench_reference(args):
         t = time.perf_counter()
         stepper()
         times.append(time.perf_counter() - t)
-    t_sample = statistics.median(times)
-    t_grid = 0.0
-    if estep is not None:
-        et = []
-        for _ in range(3):
-            t = time.perf_counter()
-            estep()
-            et.append(time.perf_counter() - t)
-        t_grid = min(et)
-    per_particle = max(t_sample - t_grid, 1e-12) / k
-    t_full = t_grid + per_particle * s.n
-    value = s.n / t_full
-    sample_desc = (f"{k} of {s.n} particles of the workload scene per step ({args.steps} timed steps, "
-                   f"median {t_sample:.3f} s); full-scene rate extrapolated as N / (T_grid + N * t_particle) "
-                   f"with T_grid = {t_grid:.3f} s measured on a 1-particle step")
-    return dict(value=value, unit=UNIT, cores=threads, kind=kind, sample=sample_desc, t_sample=t_sample)
+    total = sum(times)
+    value = s.n * args.steps / total
+    what = ("the reference's compute shaders compiled as C++" if kind == "reference"
+            else "the oracle's FP32 restatement of the shaders")
+    sample_desc = (f"the whole {s.n}-particle scene ({args.grid}^3 grid) every step: {args.warmup} warm-up + "
+                   f"{args.steps} timed steps of {what}, OpenMP over {threads} threads; "
+                   f"median {statistics.median(times):.3f} s per step")
+    return dict(value=value, unit=UNIT, cores=threads, kind=kind, sample=sample_desc, total_s=total,
+                ms_per_step=1e3 * total / args.steps)
 
 
 def bench_implicit(args, local_rank):
@@ -638,8 +665,7 @@ def bench_implicit(args, local_rank):
         ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends)) / args.steps
         r = dict(ms_per_step=ms, value=s.n / (ms * 1e-3), clocks=clocks.summary())
         if beta > 0:
-            # CR iterations of the steps that follow (per-kernel times of the
-            # solve: profiles/implicit_solve_two_snowballs_1M_256.md)
+            # CR iterations of the steps that follow
             its = []
             for _ in range(4):
                 sim.step(dt, 1)
@@ -692,8 +718,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--particles", type=int, default=1 << 20)
     ap.add_argument("--grid", type=int, default=256)
-    ap.add_argument("--ref-sample", type=int, default=32768)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-scale-check", action="store_true",
+                    help="skip the oracle check of a batched step of a 2M-particle, 384^3 scene")
     ap.add_argument("--tuning", default="", help="SORT_INTERVAL,ITEMS_MAX,CTAS_PER_SM instead of autotuning")
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=16)
@@ -718,7 +745,7 @@ def main():
             return 0
         r = bench_reference(args)
         line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": 1e3 * args.particles / r["value"], "higher_is_better": True,
+                "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32+i32", "data": "synthetic",
                 "config": dict(workload_config(args), mode="the reference compute shaders compiled as C++ (FP32 + int32 fixed point)", l2="n/a (host)"), "impl": "reference",
                 "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": r["cores"], "kind": r["kind"],
@@ -784,6 +811,7 @@ def main():
                      "peak_source": res["peak_kind"],
                      "traffic": (TRAFFIC_MEASURED.get((args.particles, args.grid))
                                  if res["dominant"] == "g2p2g" else None),
+                     "traffic_source": TRAFFIC_SOURCE,
                      "algorithmic_bytes_per_launch": res["alg_bytes"], "active_nodes": res["A"]},
         "issue_roofline": ({"achieved": INSTRUCTIONS_MEASURED[(args.particles, args.grid)] /
                                         (res["per"]["g2p2g"] * 1e-3),
@@ -814,9 +842,13 @@ def main():
         line["serving"] = bench_serving(args, local_rank)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_port(res["scene"], steps=2)
-        # the same leg checks the timed workload's next step against the oracle
+        # the same leg checks the timed workload's next step against the
+        # oracle, and one batched step at the size of the 16-scene batch's
+        # scenes
         if res["check_states"] is not None:
             line["oracle_check"] = oracle_check(res["scene"], res["check_states"])
+        if not args.no_scale_check:
+            line["oracle_check_batched_at_scale"] = oracle_check_batched_at_scale(local_rank)
     print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()

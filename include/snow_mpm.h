@@ -127,10 +127,12 @@ typedef struct snow_stats {
 } snow_stats;
 
 /* Device-timed phases of snow_scene_step when profiling is on (ms, summed
- * over steps since the last reset). */
+ * over steps since the last reset). `binnings` counts the steps that
+ * re-binned the particles (profiling on or off). */
 typedef struct snow_phase_times {
   double sort_ms, p2g_ms, grid_ms, g2p_ms, other_ms, total_ms;
   uint64_t steps;
+  uint64_t binnings;
 } snow_phase_times;
 
 typedef struct snow_ctx snow_ctx;
@@ -192,6 +194,22 @@ snow_status snow_scene_init(snow_scene* s);
  * particles at once. CUDA errors surface at the next call that synchronises
  * (download, stats, snow_ctx_synchronize). */
 snow_status snow_scene_step(snow_scene* s, double dt, int n_steps);
+/* Waits for the scene's queued work and returns the first condition its
+ * device counters hold (SNOW_ETIMEDOUT, SNOW_ECAPACITY, SNOW_ENUMERIC) or
+ * SNOW_OK: the same checks snow_scene_step makes at its re-binning points,
+ * at once. (No counterpart in the reference, which reports no errors.) */
+snow_status snow_scene_check(snow_scene* s);
+/* Bounded waits of the FAST kernels. A work item's wait for the bulk copies
+ * of its grid tile into shared memory gives up after `wait_ns` nanoseconds
+ * of the GPU's global timer (0 = the default, one second): the CTA stops
+ * without reading the tile, waits once more (bounded) for copies still in
+ * flight, and returns; the scene's next check returns SNOW_ETIMEDOUT and its
+ * state is no longer a valid step (the context stays usable). `unsent_bytes`
+ * is 0 in normal use: a positive value makes every such wait expect that
+ * many bytes more than its copies deliver, so that the wait runs out, to
+ * test this path (at most 65536). FAST mode only. (No counterpart in the
+ * reference.) */
+snow_status snow_scene_set_wait_limit(snow_scene* s, uint32_t wait_ns, uint32_t unsent_bytes);
 /* One kernel of the step (per-kernel parity checks). In SNOW_MODE_FAST the
  * gather and the particle update are one kernel: SNOW_K_G2P runs both and
  * SNOW_K_P_ADVANCE does nothing; SNOW_K_G_RESET does nothing (the block pool
@@ -327,9 +345,11 @@ snow_status snow_server_drain(snow_server* srv, double timeout_s);
  * Sorts n 32-bit keys (device memory, `key_bits` significant low bits,
  * 1..32) stably: sorted_keys receives the keys in ascending order and perm[i]
  * the input index of the i-th smallest key (ties keep input order, as
- * std::stable_sort). `keys` may alias `sorted_keys`. The work is queued on
- * `stream` (a cudaStream_t; NULL = the default stream) and the call returns
- * without waiting.
+ * std::stable_sort). `keys` may be the same array as `sorted_keys` (sorted
+ * in place); any other overlap between the three arrays, including `perm`
+ * sharing memory with either key array, returns SNOW_EINVAL and queues
+ * nothing. The work is queued on `stream` (a cudaStream_t; NULL = the
+ * default stream) and the call returns without waiting.
  *
  * Scratch lives in one fixed device array inside the library, sized for
  * SNOW_SORT_STATIC_MAX_KEYS keys (about 2.1 MB, held by every GPU that loads
@@ -337,9 +357,10 @@ snow_status snow_server_drain(snow_server* srv, double timeout_s);
  * SNOW_EINVAL and queues nothing. All calls share the array, so calls whose
  * work overlaps on the GPU (other streams, other host threads) race and must
  * be ordered by the caller; every pass overwrites the scratch it reads, so
- * nothing carried over from an earlier call needs clearing. The first call on
- * a device looks up the array's device address; make that first call before
- * any stream capture. Returns SNOW_ECUDA if a CUDA call fails. */
+ * nothing carried over from an earlier call needs clearing. The first call in
+ * a device context (and the first after that device's context was reset)
+ * looks up the array's device address; make that first call before any
+ * stream capture. Returns SNOW_ECUDA if a CUDA call fails. */
 snow_status snow_sort_keys_static(const uint32_t* keys, uint32_t* sorted_keys, uint32_t* perm, size_t n,
                                   int key_bits, void* stream);
 
@@ -357,10 +378,12 @@ typedef struct snow_tuning {
   int steps_taken;     /* autotune: steps the batch advanced while timing */
   double ms_per_step;  /* autotune: measured time per step of the choice */
 } snow_tuning;
-/* Applies a tuning to one FAST scene; takes effect at its next re-binning. */
+/* Applies a tuning to one FAST scene; the scene's next step re-bins its
+ * particles with it (and so starts a new re-binning interval). */
 snow_status snow_scene_set_tuning(snow_scene* s, const snow_tuning* t);
 /* Applies a tuning to every scene of the batch (e.g. one kept from an
- * earlier autotune); takes effect at each scene's next re-binning. */
+ * earlier autotune); the batch's next step starts the re-binning cycle
+ * again (scene i re-bins at cycle step i mod sort_interval). */
 snow_status snow_batch_set_tuning(snow_batch* b, const snow_tuning* t);
 /* Times candidate tunings (sort interval 1/2/4/8/12/16/24/32 x 128/256 particles per work
  * item x 1/2 CTAs per SM) on real steps of the batch and keeps the fastest;

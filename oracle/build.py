@@ -16,7 +16,9 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-REFERENCE_TREE = "/root/reference"
+# The reference tree whose shaders are translated: $SNOW_REFERENCE_TREE, else
+# the read-only checkout this recipe was written against.
+REFERENCE_TREE = os.environ.get("SNOW_REFERENCE_TREE", "/root/reference")
 
 CXXFLAGS = ["-O2", "-std=gnu++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-fno-strict-aliasing"]
 

@@ -57,6 +57,7 @@ def lib():
         _lib.oracle_hessian.argtypes = [C.c_void_p, dp, dp]
         _lib.oracle_force_at.argtypes = [C.c_void_p, dp, C.c_double, dp]
         _lib.oracle_solver_report.argtypes = [C.c_void_p, dp]
+        _lib.oracle_flip_scale.argtypes = [C.c_void_p, dp]
     return _lib
 
 
@@ -189,6 +190,18 @@ class OracleSim:
 
     def phase(self, which, dt=None):
         self.L.oracle_phase(self.h, int(which), float(self.scene.dt if dt is None else dt))
+
+    def step_with_flip_scale(self, dt=None):
+        """One step (the phases of step()), returning per particle the
+        magnitude scale of its FLIP velocity update taken between the grid
+        update and G2P: alpha |v_p| + sum_i w_ip (|v*_i| + alpha |p_i/m_i|)."""
+        for ph in (PH_RIGID, PH_RESET, PH_P2G, PH_GRID, PH_IMPLICIT):
+            self.phase(ph, dt)
+        out = np.zeros(self.n)
+        self.L.oracle_flip_scale(self.h, _p(out, C.c_double))
+        for ph in (PH_G2P, PH_ADVANCE):
+            self.phase(ph, dt)
+        return out
 
     def state(self):
         n = self.n
@@ -360,3 +373,42 @@ def cell_keys(x, grid_pos, grid_dim, h):
     lib().oracle_cell_keys(_p(x, C.c_float), n, _p(gp, C.c_float), _p(gd, C.c_int), float(np.float32(h)),
                            _p(lin, C.c_uint32), _p(blk, C.c_uint32), _p(perm, C.c_uint32))
     return lin, blk, perm
+
+
+def parity_errors(got, ref, flip_scale=None):
+    """Per-particle relative errors of a single-precision state `got` against
+    an oracle state `ref` (dicts with x, v, FE, Jp), as the parity tests and
+    the benchmark's full-size check report them:
+
+      x       |dx| / max(|x|, 1e-3 m)
+      v       |dv| / max(|v|, 1e-3 m/s)                  (the strict floor)
+      v_flip  |dv| / max(|v|, 1e-3 m/s, S_p)             (needs flip_scale)
+      FE      max|dF_E| / max|F_E| per particle
+      Jp      |dJ_p| / |J_p|
+
+    S_p = alpha |v_p| + sum_i w_ip (|v*_i| + alpha |p_i/m_i|) is the size of
+    the terms the FLIP update v' = alpha v_p + sum_i w_ip (v*_i - alpha
+    p_i/m_i) adds up (OracleSim.step_with_flip_scale). A particle that a
+    collider or the snow around it stops within the step has |v'| << S_p;
+    any single-precision evaluation of the update resolves v' only to a few
+    ulps of S_p there, so for such particles the strict floor cannot be met
+    and v_flip is the bound that FP32 arithmetic allows.
+    Returns the max, p99 and median of each and the worst particle's data."""
+    x, v = np.asarray(got["x"], np.float64), np.asarray(got["v"], np.float64)
+    speed = np.linalg.norm(ref["v"], axis=1)
+    dv = np.linalg.norm(v - ref["v"], axis=1)
+    err = {
+        "x": (np.abs(x - ref["x"]) / np.maximum(np.abs(ref["x"]), 1e-3)).max(1),
+        "v": dv / np.maximum(speed, 1e-3),
+        "FE": np.abs(np.asarray(got["FE"], np.float64) - ref["FE"]).max((1, 2)) / np.abs(ref["FE"]).max((1, 2)),
+        "Jp": np.abs(np.asarray(got["Jp"], np.float64) - ref["Jp"]) / np.abs(ref["Jp"]),
+    }
+    if flip_scale is not None:
+        err["v_flip"] = dv / np.maximum(np.maximum(speed, 1e-3), flip_scale)
+    out = {"max": {k: float(e.max()) for k, e in err.items()},
+           "p99": {k: float(np.percentile(e, 99)) for k, e in err.items()},
+           "median": {k: float(np.median(e)) for k, e in err.items()}}
+    w = int(np.argmax(err["v"]))
+    out["v_worst"] = {"ref": ref["v"][w].tolist(), "got": v[w].tolist(), "x": ref["x"][w].tolist(),
+                      "flip_scale": None if flip_scale is None else float(flip_scale[w])}
+    return out

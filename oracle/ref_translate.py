@@ -39,7 +39,9 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-DEFAULT_REF = "/root/reference"
+# The reference tree: --reference DIR, else $SNOW_REFERENCE_TREE, else the
+# read-only checkout this recipe was written against.
+DEFAULT_REF = os.environ.get("SNOW_REFERENCE_TREE", "/root/reference")
 SHADERS = [
     "gReset", "rigidAdvance", "gMassCompute", "pVolumeCompute",
     "p2gTransfer", "gForceCompute", "g2pTransfer", "particleAdvance",

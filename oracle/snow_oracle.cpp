@@ -354,6 +354,12 @@ struct OracleBase {
   virtual void hessian(const double* u, double* out) const = 0;
   virtual void force_at(const double* u, double eps, double* out) const = 0;
   virtual void solver_report(double* out) const = 0;
+  // Per particle, the magnitude scale of its FLIP velocity update from the
+  // current grid (after the grid phase, before G2P): alpha |v_p| +
+  // sum_i w_ip (|v*_i| + alpha |p_i / m_i|) over stencil nodes with mass.
+  // The update v' = alpha v_p + sum_i w_ip (v*_i - alpha p_i / m_i) sums
+  // terms of these sizes, so a float result is resolved only to ~1e-7 of it.
+  virtual void flip_scale(double* out) const = 0;
 };
 
 enum {
@@ -1049,6 +1055,34 @@ struct Oracle : OracleBase {
       gvn[g] = sq[g] > R(0) ? collide(node_pos(g), smul(isq[g], y[g])) : v3<R>(0, 0, 0);
   }
 
+  void flip_scale(double* out) const override {
+#pragma omp parallel for schedule(dynamic, 256) num_threads(threads) if (par())
+    for (long long pl = 0; pl < (long long)N; pl++) {
+      const size_t p = (size_t)pl;
+      const V3<R> pg = particle_in_grid(p);
+      const int base[3] = {(int)pg[0], (int)pg[1], (int)pg[2]};
+      const V3<R> vp = vel(p);
+      double sc = double(alpha) * std::sqrt(double(vp[0] * vp[0] + vp[1] * vp[1] + vp[2] * vp[2]));
+      for (int y = 0; y < 64; y++) {
+        int o[3];
+        neighbour_offset(y, o);
+        const int g[3] = {base[0] + o[0], base[1] + o[1], base[2] + o[2]};
+        if (!in_grid(g)) continue;
+        const size_t gI = node_index(g);
+        const R mi = node_mass(gI);
+        if (!(mi > R(0))) continue;
+        const V3<R> d = v3<R>(R(g[0]) - pg[0], R(g[1]) - pg[1], R(g[2]) - pg[2]);
+        const double w = double(weight3(d));
+        const V3<R> vs = gvn[gI];
+        const V3<R> vo = divs(node_mom(gI), mi);
+        const double a = std::sqrt(double(vs[0] * vs[0] + vs[1] * vs[1] + vs[2] * vs[2]));
+        const double b = std::sqrt(double(vo[0] * vo[0] + vo[1] * vo[1] + vo[2] * vo[2]));
+        sc += w * (a + double(alpha) * b);
+      }
+      out[p] = sc;
+    }
+  }
+
   void phase(int which, double dt_d) override {
     const R dt = R(float(dt_d));
     switch (which) {
@@ -1232,6 +1266,7 @@ void oracle_force_at(void* h, const double* u, double eps, double* out) {
 // (iterations, final relative residual, initial relative residual) of the
 // last solve.
 void oracle_solver_report(void* h, double* out) { static_cast<OracleBase*>(h)->solver_report(out); }
+void oracle_flip_scale(void* h, double* out) { static_cast<OracleBase*>(h)->flip_scale(out); }
 
 // 3x3 SVD of row-major matrices (KAT / property tests): A = W S V^T.
 void oracle_svd(const double* a, double* w, double* s, double* vmat, int n, int fp64, int vround) {

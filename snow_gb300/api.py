@@ -242,7 +242,18 @@ class SimScene:
         t = N.SnowPhaseTimes()
         self.ctx.check(self.L.snow_scene_phase_times(self.h, C.byref(t), int(bool(reset))))
         return dict(sort_ms=t.sort_ms, p2g_ms=t.p2g_ms, grid_ms=t.grid_ms, g2p_ms=t.g2p_ms,
-                    solve_ms=t.other_ms, total_ms=t.total_ms, steps=int(t.steps))
+                    solve_ms=t.other_ms, total_ms=t.total_ms, steps=int(t.steps), binnings=int(t.binnings))
+
+    def check(self):
+        """Waits for the queued work; raises SnowError for a condition the
+        device counted (timeout, pool overflow, non-finite state)."""
+        self.ctx.check(self.L.snow_scene_check(self.h))
+        return self
+
+    def set_wait_limit(self, wait_ns: int = 0, unsent_bytes: int = 0):
+        """Bounded copy waits of the FAST kernels (snow_scene_set_wait_limit)."""
+        self.ctx.check(self.L.snow_scene_set_wait_limit(self.h, int(wait_ns), int(unsent_bytes)))
+        return self
 
     def solver_report(self) -> dict:
         """The last step's semi-implicit solve (iterations, relative residuals)."""

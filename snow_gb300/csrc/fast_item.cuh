@@ -32,7 +32,6 @@ constexpr int kPd = 11;  // float4 per particle of P2G data in shared memory: 10
                          // the stride to 44 words so the 8 threads of a 16-byte store phase hit 8
                          // distinct groups of 4 banks
 constexpr int kShColliders = 16;  // colliders cached in shared memory
-constexpr uint32_t kWaitPolls = 1u << 24;
 
 __device__ __forceinline__ int find_scene(const int* __restrict__ prefix, int nscenes, long long u) {
   int lo = 0, hi = nscenes;
@@ -311,6 +310,7 @@ struct ItemShared {
   int4 item_q[2];                    // this and the next work item of the CTA
   int scene_q[2];                    // ... and their scenes
   int coll_scene;                    // scene whose colliders sit in coll
+  int abort;                         // 1 + parity of a copy wait that ran out, else 0
   uint64_t bar;
   snow_collider coll[kShColliders];
   float4 chit[kShColliders];         // packed hit tests of the colliders
@@ -342,15 +342,17 @@ __device__ __forceinline__ int tile_slot(const SceneDev& S, int4 it, int k) {
 // One full warp issues the bulk copies (TMA) of the tile's pool blocks into
 // `stage` (lane k < 27 copies block k, `block_floats` floats from pool slot
 // `slot` of `pool`; block_floats <= 384 and a multiple of 4) and zero-fills
-// the blocks without a slot; completion lands on sh.bar. The caller
-// guarantees nobody reads `stage` until the barrier's phase completes and
-// that all earlier reads of `stage` are done.
-__device__ __forceinline__ void stage_issue(ItemShared& sh, const float* pool, int block_floats, int slot) {
+// the blocks without a slot; completion lands on sh.bar, which expects
+// `unsent` bytes more than are copied (0 except in tests of the timeout
+// path). The caller guarantees nobody reads `stage` until the barrier's
+// phase completes and that all earlier reads of `stage` are done.
+__device__ __forceinline__ void stage_issue(ItemShared& sh, const float* pool, int block_floats, int slot,
+                                            uint32_t unsent) {
   const int k = threadIdx.x & 31;
   const bool mine = k < 27 && slot >= 0;
   const uint32_t bytes = (uint32_t)(block_floats * sizeof(float));
   const uint32_t valid = __ballot_sync(0xffffffffu, mine);
-  if (k == 0) mbar_arrive_expect_tx(&sh.bar, __popc(valid) * bytes);
+  if (k == 0) mbar_arrive_expect_tx(&sh.bar, __popc(valid) * bytes + unsent);
   __syncwarp();
   if (mine) {
     fence_proxy_async_smem();
@@ -366,17 +368,32 @@ __device__ __forceinline__ void stage_issue(ItemShared& sh, const float* pool, i
 }
 // ... of the grid update's output (v*, d).
 __device__ __forceinline__ void stage_issue(ItemShared& sh, const SceneDev& S, int slot) {
-  stage_issue(sh, S.gout, kOutBlockFloats, slot);
+  stage_issue(sh, S.gout, kOutBlockFloats, slot, S.tx_unsent);
 }
 
-// Every thread waits for the stage copies of the current phase (bounded; a
-// copy that never lands is counted and the kernel carries on).
-__device__ __forceinline__ void stage_wait(ItemShared& sh, const SceneDev& S, uint32_t& phase) {
-  if (!mbar_wait(&sh.bar, phase, kWaitPolls)) {
-    if (threadIdx.x == 0) atomicAdd(&S.counters[CNT_TIMEOUT], 1);
-    mbar_wait(&sh.bar, phase, kWaitPolls);
+// Every thread waits for the stage copies of the current phase, at most
+// S.wait_ns. Returns false if the wait ran out; the thread then records the
+// phase in sh.abort (1 + parity), and the CTA stops at its next barrier that
+// checks it (stage_abort) without reading the stage.
+__device__ __forceinline__ bool stage_wait(ItemShared& sh, const SceneDev& S, uint32_t& phase) {
+  if (!mbar_wait(&sh.bar, phase, S.wait_ns)) {
+    sh.abort = 1 + (int)phase;
+    return false;
   }
   phase ^= 1u;
+  return true;
+}
+
+// The end of a CTA whose copy wait ran out (every thread calls it, after a
+// barrier that made sh.abort visible): the timeout is counted once (the host
+// returns SNOW_ETIMEDOUT) and thread 0 gives the copies still in flight one
+// more bounded wait, so the CTA does not exit while bulk copies into its
+// shared memory may still land. Issues no copies.
+__device__ __forceinline__ void stage_abort(ItemShared& sh, const SceneDev& S) {
+  if (threadIdx.x == 0) {
+    atomicAdd(&S.counters[CNT_TIMEOUT], 1);
+    mbar_wait(&sh.bar, (uint32_t)(sh.abort - 1), S.wait_ns);
+  }
 }
 
 // Colliders of scene S into shared memory (when they fit). Ends with
@@ -412,7 +429,10 @@ __device__ __forceinline__ void tile_zero(ItemShared& sh, int nf) {
 __device__ __forceinline__ void tile_init(ItemShared& sh) {
   for (int i = threadIdx.x; i < kCells; i += blockDim.x) sh.ccount[i] = 0;
   if (threadIdx.x == 32) sh.nrows = 0;
-  if (threadIdx.x == 0) mbar_init(&sh.bar, 1);
+  if (threadIdx.x == 0) {
+    mbar_init(&sh.bar, 1);
+    sh.abort = 0;
+  }
   __syncthreads();
 }
 
@@ -692,8 +712,11 @@ __device__ __forceinline__ int cell_row_node(int ci, int b, int c) {
 //      flush from the next item's use of the tile with a barrier.
 // `between` runs between steps 3 and 4, long after the staged G2P tile was
 // last read (the fused kernel issues the next item's copies there).
+// Returns false (at its first barrier, before any shared or global write
+// beyond the cell counts and fall-back scatters) when a copy wait of the CTA
+// ran out (sh.abort): the caller then stops the CTA.
 template <int KIND, class Between>
-__device__ __forceinline__ void p2g_tile_pass(ItemShared& sh, const SceneDev& S, int bx, int by, int bz, bool have,
+__device__ __forceinline__ bool p2g_tile_pass(ItemShared& sh, const SceneDev& S, int bx, int by, int bz, bool have,
                                               const P2GParticle& q, const AxisW& w, const int base[3],
                                               Between between) {
   constexpr int nf = P2gFields<KIND>::nf;
@@ -713,6 +736,7 @@ __device__ __forceinline__ void p2g_tile_pass(ItemShared& sh, const SceneDev& S,
     }
   }
   __syncthreads();  // counts done
+  if (sh.abort) return false;  // a copy wait ran out
   if (threadIdx.x == 32) sh.nrows = 0;  // the previous item's flush is long done
   // exclusive scan of the cell counts and list of the occupied cells, one
   // cell per thread
@@ -857,6 +881,7 @@ __device__ __forceinline__ void p2g_tile_pass(ItemShared& sh, const SceneDev& S,
       if (flag) S.blk_flag[blk] = 1;
     }
   }
+  return true;
 }
 }  // namespace
 }  // namespace snow

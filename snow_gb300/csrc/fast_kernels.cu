@@ -76,15 +76,6 @@ __global__ void k_gather_counters(const SceneDev* __restrict__ scenes, int nscen
   __threadfence_system();
 }
 
-__global__ void k_count_flags(const SceneDev* __restrict__ sd, int nblocks) {
-  int c = 0;
-  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nblocks; b += gridDim.x * blockDim.x)
-    c += sd->blk_flag[b] != 0;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
-  if ((threadIdx.x & 31) == 0 && c) atomicAdd(&sd->counters[CNT_ACTIVE], c);
-}
-
 // Flags -> active-block list and pool slots (one thread per block); the CTA
 // that finishes last forms the item and active-block prefixes.
 __global__ void k_compact(const SceneDev* __restrict__ scenes, const int* __restrict__ block_prefix, int nscenes,
@@ -258,6 +249,11 @@ __global__ void __launch_bounds__(kItemMax) k_g2p_advance(const SceneDev* __rest
     if (threadIdx.x < 32) stage_issue(sh, S, tile_slot(S, it, threadIdx.x));
     load_colliders(sh, S);
     stage_wait(sh, S, phase);
+    __syncthreads();
+    if (sh.abort) {
+      stage_abort(sh, S);
+      return;
+    }
     for (int i = threadIdx.x; i < it.z; i += blockDim.x) {
       const int p = it.y + i;
       const PState ps = load_state(S, p, false);  // per-kernel dispatches: binned in place
@@ -336,12 +332,12 @@ __global__ void __launch_bounds__(kItemMax, 2) k_g2p2g(const SceneDev* __restric
     PState ps;
     const bool binned = BINNED && particles_binned(S);
     if (mine) ps = load_state(S, p, binned);
-    stage_wait(sh, S, phase);
+    const bool landed = stage_wait(sh, S, phase);
     bool have = false;
     P2GParticle q;
     AxisW wn;
     int nbase[3] = {0, 0, 0};
-    if (mine) {
+    if (mine && landed) {
       float pg[3];
       int base[3];
       grid_coords(S, ps.xm, pg, base);
@@ -366,15 +362,21 @@ __global__ void __launch_bounds__(kItemMax, 2) k_g2p2g(const SceneDev* __restric
         all_weights(npg, nbase, wn);
       }
     }
-    p2g_tile_pass<kP2gFull>(sh, S, bx, by, bz, have, q, wn, nbase, [&] {
-      if (lastw && un < total) {
-        if (lane == 0) {
-          sh.item_q[par ^ 1] = itn;
-          sh.scene_q[par ^ 1] = sn;
-        }
-        stage_issue(sh, scenes[sn], lane < 27 ? slot : -1);
-      }
-    });
+    const bool done = p2g_tile_pass<kP2gFull>(
+        sh, S, bx, by, bz, have, q, wn, nbase,
+        [&] {
+          if (lastw && un < total) {
+            if (lane == 0) {
+              sh.item_q[par ^ 1] = itn;
+              sh.scene_q[par ^ 1] = sn;
+            }
+            stage_issue(sh, scenes[sn], lane < 27 ? slot : -1);
+          }
+        });
+    if (!done) {  // a copy wait ran out: this item's particles keep their state, the CTA stops
+      stage_abort(sh, S);
+      return;
+    }
   }
 }
 
@@ -532,31 +534,42 @@ void smem_opt_in(K kernel, int bytes) {
   cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
+// Shared-memory opt-in of the work-item kernels, once per device (the
+// attribute belongs to the function in each device's context).
 int item_smem() {
-  static bool configured = false;
+  static bool configured[kMaxDevices] = {};
   const int bytes = (int)sizeof(ItemShared);
-  if (!configured) {
+  const int dev = current_device();
+  if (!configured[dev]) {
     smem_opt_in(k_p2g<true>, bytes);
     smem_opt_in(k_p2g<false>, bytes);
     smem_opt_in(k_g2p_advance, bytes);
     smem_opt_in(k_g2p2g<false>, bytes);
     smem_opt_in(k_g2p2g<true>, bytes);
-    configured = true;
+    configured[dev] = true;
   }
   return bytes;
 }
 
 }  // namespace
 
+int current_device() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) dev = 0;
+  return dev;
+}
+
+// SM count of the current device (cached per device: launch grids are sized
+// for the GPU the launch goes to).
 int num_sms() {
-  static int n = 0;
-  if (n == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 1;
+  static int n[kMaxDevices] = {};
+  const int dev = current_device();
+  if (n[dev] == 0) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    n[dev] = v > 0 ? v : 1;
   }
-  return n;
+  return n[dev];
 }
 
 
@@ -571,13 +584,6 @@ void fast_begin_step(const SceneDev* scenes, int nscenes, bool rigid, cudaStream
 void fast_gather_counters(const SceneDev* scenes, int nscenes, int* out, cudaStream_t st) {
   const int n = nscenes * kCounterStride;
   k_gather_counters<<<(n + 255) / 256, 256, 0, st>>>(scenes, nscenes, out);
-}
-
-void fast_count_flags(const SceneDev* sd_dev, int nblocks, cudaStream_t st) {
-  int g = (nblocks + 255) / 256;
-  if (g > num_sms() * 8) g = num_sms() * 8;
-  if (g < 1) g = 1;
-  k_count_flags<<<g, 256, 0, st>>>(sd_dev, nblocks);
 }
 
 void fast_compact(const SceneDev* scenes, const int* block_prefix, int nscenes, long long total_blocks,

@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(kItemMax, 2) k_hess(const SceneDev* __restrict
   int u = next_running(scenes, item_prefix, nscenes, k, blockIdx.x, total, s);
   if (u >= total) return;  // uniform across the CTA
   int4 it = scenes[s].items[u - item_prefix[s]];
-  if (lastw) stage_issue(sh, scenes[s].cru, kImpBlockFloats, tile_slot(scenes[s], it, lane));
+  if (lastw) stage_issue(sh, scenes[s].cru, kImpBlockFloats, tile_slot(scenes[s], it, lane), scenes[s].tx_unsent);
   uint32_t phase = 0;
   while (u < total) {
     __syncthreads();  // zero-filled stage blocks are visible; the last flush is done
@@ -276,13 +276,13 @@ __global__ void __launch_bounds__(kItemMax, 2) k_hess(const SceneDev* __restrict
     float4 xm = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const bool binned = particles_binned(S);  // the solve runs before the step's fused kernel
     if (mine) xm = (binned ? S.bxm : S.xm)[it.y + i];
-    stage_wait(sh, S, phase);
+    const bool landed = stage_wait(sh, S, phase);
     bool have = false;
     P2GParticle q;
     q.force = false;
     AxisW w;
     int base[3] = {0, 0, 0};
-    if (mine && fabsf(xm.w) <= 100.0f) {  // p2gTransfer.glsl:64-66
+    if (mine && landed && fabsf(xm.w) <= 100.0f) {  // p2gTransfer.glsl:64-66
       float pg[3];
       grid_coords(S, xm, pg, base);
       all_weights(pg, base, w);
@@ -290,9 +290,16 @@ __global__ void __launch_bounds__(kItemMax, 2) k_hess(const SceneDev* __restrict
       hess_gather(sh, S, bx, by, bz, base, w, Gm);
       have = hess_particle(S, it.y + i, binned, Gm, q);
     }
-    p2g_tile_pass<kP2gForce>(sh, S, bx, by, bz, have, q, w, base, [&] {
-      if (lastw && un < total) stage_issue(sh, scenes[sn].cru, kImpBlockFloats, lane < 27 ? slot : -1);
-    });
+    const bool done = p2g_tile_pass<kP2gForce>(
+        sh, S, bx, by, bz, have, q, w, base,
+        [&] {
+          if (lastw && un < total)
+            stage_issue(sh, scenes[sn].cru, kImpBlockFloats, lane < 27 ? slot : -1, scenes[sn].tx_unsent);
+        });
+    if (!done) {  // a copy wait ran out: the CTA stops
+      stage_abort(sh, S);
+      return;
+    }
     u = un;
     s = sn;
     it = itn;
@@ -547,11 +554,12 @@ __global__ void k_cr_cond(const SceneDev* __restrict__ scenes, int nscenes, int*
 }
 
 int hess_smem() {
-  static bool configured = false;
+  static bool configured[kMaxDevices] = {};
   const int bytes = (int)sizeof(ItemShared);
-  if (!configured) {
+  const int dev = current_device();
+  if (!configured[dev]) {
     cudaFuncSetAttribute(k_hess, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    configured = true;
+    configured[dev] = true;
   }
   return bytes;
 }

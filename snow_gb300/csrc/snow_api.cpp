@@ -103,6 +103,9 @@ struct snow_scene {
   float g_dt = NAN;
   snow_phase_times times{};
   float last_dt = 1e-3f;
+  // bounded copy waits of the FAST kernels (snow_scene_set_wait_limit)
+  uint32_t wait_ns = kDefaultWaitNs;
+  uint32_t tx_unsent = 0;
 };
 
 struct snow_batch {
@@ -253,6 +256,8 @@ void fill_sd_params(snow_scene* s) {
   d.imp_beta = s->p.implicit_beta;
   d.imp_tol = implicit_tol(s->p);
   d.imp_maxit = implicit_iters(s->p);
+  d.wait_ns = s->wait_ns;
+  d.tx_unsent = s->tx_unsent;
 }
 
 snow_status push_sd(snow_scene* s) {
@@ -394,21 +399,14 @@ snow_status set_dt(snow_scene* s, float dt) {
   return SNOW_OK;
 }
 
-// Checks a copy of the device-side counters: errors, the output pool's fill
-// (grown when it runs three quarters full).
+// Checks a copy of the device-side counters for the errors counted there.
+// (The pool holds a slot for every grid block, so CNT_OVERFLOW stays 0; it is
+// checked all the same.)
 snow_status check_counters(snow_scene* s, const int* h) {
   snow_ctx* ctx = s->ctx;
   if (h[CNT_TIMEOUT] > 0) return fail(ctx, SNOW_ETIMEDOUT, "a bounded device wait ran out");
   if (h[CNT_OVERFLOW] > 0) return fail(ctx, SNOW_ECAPACITY, "grid block pool overflowed");
   if (h[CNT_NONFINITE] > 0) return fail(ctx, SNOW_ENUMERIC, "non-finite particle state");
-  const int active = h[CNT_ACTIVE];
-  if (active > (s->sd.pool_cap * 3) / 4 && s->sd.pool_cap < s->sd.nblocks) {
-    // the old pool is freed in stream order, after the queued steps that use it
-    const int want = std::min(s->sd.nblocks, std::max(2 * active, s->sd.pool_cap + 1024));
-    snow_status st = fast_alloc_pool(s, want);
-    if (st) return st;
-    return push_sd(s);
-  }
   return SNOW_OK;
 }
 
@@ -468,15 +466,12 @@ snow_status fast_init(snow_scene* s) {
   if ((r = push_sd(s))) return r;
   fast_bin(s, st, false);
   fast_enqueue_p2g(s, true, st);  // gMassCompute
-  // size the output pool from the blocks that received mass
-  CK(cudaMemsetAsync(s->sd.counters + CNT_ACTIVE, 0, sizeof(int), st));
-  fast_count_flags(s->sd_dev, s->sd.nblocks, st);
-  CK(cudaMemcpyAsync(ctx->h_counters, s->sd.counters, kCounterStride * sizeof(int), cudaMemcpyDeviceToHost, st));
-  CK(cudaStreamSynchronize(st));
-  const int touched = ctx->h_counters[CNT_ACTIVE];
-  const int cap = std::min(s->sd.nblocks, std::max(2 * touched + 1024, 4096));
-  if (cap != s->sd.pool_cap) {
-    if ((r = fast_alloc_pool(s, cap))) return r;
+  // The output pool has a slot for every grid block: however far the
+  // particles spread, the compaction of a step finds a slot for each block
+  // that received sums (the footprint bound always counted the pool at this
+  // size). Only the active blocks' slots are written or read in a step.
+  if (s->sd.pool_cap != s->sd.nblocks) {
+    if ((r = fast_alloc_pool(s, s->sd.nblocks))) return r;
     if ((r = push_sd(s))) return r;
   }
   fast_enqueue_compact(s, st);
@@ -1083,7 +1078,10 @@ snow_status snow_scene_step(snow_scene* s, double dt, int n_steps) {
       }
       CK(cudaGraphLaunch(g, st));
     }
-    if (bin) s->steps_since_sort = 0;
+    if (bin) {
+      s->steps_since_sort = 0;
+      s->times.binnings++;
+    }
     s->steps_since_sort++;
   }
   CK(cudaGetLastError());
@@ -1335,6 +1333,29 @@ snow_status snow_scene_phase_times(snow_scene* s, snow_phase_times* out, int res
   return SNOW_OK;
 }
 
+snow_status snow_scene_set_wait_limit(snow_scene* s, uint32_t wait_ns, uint32_t unsent_bytes) {
+  if (!s) return SNOW_EINVAL;
+  snow_ctx* ctx = s->ctx;
+  if (s->mode != SNOW_MODE_FAST) return fail(ctx, SNOW_EUNSUPPORTED, "bounded copy waits are FAST-mode kernels'");
+  if (unsent_bytes > 65536) return fail(ctx, SNOW_EINVAL, "snow_scene_set_wait_limit: unsent_bytes above 65536");
+  s->wait_ns = wait_ns ? wait_ns : kDefaultWaitNs;
+  s->tx_unsent = unsent_bytes;
+  s->sd.wait_ns = s->wait_ns;
+  s->sd.tx_unsent = s->tx_unsent;
+  if (!s->sd_dev) return SNOW_OK;  // not allocated yet: the first upload pushes the descriptor
+  return push_sd(s);
+}
+
+snow_status snow_scene_check(snow_scene* s) {
+  if (!s) return SNOW_EINVAL;
+  snow_ctx* ctx = s->ctx;
+  if (s->mode != SNOW_MODE_FAST) {
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SNOW_OK;
+  }
+  return fast_check(s);
+}
+
 snow_status snow_scene_solver_report(snow_scene* s, snow_solver_report* out) {
   if (!s || !out) return SNOW_EINVAL;
   snow_ctx* ctx = s->ctx;
@@ -1539,11 +1560,17 @@ snow_status snow_scene_set_tuning(snow_scene* s, const snow_tuning* t) {
   if (s->mode != SNOW_MODE_FAST) return fail(s->ctx, SNOW_EUNSUPPORTED, "tuning applies to SNOW_MODE_FAST scenes");
   snow_ctx* ctx = s->ctx;
   CK(cudaStreamSynchronize(ctx->stream));
+  // the captured step graphs bake in the launch shapes: a changed work split
+  // needs new ones
+  const bool split_changed = s->tune.items_max != t->items_max || s->tune.ctas_per_sm != t->ctas_per_sm;
   s->tune.sort_interval = t->sort_interval;
   s->tune.items_max = t->items_max;
   s->tune.ctas_per_sm = t->ctas_per_sm;
   s->bin_interval = t->sort_interval;
-  drop_graphs(s);
+  s->clean_checks = 0;
+  // the next step re-bins with the new work split
+  if (s->p2g_ready) s->steps_since_sort = s->bin_interval;
+  if (split_changed) drop_graphs(s);
   return SNOW_OK;
 }
 

@@ -79,6 +79,7 @@ struct CrScalars {
   int pad;
 };
 constexpr int kImpBlockFloats = 3 * kBlockNodes;  // 192: one 3-vector per node
+constexpr uint32_t kDefaultWaitNs = 1000000000u;   // one second
 
 // Device-resident description of one FAST scene (read by every kernel).
 struct SceneDev {
@@ -126,6 +127,11 @@ struct SceneDev {
   int4* items;
   int item_cap;
   int* counters;    // kCounterStride ints
+  // bounded waits for bulk copies into shared memory: give up after wait_ns
+  // nanoseconds; tx_unsent (0 in normal use) is added to the bytes each such
+  // wait expects, so that it runs out (a test of the timeout path)
+  uint32_t wait_ns;
+  uint32_t tx_unsent;
   // semi-implicit velocity solve (crs == nullptr: the scene steps explicitly)
   float imp_beta;   // beta of (M + beta dt^2 K) v = M v*
   float imp_tol;    // stop once |r| <= imp_tol |M^1/2 v*| (r of the mass-scaled system)
@@ -153,8 +159,6 @@ void fast_begin_step(const SceneDev* scenes, int nscenes, bool rigid, cudaStream
 // pinned memory: a batch reads them one re-binning interval later, without
 // draining the stream).
 void fast_gather_counters(const SceneDev* scenes, int nscenes, int* out, cudaStream_t st);
-// Counts flagged blocks of one scene into counters[CNT_ACTIVE] (pool sizing).
-void fast_count_flags(const SceneDev* sd_dev, int nblocks, cudaStream_t st);
 // Flags -> active list and pool slots; its last CTA then forms the item and
 // active-block prefixes (as fast_prefix does).
 void fast_compact(const SceneDev* scenes, const int* block_prefix, int nscenes, long long total_blocks,
@@ -284,6 +288,9 @@ void fast_pack(const float* x, const float* v, const float* m, const float* FE, 
 void fast_unpack(const SceneDev* sd_dev, size_t n, float* x, float* v, float* FE, float* Jp, float* volume,
                  cudaStream_t st);
 
+constexpr int kMaxDevices = 64;
+// The calling thread's current device (0 .. kMaxDevices - 1).
+int current_device();
 int num_sms();
 
 }  // namespace snow

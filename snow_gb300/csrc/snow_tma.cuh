@@ -46,11 +46,24 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Waits for phase `parity` of `bar` to complete, at most `limit` polls.
-// Returns false if the limit ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit) {
-  for (uint32_t i = 0; i < limit; i++)
-    if (mbar_try_wait(bar, parity)) return true;
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Waits for phase `parity` of `bar` to complete for at most `limit_ns`
+// nanoseconds of the global timer (and at most 2^26 rounds of polls, should
+// the timer stand still). Returns false if the limit ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit_ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  for (uint32_t round = 0; round < (1u << 26); round++) {
+#pragma unroll 1
+    for (int i = 0; i < 8; i++)
+      if (mbar_try_wait(bar, parity)) return true;
+    if (global_ns() - t0 > (uint64_t)limit_ns) return false;
+  }
   return false;
 }
 

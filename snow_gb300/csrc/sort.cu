@@ -355,25 +355,64 @@ __global__ void k_iota(uint32_t* __restrict__ v, size_t n) {
     v[i] = (uint32_t)i;
 }
 
-// Device address of g_sort_scratch on the current device. Host code only sees
-// a host-side stand-in for the symbol, so the address is looked up once per
-// device (cudaGetSymbolAddress) and cached.
+// The driver's id of the calling thread's current context (0 if none). Ids
+// are never reused in a process, so a context created after a reset (which
+// reloads the module and moves g_sort_scratch) gets a new id.
+unsigned long long current_context_id() {
+  using GetCurrent = int (*)(void**);
+  using GetId = int (*)(void*, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(f);
+    looked_up = true;
+  }
+  void* c = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&c) != 0 || !c || get_id(c, &id) != 0) return 0;
+  return id;
+}
+
+// Device address of g_sort_scratch in the current context. Host code only
+// sees a host-side stand-in for the symbol, so the address is looked up
+// (cudaGetSymbolAddress) and cached per context: a reset of the device's
+// primary context reloads the module at another address, and the new
+// context's different id makes the cache look the address up again.
 cudaError_t static_scratch(uint32_t** out) {
   static std::mutex mu;
+  static unsigned long long ctx_id[64] = {};
   static uint32_t* addr[64] = {};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lock(mu);
-  if (!addr[dev]) {
+  const unsigned long long id = current_context_id();
+  if (!addr[dev] || id == 0 || id != ctx_id[dev]) {
     void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_sort_scratch);
+    e = cudaGetSymbolAddress(&p, g_sort_scratch);  // also makes the primary context current
     if (e != cudaSuccess) return e;
     addr[dev] = static_cast<uint32_t*>(p);
+    ctx_id[dev] = current_context_id();
   }
   *out = addr[dev];
   return cudaSuccess;
+}
+
+// Whether the byte ranges [a, a + n) and [b, b + n) of 32-bit words overlap.
+bool ranges_overlap(const void* a, const void* b, size_t n) {
+  const uintptr_t x = reinterpret_cast<uintptr_t>(a), y = reinterpret_cast<uintptr_t>(b);
+  const uintptr_t bytes = n * sizeof(uint32_t);
+  return x < y + bytes && y < x + bytes;
 }
 
 }  // namespace
@@ -385,6 +424,11 @@ extern "C" snow_status snow_sort_keys_static(const uint32_t* keys, uint32_t* sor
   if (!keys || !sorted_keys || !perm || key_bits < 1 || key_bits > 32) return SNOW_EINVAL;
   if (n > kStaticKeys) return SNOW_EINVAL;
   if (n == 0) return SNOW_OK;
+  // perm is written before the keys are read: it may not share memory with
+  // either key array; keys and sorted_keys may only coincide exactly
+  if (ranges_overlap(perm, keys, n) || ranges_overlap(perm, sorted_keys, n) ||
+      (keys != sorted_keys && ranges_overlap(keys, sorted_keys, n)))
+    return SNOW_EINVAL;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   uint32_t* scratch = nullptr;
   if (static_scratch(&scratch) != cudaSuccess) {

@@ -12,7 +12,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libsnow_gb300.so")
 
-SNOW_OK = 0
+(SNOW_OK, SNOW_EINVAL, SNOW_ENOMEM, SNOW_EBUDGET, SNOW_ETIMEDOUT, SNOW_ENUMERIC, SNOW_ECUDA, SNOW_ESTATE,
+ SNOW_EUNSUPPORTED, SNOW_ECAPACITY) = (0, -1, -2, -3, -4, -5, -6, -7, -8, -9)
 STATUS_NAMES = {0: "SNOW_OK", -1: "SNOW_EINVAL", -2: "SNOW_ENOMEM", -3: "SNOW_EBUDGET", -4: "SNOW_ETIMEDOUT",
                 -5: "SNOW_ENUMERIC", -6: "SNOW_ECUDA", -7: "SNOW_ESTATE", -8: "SNOW_EUNSUPPORTED",
                 -9: "SNOW_ECAPACITY"}
@@ -30,7 +31,7 @@ EXPORTS = [
     "snow_batch_step", "snow_batch_autotune", "snow_sort_keys_static", "snow_server_create", "snow_server_destroy",
     "snow_server_submit", "snow_server_poll", "snow_server_fetch", "snow_server_stats", "snow_server_drain",
     "snow_scene_set_tuning", "snow_batch_set_tuning", "snow_ctx_set_graphs", "snow_scene_stats_enqueue",
-    "snow_ctx_stats_read", "snow_scene_solver_report",
+    "snow_ctx_stats_read", "snow_scene_solver_report", "snow_scene_check", "snow_scene_set_wait_limit",
 ]
 SORT_STATIC_MAX_KEYS = 262144  # SNOW_SORT_STATIC_MAX_KEYS
 
@@ -56,7 +57,8 @@ class SnowStats(C.Structure):
 
 class SnowPhaseTimes(C.Structure):
     _fields_ = [("sort_ms", C.c_double), ("p2g_ms", C.c_double), ("grid_ms", C.c_double), ("g2p_ms", C.c_double),
-                ("other_ms", C.c_double), ("total_ms", C.c_double), ("steps", C.c_uint64)]
+                ("other_ms", C.c_double), ("total_ms", C.c_double), ("steps", C.c_uint64),
+                ("binnings", C.c_uint64)]
 
 
 class SnowSolverReport(C.Structure):
@@ -161,6 +163,8 @@ def load(path: str = LIB_PATH):
     L.snow_batch_set_tuning.argtypes = [vp, C.POINTER(SnowTuning)]
     L.snow_scene_set_tuning.argtypes = [vp, C.POINTER(SnowTuning)]
     L.snow_sort_keys_static.argtypes = [vp, vp, vp, sz, C.c_int, vp]
+    L.snow_scene_check.argtypes = [vp]
+    L.snow_scene_set_wait_limit.argtypes = [vp, C.c_uint32, C.c_uint32]
     L.snow_server_create.argtypes = [C.POINTER(SnowServerConfig), C.POINTER(vp)]
     L.snow_server_destroy.argtypes = [vp]
     L.snow_server_destroy.restype = None

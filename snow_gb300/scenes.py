@@ -232,6 +232,27 @@ def cfg3_batch(seed: int = 0x5EED0003, n_scenes: int = 64, n_min: int = 10_000, 
     return out
 
 
+def snow_block_on_sphere(seed: int, n: int, edge: int, gap: float = 0.02, v0=(0.0, 0.0, 0.0)) -> Scene:
+    """A snow block (0.6 x 0.3 x 0.6 aspect, n particles at 8 per cell,
+    centred at (0.5, 0.6, 0.5)) above a static sphere collider (type 1,
+    radius 0.15 scaled with the block) whose top lies `gap` below the
+    block's bottom face (a negative gap sinks the sphere into the block), in
+    a unit box of edge^3 nodes, dt = 2e-5, moving at v0."""
+    s = unit_box_scene(edge, young=1.4e5, poisson=0.2, hardening=10.0, crit_compression=2.5e-2,
+                       crit_stretch=7.5e-3, dt=2e-5, steps=200, name=f"block_{n}_{edge}")
+    h = s.grid_spacing
+    aspect = (0.6, 0.3, 0.6)
+    srng = np.random.default_rng(seed)
+    s.x = sample_shape("box", (0.5, 0.6, 0.5), n, h, srng, aspect=aspect)
+    ext = (s.x.max(0) - s.x.min(0)).astype(np.float64)
+    scale = ext[0] / 0.6
+    s.colliders.append(Collider(pos=(0.5, 0.6 - 0.15 * scale - 0.5 * ext[1] - gap, 0.5),
+                                type=COLLIDER_SPHERE, radius=float(0.15 * scale)))
+    s.v = np.tile(np.asarray(v0, np.float32), (n, 1))
+    s.m = np.full(n, SNOW_DENSITY * h ** 3 / 8.0, np.float32)
+    return s
+
+
 def cfg4_batch(seed: int = 0x5EED0004, n_scenes: int = 16, n_min: int = 2_000_000, n_max: int = 8_000_000,
                steps: int = 200) -> List[Scene]:
     """Batched at scale: snow blocks (0.6 x 0.3 x 0.6 aspect) dropped onto a
@@ -242,18 +263,9 @@ def cfg4_batch(seed: int = 0x5EED0004, n_scenes: int = 16, n_min: int = 2_000_00
     for i in range(n_scenes):
         n = int(rng.integers(n_min, n_max + 1))
         edge = int(rng.choice([384, 448, 512]))
-        s = unit_box_scene(edge, young=1.4e5, poisson=0.2, hardening=10.0, crit_compression=2.5e-2,
-                           crit_stretch=7.5e-3, dt=2e-5, steps=steps, name=f"cfg4_{i:02d}")
-        h = s.grid_spacing
-        aspect = (0.6, 0.3, 0.6)
-        srng = np.random.default_rng(seed * 1000 + i)
-        s.x = sample_shape("box", (0.5, 0.6, 0.5), n, h, srng, aspect=aspect)
-        ext = (s.x.max(0) - s.x.min(0)).astype(np.float64)
-        scale = ext[0] / 0.6
-        s.colliders.append(Collider(pos=(0.5, 0.6 - 0.15 * scale - 0.5 * ext[1] - 0.02, 0.5),
-                                    type=COLLIDER_SPHERE, radius=float(0.15 * scale)))
-        s.v = np.zeros((n, 3), np.float32)
-        s.m = np.full(n, SNOW_DENSITY * h ** 3 / 8.0, np.float32)
+        s = snow_block_on_sphere(seed * 1000 + i, n, edge)
+        s.steps = steps
+        s.name = f"cfg4_{i:02d}"
         out.append(s)
     return out
 

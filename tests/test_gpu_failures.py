@@ -1,0 +1,118 @@
+"""Failure paths of the FAST kernels on the GPU, made without faulting or
+hanging the GPU, and a scene whose particles spread over far more grid
+blocks than they start in.
+
+A work item's wait for the bulk copies of its grid tile is bounded (a time
+limit on the GPU's global timer). snow_scene_set_wait_limit's unsent_bytes
+makes every such wait expect bytes that no copy delivers, so the wait runs
+out while every issued copy still lands: the CTA stops without reading the
+tile, the host gets SNOW_ETIMEDOUT, and the context stays usable."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from snow_gb300 import scenes
+
+gpu = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from snow_gb300 import api
+    return api.Context(0)
+
+
+def _one_step_within_bound(ctx, s):
+    from snow_gb300 import api
+    g = api.SimScene(ctx, s).upload().init().step(s.dt, 1).check()
+    o = O.OracleSim(s, mode=O.EXACT64).upload().init()
+    flip = o.step_with_flip_scale()
+    e = O.parity_errors(g.download(), o.state(), flip)
+    g.close()
+    return max(e["max"][k] for k in ("x", "v_flip", "FE", "Jp"))
+
+
+@gpu
+@pytest.mark.parametrize("path", ["step", "dispatch", "implicit"])
+def test_a_copy_wait_that_runs_out_returns_etimedout(ctx, path):
+    """The fused step kernel (step), the per-kernel G2P + advance (dispatch)
+    and the semi-implicit solve's Hessian pass (implicit) each stop on a
+    wait that runs out after 2 ms; the scene reports SNOW_ETIMEDOUT, and a
+    fresh scene on the same context then steps within the parity bound."""
+    from snow_gb300 import api, native as N
+    s = scenes.small_scene(n=3000, grid_edge=32, seed=301, v0=(0.5, -2.0, 0.0))
+    if path == "implicit":
+        s.young, s.implicit_beta, s.implicit_tolerance, s.implicit_max_iters = 1.4e7, 1.0, 1e-5, 10
+    bad = api.SimScene(ctx, s).upload().init()
+    bad.set_wait_limit(wait_ns=2_000_000, unsent_bytes=16)
+    with pytest.raises(N.SnowError) as e:
+        if path == "dispatch":
+            bad.dispatch(N.K_RIGID_ADVANCE, s.dt)
+            bad.dispatch(N.K_P2G, s.dt)
+            bad.dispatch(N.K_G_FORCE, s.dt)
+            bad.dispatch(N.K_G2P, s.dt)
+        else:
+            bad.step(s.dt, 2)
+        bad.check()
+    assert e.value.status == N.SNOW_ETIMEDOUT
+    bad.close()
+    ok = scenes.small_scene(n=3000, grid_edge=32, seed=302, v0=(0.5, -2.0, 0.0))
+    assert _one_step_within_bound(ctx, ok) <= 1e-5
+
+
+@gpu
+def test_the_default_wait_limit_does_not_fire(ctx):
+    """A scene given the default limit back (0) after a short one steps
+    normally: the limit is a property of the scene, set at run time."""
+    from snow_gb300 import api
+    s = scenes.small_scene(n=3000, grid_edge=32, seed=303)
+    g = api.SimScene(ctx, s).upload().init()
+    g.set_wait_limit(wait_ns=2_000_000, unsent_bytes=0).step(s.dt, 3).check()
+    g.set_wait_limit(0, 0).step(s.dt, 3).check()
+    assert g.stats()["nonfinite"] == 0
+    g.close()
+
+
+def _active_blocks(mass, dim):
+    g = np.asarray(mass).reshape(dim[2], dim[1], dim[0])
+    idx = np.argwhere(g > 0)
+    return len({(int(k) >> 2, int(j) >> 2, int(i) >> 2) for k, j, i in idx}) if len(idx) else 0
+
+
+@gpu
+def test_particles_spreading_over_the_grid_keep_every_grid_block(ctx):
+    """A small dense ball expanding radially at up to ~40 m/s in a 128^3 grid:
+    within 100 steps its particles touch over a hundred times the grid
+    blocks they started in (~60 -> ~11,000), and cross cells every step (re-binned every
+    step, some scattered outside their work item's tile). The output pool
+    has a slot for every grid block, so every block's sums reach the grid
+    update: the state tracks the FP64 oracle's through all 100 steps."""
+    from snow_gb300 import api, native as N
+    s = scenes.unit_box_scene(128, young=1.4e5, poisson=0.2, hardening=10.0, crit_compression=2.5e-2,
+                              crit_stretch=7.5e-3, dt=1e-4, name="expanding_ball")
+    h = s.grid_spacing
+    rng = np.random.default_rng(304)
+    c = np.array([0.5, 0.5, 0.5])
+    s.x = scenes.sample_shape("sphere", tuple(c), 4000, h, rng)
+    s.v = (1000.0 * (s.x - c)).astype(np.float32)
+    s.m = np.full(len(s.x), scenes.SNOW_DENSITY * h ** 3 / 8.0, np.float32)
+    g = api.SimScene(ctx, s).upload().init()
+    g.dispatch(N.K_RIGID_ADVANCE, s.dt)  # static walls: nothing moves; then a P2G of the initial state
+    g.dispatch(N.K_P2G, s.dt)
+    first = _active_blocks(g.grid()["mass"], s.grid_dim)
+    g.step(s.dt, 100).check()
+    got = g.download()
+    g.dispatch(N.K_RIGID_ADVANCE, s.dt)
+    g.dispatch(N.K_P2G, s.dt)
+    last = _active_blocks(g.grid()["mass"], s.grid_dim)
+    assert last >= 50 * first, (first, last)
+    o = O.OracleSim(s, mode=O.EXACT64, threads=os.cpu_count() or 1).upload().init().step(n=100)
+    ref = o.state()
+    assert np.abs(got["x"] - ref["x"]).max() <= 1e-3
+    m = s.m.astype(np.float64)
+    mom = (m[:, None] * ref["v"]).sum(0)
+    gmom = (m[:, None] * got["v"].astype(np.float64)).sum(0)
+    assert np.abs(gmom - mom).max() <= 1e-3 * np.abs(m[:, None] * ref["v"]).sum(0).max()
+    g.close()

@@ -9,17 +9,21 @@ Tolerances:
     count now and then. Density after init is bit-exact (no expf on that
     path); after steps: |dx| <= 1e-6 m, |dv| <= 1e-4 m/s, |dF| <= 1e-5.
   * SNOW_MODE_FAST vs the EXACT64 oracle (FP64, no fixed point, no V
-    rounding), one step: per-field relative error <= 1e-5 with denominators
-    floored at the field's scale in the scene:
+    rounding), one step: per-field relative error <= 1e-5
+    (oracle.parity_errors):
         x  : |dx| / max(|x|, 1e-3 m)
-        v  : |dv| / max(|v|, 1e-3 m/s, 1e-2 * max|v|)
+        v  : |dv| / max(|v|, 1e-3 m/s)           (strict floor)
         F_E: max|dF| / max|F| per particle
         J_p: |dJ| / |J|
-    The velocity floor is 1% of the scene's largest speed: v' = alpha v + sum
-    w d cancels terms of the scene's speed scale, so an FP32 result resolves
-    velocities only to ~1e-7 of that scale. Grid forces are compared in a
-    deformed state, where stresses are far above the ~1e-7 strain FP32 can
-    resolve in F_E - R.
+    The strict velocity floor holds where no particle is stopped within the
+    step (free flight, first contact). A particle that a collider or the
+    snow around it stops has |v'| far below the size S_p of the terms its
+    FLIP update adds up (alpha |v_p| + sum_i w_ip (|v*_i| + alpha |p_i/m_i|));
+    an FP32 evaluation resolves v' only to a few ulps of S_p, so there the
+    asserted bound is |dv| / max(|v|, 1e-3 m/s, S_p) <= 1e-5 (v_flip), with
+    S_p from the oracle's own grid of that step. Both are reported. Grid
+    forces are compared in a deformed state, where stresses are far above
+    the ~1e-7 strain FP32 can resolve in F_E - R.
   * binning: keys and stable permutation bit-exact vs std::stable_sort.
 """
 import numpy as np
@@ -45,22 +49,15 @@ def sim(ctx, scene, mode, **kw):
     return api.SimScene(ctx, scene, mode=mode, **kw)
 
 
-def field_errors(gpu_state, ref):
-    """Relative errors per field as documented in the module docstring."""
-    x, v = gpu_state["x"].astype(np.float64), gpu_state["v"].astype(np.float64)
-    ex = np.abs(x - ref["x"]) / np.maximum(np.abs(ref["x"]), 1e-3)
-    speed = np.linalg.norm(ref["v"], axis=1)
-    vfloor = max(1e-3, 1e-2 * speed.max())
-    ev = np.linalg.norm(v - ref["v"], axis=1) / np.maximum(speed, vfloor)
-    ev_strict = np.linalg.norm(v - ref["v"], axis=1) / np.maximum(speed, 1e-3)
-    fe, rfe = gpu_state["FE"].astype(np.float64), ref["FE"]
-    ef = np.abs(fe - rfe).max((1, 2)) / np.abs(rfe).max((1, 2))
-    ej = np.abs(gpu_state["Jp"].astype(np.float64) - ref["Jp"]) / np.abs(ref["Jp"])
-    w = int(np.argmax(ev))
-    return dict(x=ex.max(), v=ev.max(), FE=ef.max(), Jp=ej.max(),
-                x_p99=np.percentile(ex, 99), v_p99=np.percentile(ev, 99), FE_p99=np.percentile(ef, 99),
-                v_strict_p99=np.percentile(ev_strict, 99), v_strict_max=ev_strict.max(),
-                v_worst_ref=ref["v"][w].tolist(), v_worst_gpu=v[w].tolist(), x_worst=ref["x"][w].tolist())
+def check_step(got, ref, flip, strict):
+    """Asserts the FAST single-step bound (module docstring); `strict` also
+    asserts the 1e-3 m/s velocity floor for every particle."""
+    e = O.parity_errors(got, ref, flip)
+    m = e["max"]
+    assert max(m["x"], m["v_flip"], m["FE"], m["Jp"]) <= REL_TOL, e
+    if strict:
+        assert m["v"] <= REL_TOL, e
+    return e
 
 
 # ---------------------------------------------------------------------------
@@ -127,9 +124,9 @@ def test_fast_single_step_from_rest_within_1e5(ctx, seed, n, edge, v0):
     from snow_gb300 import native as N
     s = scenes.small_scene(n=n, grid_edge=edge, seed=seed, v0=v0)
     g = sim(ctx, s, N.MODE_FAST).upload().init().step(s.dt, 1)
-    o = _exact_oracle(s).upload().init().step()
-    e = field_errors(g.download(), o.state())
-    assert max(e["x"], e["v"], e["FE"], e["Jp"]) <= REL_TOL, e
+    o = _exact_oracle(s).upload().init()
+    flip = o.step_with_flip_scale()
+    check_step(g.download(), o.state(), flip, strict=True)
 
 
 @gpu
@@ -145,9 +142,9 @@ def test_fast_single_step_with_sphere_and_moving_colliders_within_1e5(ctx):
     s.colliders.append(scenes.Collider(pos=(0.0, 0.2, 0.0), type=0, normal=(0.0, 1.0, 0.0), vel=(0.0, 1.0, 0.0),
                                        friction=0.1))
     g = sim(ctx, s, N.MODE_FAST).upload().init().step(s.dt, 1)
-    o = _exact_oracle(s).upload().init().step()
-    e = field_errors(g.download(), o.state())
-    assert max(e["x"], e["v"], e["FE"], e["Jp"]) <= REL_TOL, e
+    o = _exact_oracle(s).upload().init()
+    flip = o.step_with_flip_scale()
+    check_step(g.download(), o.state(), flip, strict=False)
     assert np.abs(g.colliders() - o.colliders()).max() <= 1e-6
 
 
@@ -174,14 +171,81 @@ def _deformed_restart(ctx, warm_steps, seed=41):
     return s2, o, g
 
 
+def _oracle_from_gpu_state(scene, y):
+    """The FP64 oracle restarted from a FAST scene's downloaded state y (the
+    colliders must be static: their advanced positions are not carried
+    over). Only det F_P enters a step, so F_P = diag(J_p, 1, 1); the
+    densities come from the particles' initial volumes."""
+    n = len(y["x"])
+    fp = np.zeros((n, 3, 3))
+    fp[:, 0, 0] = y["Jp"]
+    fp[:, 1, 1] = fp[:, 2, 2] = 1.0
+    s3 = scenes.Scene(**{k: getattr(scene, k) for k in ("grid_pos", "grid_dim", "grid_spacing", "young",
+                                                        "poisson", "hardening", "crit_compression", "crit_stretch",
+                                                        "alpha", "gravity", "dt")})
+    assert all(tuple(c.vel) == (0.0, 0.0, 0.0) for c in scene.colliders)
+    s3.colliders = list(scene.colliders)
+    s3.x, s3.v, s3.m = y["x"], y["v"], scene.m.copy()
+    rho = np.where(y["volume"] > 0, s3.m.astype(np.float64) / np.maximum(y["volume"], 1e-30), 0.0)
+    return _exact_oracle(s3).upload(FE=y["FE"].astype(np.float64), FP=fp).set_density(rho)
+
+
+def _uneven_batch(n_scenes=8, seed=0x5EED0103):
+    """Scenes drawn as the 64-scene batched workload draws them, at sizes the
+    oracle steps in seconds: particle counts log-uniform in [2k, 30k],
+    sphere or box, per-scene E0 ~ U[4.8e4, 1.4e5] and xi ~ U[5, 10], initial
+    velocity |v| <= 4 m/s in a random direction, dt = 1e-4, grids of uneven
+    edge (including edges that are not a multiple of the 4-node block)."""
+    rng = np.random.default_rng(seed)
+    edges = [48, 64, 50, 96, 72, 64, 41, 80, 56, 88][:n_scenes]
+    out = []
+    for i, edge in enumerate(edges):
+        n = int(round(np.exp(rng.uniform(np.log(2000), np.log(30000)))))
+        kind = "sphere" if i % 2 == 0 else "box"
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        v0 = tuple(float(c) for c in d * rng.uniform(0.5, 4.0))
+        center = tuple(float(c) for c in 0.5 + rng.uniform(-0.05, 0.05, size=3))
+        out.append(scenes.small_scene(n=n, grid_edge=edge, seed=seed * 100 + i, v0=v0, kind=kind, center=center,
+                                      young=float(rng.uniform(4.8e4, 1.4e5)),
+                                      hardening=float(rng.uniform(5.0, 10.0))))
+    return out
+
+
+@gpu
+@pytest.mark.parametrize("warm", [0, 5])
+def test_fast_batched_step_matches_the_oracle_per_scene(ctx, warm):
+    """Eight uneven scenes advanced together by snow_batch_step (one launch
+    per phase for all scenes, CUDA graph), each checked against the FP64
+    oracle on its own: one step from the initial state (warm = 0), or one
+    step after five batched steps, the oracle restarted from the GPU state
+    (warm SVD frames, re-binned particles)."""
+    from snow_gb300 import api, native as N
+    scs = _uneven_batch()
+    sims = [sim(ctx, s, N.MODE_FAST).upload().init() for s in scs]
+    batch = api.Batch(ctx, sims)
+    dts = [s.dt for s in scs]
+    if warm:
+        batch.step(warm, dts)
+        oracles = [_oracle_from_gpu_state(s, g.download()) for s, g in zip(scs, sims)]
+    else:
+        oracles = [_exact_oracle(s).upload().init() for s in scs]
+    flips = [o.step_with_flip_scale() for o in oracles]
+    batch.step(1, dts)
+    for s, g, o, flip in zip(scs, sims, oracles, flips):
+        check_step(g.download(), o.state(), flip, strict=True)
+    batch.close()
+    for g in sims:
+        g.close()
+
+
 @gpu
 @pytest.mark.parametrize("warm_steps", [5, 20])
 def test_fast_single_step_from_deformed_state_within_1e5(ctx, warm_steps):
     s2, o, g = _deformed_restart(ctx, warm_steps)
-    o.step()
+    flip = o.step_with_flip_scale()
     g.step(s2.dt, 1)
-    e = field_errors(g.download(), o.state())
-    assert max(e["x"], e["v"], e["FE"], e["Jp"]) <= REL_TOL, repr(e)
+    check_step(g.download(), o.state(), flip, strict=False)
 
 
 @gpu
@@ -192,23 +256,10 @@ def test_fast_step_with_warm_svd_frames_within_1e5(ctx):
     that step, and compare the next step of both."""
     s2, o, g = _deformed_restart(ctx, 20, seed=61)
     g.step(s2.dt, 1)
-    y = g.download()
-    n = len(y["x"])
-    fp = np.zeros((n, 3, 3))
-    fp[:, 0, 0] = y["Jp"]
-    fp[:, 1, 1] = fp[:, 2, 2] = 1.0  # only det F_P enters the step
-    s3 = scenes.Scene(**{k: getattr(s2, k) for k in ("grid_pos", "grid_dim", "grid_spacing", "young", "poisson",
-                                                     "hardening", "crit_compression", "crit_stretch", "alpha",
-                                                     "gravity", "dt")})
-    assert all(c.vel == (0.0, 0.0, 0.0) or tuple(c.vel) == (0.0, 0.0, 0.0) for c in s2.colliders)
-    s3.colliders = list(s2.colliders)  # static walls
-    s3.x, s3.v, s3.m = y["x"], y["v"], s2.m.copy()
-    rho = np.where(y["volume"] > 0, s3.m.astype(np.float64) / np.maximum(y["volume"], 1e-30), 0.0)
-    o2 = _exact_oracle(s3).upload(FE=y["FE"].astype(np.float64), FP=fp).set_density(rho)
-    o2.step()
+    o2 = _oracle_from_gpu_state(s2, g.download())
+    flip = o2.step_with_flip_scale()
     g.step(s2.dt, 1)
-    e = field_errors(g.download(), o2.state())
-    assert max(e["x"], e["v"], e["FE"], e["Jp"]) <= REL_TOL, repr(e)
+    check_step(g.download(), o2.state(), flip, strict=False)
 
 
 @gpu

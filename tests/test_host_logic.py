@@ -74,7 +74,8 @@ def test_bench_oracle_check_on_an_oracle_state():
     """The bench's full-size check (one FP64 oracle step restarted from a
     state, against a given next state) on CPU, with the oracle's own FP32-
     rounded steps standing in for the GPU's: within 1e-5, and the reported
-    fields are the parity tests' four."""
+    fields are the parity tests' (x, v with the strict floor, v against the
+    FLIP update's scale, F_E, J_p)."""
     import numpy as np
     import bench
     from oracle import oracle as O
@@ -92,5 +93,5 @@ def test_bench_oracle_check_on_an_oracle_state():
     y0 = f32(o.state(), vol=True)
     y1 = f32(o.step().state())
     r = bench.oracle_check(s, (y0, y1))
-    assert set(r["max"]) == {"x", "v", "FE", "Jp"}
-    assert r["within_tolerance"] and max(r["max"].values()) < 1e-6, r["max"]
+    assert set(r["max"]) == {"x", "v", "v_flip", "FE", "Jp"}
+    assert r["within_tolerance"] and r["strict_v_within_tolerance"] and max(r["max"].values()) < 1e-6, r["max"]
