@@ -207,13 +207,118 @@ __device__ __forceinline__ void collide_packed(const snow_collider* coll, const 
   }
 }
 
+// ---- fixed-point P2G sums ------------------------------------------------------
+// Every contribution of a particle to a grid node (mass m w, momentum m v w,
+// force A grad w) is rounded to an integer at a per-scene power-of-two scale
+// (s_m, s_p, s_f), and integers are summed: in registers and in the shared
+// tile as int32, into acc as int64 ((m, p_x) and (p_y, p_z) as packed pairs
+// of int32 sums, f_x, f_y, f_z as int64). Integer sums do not depend on the
+// order in which they are formed, so the grid a particle state produces does
+// not depend on how particles are grouped into work items, on the binning
+// schedule, on CTA scheduling or on the other scenes of a batch. The rounding
+// of one contribution is the same on every path that forms it: the tile path
+// and the per-node scatter of a particle outside its work item's tile both
+// compute it with the same pinned (_rn) operations.
+//
+// A contribution y (|y| < 2^22 after scaling) is rounded by one FMA against
+// kMagic = 1.5 * 2^23: fma(w, x, kMagic) lies in [2^23, 2^24), where floats
+// are spaced by 1, so its bits minus kMagicBits are round(w x). A force
+// contribution g_x kk + w_x hh is rounded as round(g_x kk + round(w_x hh)).
+// The scales put the largest expected term near 2^20; a particle whose terms
+// reach 2^21 (it outgrew the magnitudes the scale was chosen from) is
+// scattered with int64 contributions rounded in double precision ("wide"),
+// which depends only on the particle itself, so it is as deterministic.
+constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
+constexpr int kMagicBits = 0x4B400000;
+constexpr float kWmax = 0.2962963f;       // (2/3)^3 >= any weight or weight-gradient product
+constexpr float kFastLimit = 2095104.0f;  // 2^21 (1 - 2^-11): bound of one fast-path term
+
+// The largest power of two s with x s <= 2^20 (1 for x <= 0 or not finite).
+__device__ __forceinline__ float pow2_scale(float x) {
+  if (!(x > 0.0f) || !isfinite(x)) return 1.0f;
+  int e;
+  frexpf(x, &e);  // x = f 2^e, f in [0.5, 1): x 2^(20 - e) in [2^19, 2^20)
+  return ldexpf(1.0f, max(-126, min(127, 20 - e)));
+}
+
+struct FixScale {
+  float m, p, f;
+};
+
+__device__ __forceinline__ float bits_float(uint32_t b) { return __uint_as_float(b); }
+
+// Scales of a P2G that follows a grid update in the same step (the fused
+// kernel): from the magnitudes of the particles the previous P2G scattered
+// (FixState::*_prev) and the grid update's largest |v*|. The momentum scale
+// is a bound, not an estimate: a G2P gives v' = alpha v_p + sum_i w_i (v*_i -
+// alpha p_i/m_i) with sum_i w_i <= 1 and |p_i/m_i| <= max |v_p|, and a
+// collider projection adds at most twice the collider's speed, so
+// |v'| <= 2 alpha max|v_p| + max|v*| + 2 max|v_collider|. The force scale
+// leaves a factor 2 for the growth of the stresses in one step (a particle
+// that outgrows it takes the wide path); the floor 1e-9 E0 V0max keeps it
+// finite for a scene without stress.
+__device__ __forceinline__ FixScale step_scales(const SceneDev& S) {
+  const FixState& f = *S.fix;
+  const float mmax = bits_float(f.m_prev);
+  float vcoll = 0.0f;
+  for (int i = 0; i < S.ncoll; i++) {
+    const float* cv = S.coll[i].vel;
+    vcoll = fmaxf(vcoll, sqrtf(cv[0] * cv[0] + cv[1] * cv[1] + cv[2] * cv[2]));
+  }
+  const float vb = 2.0f * S.alpha * bits_float(f.v_prev) + bits_float(f.vstar) + 2.0f * vcoll;
+  const float afloor = 1e-9f * S.young * bits_float(f.v0max);
+  FixScale sc;
+  sc.m = pow2_scale(mmax * kWmax);
+  sc.p = pow2_scale(mmax * vb * kWmax);
+  sc.f = pow2_scale(fmaxf(2.0f * bits_float(f.a_prev), afloor) * kWmax);
+  return sc;
+}
+
+// Scales of a P2G of the stored state (set-up, per-kernel dispatches): from
+// the exact magnitudes a pass over the particles just measured (k_fix_measure).
+__device__ __forceinline__ FixScale measured_scales(const SceneDev& S) {
+  const FixState& f = *S.fix;
+  const float mmax = bits_float(f.m_prev);
+  const float afloor = 1e-9f * S.young * bits_float(f.v0max);
+  FixScale sc;
+  sc.m = pow2_scale(mmax * kWmax);
+  sc.p = pow2_scale(mmax * bits_float(f.v_prev) * kWmax);
+  sc.f = pow2_scale(fmaxf(bits_float(f.a_prev), afloor) * kWmax);
+  return sc;
+}
+
+// Packed pair of int32 sums in one 64-bit word: hi * 2^32 + lo (mod 2^64).
+// Sums of packed words unpack to the sums of the halves whenever those fit
+// in int32, whatever the intermediate carries.
+__device__ __forceinline__ unsigned long long pack2(int hi, int lo) {
+  return ((unsigned long long)(unsigned)hi << 32) + (unsigned long long)(long long)lo;
+}
+__device__ __forceinline__ void unpack2(unsigned long long w, int& hi, int& lo) {
+  lo = (int)(unsigned)(w & 0xffffffffull);
+  hi = (int)(unsigned)((w - (unsigned long long)(long long)lo) >> 32);
+}
+
+// Adds one node's seven integer sums (m, p, f) into acc.
+__device__ __forceinline__ void acc_add(const SceneDev& S, int blk, int node, long long m, long long px, long long py,
+                                        long long pz, long long fx, long long fy, long long fz, bool mass_only) {
+  unsigned long long* a = S.acc + (size_t)blk * kAccBlockWords + node;
+  atomicAdd(a, ((unsigned long long)px << 32) + (unsigned long long)m);
+  if (mass_only) return;
+  atomicAdd(a + kBlockNodes, ((unsigned long long)pz << 32) + (unsigned long long)py);
+  atomicAdd(a + 2 * kBlockNodes, (unsigned long long)fx);
+  atomicAdd(a + 3 * kBlockNodes, (unsigned long long)fy);
+  atomicAdd(a + 4 * kBlockNodes, (unsigned long long)fz);
+}
+
 // ---- P2G quantities of one particle -----------------------------------------
 // mass, momentum and A = -V0 * stress, stress = 2 mu(Jp) (FE - R) FE^T +
 // lambda(Jp) (JE - 1) JE I with R the polar rotation of FE
-// (p2gTransfer.glsl:109-141); V0 = m / rho0.
+// (p2gTransfer.glsl:109-141); V0 = m / rho0. `a` bounds the two terms of a
+// force contribution: max over rows r of max(|A_r0|, |A_r1| + |A_r2|).
 struct P2GParticle {
   float m, mv[3];
   float A[3][3];  // A[r][c]
+  float a;
   bool force;
 };
 
@@ -230,10 +335,14 @@ __device__ __forceinline__ void p2g_stress(const SceneDev& S, const M3& F, const
     for (int r = 0; r < 3; r++) D.m[c][r] = F.m[c][r] - R.m[c][r];
   const M3 P = m3_mul_bt(D, F);  // (FE - R) FE^T
   const float s2 = lam * (je - 1.0f) * je;
+  float a = 0.0f;
 #pragma unroll
-  for (int r = 0; r < 3; r++)
+  for (int r = 0; r < 3; r++) {
 #pragma unroll
     for (int c = 0; c < 3; c++) q.A[r][c] = -vol * (2.0f * mu * P.m[c][r] + (r == c ? s2 : 0.0f));
+    a = fmaxf(a, fmaxf(fabsf(q.A[r][0]), fabsf(q.A[r][1]) + fabsf(q.A[r][2])));
+  }
+  q.a = a;
   q.force = true;
 }
 
@@ -242,6 +351,8 @@ __device__ __forceinline__ P2GParticle p2g_particle(const SceneDev& S, int p, fl
   P2GParticle q;
   q.m = xm.w;
   q.force = false;
+  q.a = 0.0f;
+  q.mv[0] = q.mv[1] = q.mv[2] = 0.0f;
   if (mass_only) return q;
   const float4 vv = S.vv[p];
   q.mv[0] = q.m * vv.x;
@@ -258,11 +369,103 @@ __device__ __forceinline__ P2GParticle p2g_particle(const SceneDev& S, int p, fl
   return q;
 }
 
-// Scatter of one particle's 64 stencil nodes straight into acc (global
-// atomics) for a particle outside its work item's tile.
+// Whether every term of the particle's contributions fits the fast path's
+// range at scales sc (KIND kP2gMass: the mass alone).
 template <int KIND>
-__device__ __forceinline__ void scatter_global(const SceneDev& S, const P2GParticle& q, const AxisW& w,
-                                            const int base[3]) {
+__device__ __forceinline__ bool fix_fits(const P2GParticle& q, const FixScale& sc) {
+  bool ok = fabsf(q.m) * sc.m * kWmax < kFastLimit;
+  if (KIND == kP2gFull) {
+    const float mv = fmaxf(fabsf(q.mv[0]), fmaxf(fabsf(q.mv[1]), fabsf(q.mv[2])));
+    ok = ok && mv * sc.p * kWmax < kFastLimit && (!q.force || q.a * sc.f * kWmax < kFastLimit);
+  }
+  return ok;  // false for non-finite values as well
+}
+
+// The per-lane factors of one particle's contributions in stencil row
+// (b, c), the same operations on every path: t1 = wy wz, t2 = gy wz,
+// t3 = wy gz; mw = m_s t1, pv = mv_s t1, kk = A_s[r][0] t1,
+// hh = A_s[r][1] t2 + A_s[r][2] t3 (scaled quantities, _s).
+struct RowFactors {
+  float mw, pv[3], kk[3], hh[3];
+};
+__device__ __forceinline__ void row_factors(float ms, const float mvs[3], const float As[3][3], float wyb, float gyb,
+                                            float wzc, float gzc, bool mass_only, RowFactors& f) {
+  const float t1 = __fmul_rn(wyb, wzc);
+  f.mw = __fmul_rn(ms, t1);
+  if (mass_only) return;
+  const float t2 = __fmul_rn(gyb, wzc), t3 = __fmul_rn(wyb, gzc);
+#pragma unroll
+  for (int r = 0; r < 3; r++) {
+    f.pv[r] = __fmul_rn(mvs[r], t1);
+    f.kk[r] = __fmul_rn(As[r][0], t1);
+    f.hh[r] = __fmaf_rn(As[r][1], t2, __fmul_rn(As[r][2], t3));
+  }
+}
+// Rounded contributions (as magic-offset bits) at node x-weights (wxa, gxa).
+__device__ __forceinline__ int fix_mass(float wxa, const RowFactors& f) {
+  return __float_as_int(__fmaf_rn(wxa, f.mw, kMagic));
+}
+__device__ __forceinline__ int fix_mom(float wxa, const RowFactors& f, int r) {
+  return __float_as_int(__fmaf_rn(wxa, f.pv[r], kMagic));
+}
+__device__ __forceinline__ int fix_force(float wxa, float gxa, const RowFactors& f, int r) {
+  return __float_as_int(__fmaf_rn(gxa, f.kk[r], __fmaf_rn(wxa, f.hh[r], kMagic)));
+}
+
+// Scatter of one particle's 64 stencil nodes straight into acc (global
+// atomics), for a particle outside its work item's tile. FAST: the particle
+// fits the fast path's range and its contributions are rounded exactly as
+// the tile path rounds them; otherwise (wide) each contribution is rounded in
+// double precision to int64. ms, mvs, As: the scaled quantities.
+template <int KIND, bool FAST>
+__device__ __forceinline__ void scatter_fix(const SceneDev& S, float ms, const float mvs[3], const float As[3][3],
+                                            const AxisW& w, const int base[3]) {
+  constexpr bool mo = KIND == kP2gMass;
+  for (int c = 0; c < 4; c++)
+    for (int b = 0; b < 4; b++) {
+      const int g1 = base[1] - 1 + b, g2 = base[2] - 1 + c;
+      if (g1 < 0 || g2 < 0 || g1 >= S.dim[1] || g2 >= S.dim[2]) continue;
+      RowFactors f;
+      row_factors(ms, mvs, As, sel4(b, w.wy[0], w.wy[1], w.wy[2], w.wy[3]), sel4(b, w.gy[0], w.gy[1], w.gy[2], w.gy[3]),
+                  sel4(c, w.wz[0], w.wz[1], w.wz[2], w.wz[3]), sel4(c, w.gz[0], w.gz[1], w.gz[2], w.gz[3]), mo, f);
+      for (int a = 0; a < 4; a++) {
+        const int g0 = base[0] - 1 + a;
+        if (g0 < 0 || g0 >= S.dim[0]) continue;
+        const float wxa = sel4(a, w.wx[0], w.wx[1], w.wx[2], w.wx[3]);
+        const float gxa = sel4(a, w.gx[0], w.gx[1], w.gx[2], w.gx[3]);
+        long long v[7] = {0, 0, 0, 0, 0, 0, 0};
+        if (FAST) {
+          v[0] = fix_mass(wxa, f) - kMagicBits;
+          if (!mo)
+#pragma unroll
+            for (int r = 0; r < 3; r++) {
+              v[1 + r] = fix_mom(wxa, f, r) - kMagicBits;
+              v[4 + r] = fix_force(wxa, gxa, f, r) - kMagicBits;
+            }
+        } else {
+          auto wide = [](double x) { return isfinite(x) && fabs(x) < 4.0e18 ? __double2ll_rn(x) : 0ll; };
+          v[0] = wide((double)wxa * (double)f.mw);
+          if (!mo)
+#pragma unroll
+            for (int r = 0; r < 3; r++) {
+              v[1 + r] = wide((double)wxa * (double)f.pv[r]);
+              const double h = (double)wide((double)wxa * (double)f.hh[r]);
+              v[4 + r] = wide(fma((double)gxa, (double)f.kk[r], h));
+            }
+        }
+        if (!(v[0] | v[1] | v[2] | v[3] | v[4] | v[5] | v[6])) continue;
+        const int blk = block_id(S, g0 >> 2, g1 >> 2, g2 >> 2);
+        acc_add(S, blk, (g0 & 3) + 4 * (g1 & 3) + 16 * (g2 & 3), v[0], v[1], v[2], v[3], v[4], v[5], v[6], mo);
+        S.blk_flag[blk] = 1;
+      }
+    }
+}
+
+// The semi-implicit solve's K u scatter for a particle outside its tile:
+// float sums into the low 4 bytes of acc's force words (free between the
+// grid update and the next P2G; the solve's node passes read and clear them).
+__device__ __forceinline__ void scatter_force(const SceneDev& S, const P2GParticle& q, const AxisW& w, const int base[3]) {
+  if (!q.force) return;
   for (int c = 0; c < 4; c++)
     for (int b = 0; b < 4; b++)
       for (int a = 0; a < 4; a++) {
@@ -274,22 +477,13 @@ __device__ __forceinline__ void scatter_global(const SceneDev& S, const P2GParti
         const float gyb = sel4(b, w.gy[0], w.gy[1], w.gy[2], w.gy[3]);
         const float wzc = sel4(c, w.wz[0], w.wz[1], w.wz[2], w.wz[3]);
         const float gzc = sel4(c, w.gz[0], w.gz[1], w.gz[2], w.gz[3]);
-        const float wgt = wxa * wyb * wzc;
-        const int blk = block_id(S, g0 >> 2, g1 >> 2, g2 >> 2);
-        float* dst = S.acc + (size_t)blk * kAccBlockFloats + (g0 & 3) + 4 * (g1 & 3) + 16 * (g2 & 3);
-        if (KIND != kP2gForce) {
-          atomicAdd(dst, q.m * wgt);
-          S.blk_flag[blk] = 1;
-        }
-        if (KIND == kP2gMass) continue;
         const float gw[3] = {gxa * wyb * wzc, wxa * gyb * wzc, wxa * wyb * gzc};
-        if (KIND == kP2gFull)
+        const int blk = block_id(S, g0 >> 2, g1 >> 2, g2 >> 2);
+        float* dst = reinterpret_cast<float*>(S.acc + (size_t)blk * kAccBlockWords + 2 * kBlockNodes +
+                                              (g0 & 3) + 4 * (g1 & 3) + 16 * (g2 & 3));
 #pragma unroll
-          for (int r = 0; r < 3; r++) atomicAdd(dst + (1 + r) * kBlockNodes, q.mv[r] * wgt);
-        if (q.force)
-#pragma unroll
-          for (int r = 0; r < 3; r++)
-            atomicAdd(dst + (4 + r) * kBlockNodes, q.A[r][0] * gw[0] + q.A[r][1] * gw[1] + q.A[r][2] * gw[2]);
+        for (int r = 0; r < 3; r++)
+          atomicAdd(dst + 2 * r * kBlockNodes, q.A[r][0] * gw[0] + q.A[r][1] * gw[1] + q.A[r][2] * gw[2]);
       }
 }
 
@@ -297,7 +491,10 @@ __device__ __forceinline__ void scatter_global(const SceneDev& S, const P2GParti
 struct ItemShared {
   float stage[27][kOutBlockFloats];  // G2P: the pool blocks around the home block
   float4 pd[kItemMax][kPd];          // P2G: per-particle data, in tile-cell order
-  float tile[kAccFields * kTile3];   // P2G sums of the tile's nodes
+  union {
+    int tilei[kAccFields * kTile3];  // P2G sums of the tile's nodes (fixed point: mass, momentum, force) ...
+    float tile[kAccFields * kTile3]; // ... or float (the semi-implicit solve's K u)
+  };
   int cstart[kCells + 1];            // first pd slot of each tile cell
   int ccount[kCells];                // particles per tile cell (zero between items)
   int wsum[kItemMax / 32];
@@ -310,6 +507,10 @@ struct ItemShared {
   int4 item_q[2];                    // this and the next work item of the CTA
   int scene_q[2];                    // ... and their scenes
   int coll_scene;                    // scene whose colliders sit in coll
+  FixScale fscale;                   // fixed-point scales of coll_scene's P2G in this launch
+  unsigned seen[3];                  // largest mass, |v|, force-term bound of coll_scene's particles (bits) ...
+  unsigned pushed[3];                // ... and the part of them already recorded in FixState
+  int next_same;                     // the CTA's next work item continues this item's home-block run
   int abort;                         // 1 + parity of a copy wait that ran out, else 0
   uint64_t bar;
   snow_collider coll[kShColliders];
@@ -631,55 +832,74 @@ __device__ __forceinline__ void advance_particle(const SceneDev& S, int p, const
 
 // Adds the particles of one tile cell (list slots j0..j1) to this lane's
 // x-row (b, c) of the cell's 4x4x4 stencil: acc[a] holds node x = lx + a.
-template <int KIND>
-__device__ __forceinline__ void cell_sums(const ItemShared& sh, int j0, int j1, int b, int c,
-                                          float (&acc)[4][kAccFields]) {
+// The semi-implicit solve's K u (float sums of A grad w).
+__device__ __forceinline__ void cell_sums_force(const ItemShared& sh, int j0, int j1, int b, int c,
+                                                float (&acc)[4][kAccFields]) {
   for (int j = j0; j < j1; j++) {
     const float4* d = sh.pd[j];
     const float* df = reinterpret_cast<const float*>(d);
-    const float4 w4 = d[4];
+    const float4 w4 = d[4], g4 = d[5];
     const float wxa[4] = {w4.x, w4.y, w4.z, w4.w};
-    const float wyb = df[6 * 4 + b], wzc = df[8 * 4 + c];
-    const float t1 = wyb * wzc;
-    if (KIND == kP2gMass) {
-      const float mw = d[0].x * t1;
-#pragma unroll
-      for (int a = 0; a < 4; a++) acc[a][0] += wxa[a] * mw;
-      continue;
-    }
-    const float4 g4 = d[5];
     const float gxa[4] = {g4.x, g4.y, g4.z, g4.w};
+    const float wyb = df[6 * 4 + b], wzc = df[8 * 4 + c];
     const float gyb = df[7 * 4 + b], gzc = df[9 * 4 + c];
-    const float t2 = gyb * wzc, t3 = wyb * gzc;
+    const float t1 = wyb * wzc, t2 = gyb * wzc, t3 = wyb * gzc;
     const float4 a1 = d[1], a2 = d[2];
     const float a22 = df[3 * 4];
     // A rows: r0 = (a1.x a1.y a1.z), r1 = (a1.w a2.x a2.y), r2 = (a2.z a2.w a22)
     const float kk[3] = {a1.x * t1, a1.w * t1, a2.z * t1};
     const float hh[3] = {a1.y * t2 + a1.z * t3, a2.x * t2 + a2.y * t3, a2.w * t2 + a22 * t3};
-    if (KIND == kP2gForce) {
 #pragma unroll
-      for (int a = 0; a < 4; a++)
+    for (int a = 0; a < 4; a++)
 #pragma unroll
-        for (int r = 0; r < 3; r++) acc[a][r] += gxa[a] * kk[r] + wxa[a] * hh[r];
-      continue;
-    }
+      for (int r = 0; r < 3; r++) acc[a][r] += gxa[a] * kk[r] + wxa[a] * hh[r];
+  }
+}
+
+// The same for the fixed-point sums (mass alone, or mass, momentum and force):
+// each contribution is rounded by the magic-offset FMA (fix_mass, fix_mom,
+// fix_force) and its bits are added to the unsigned accumulators, so every
+// accumulator gains kMagicBits per particle; np counts the particles summed.
+template <int KIND>
+__device__ __forceinline__ void cell_sums_fix(const ItemShared& sh, int j0, int j1, int b, int c,
+                                              unsigned (&acc)[4][kAccFields], int& np) {
+  constexpr bool mo = KIND == kP2gMass;
+  for (int j = j0; j < j1; j++, np++) {
+    const float4* d = sh.pd[j];
+    const float* df = reinterpret_cast<const float*>(d);
+    const float4 w4 = d[4];
+    const float wxa[4] = {w4.x, w4.y, w4.z, w4.w};
     const float4 d0 = d[0];
-    const float mw = d0.x * t1;
-    const float pv[3] = {d0.y * t1, d0.z * t1, d0.w * t1};
+    const float mvs[3] = {d0.y, d0.z, d0.w};
+    float As[3][3] = {{0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}};
+    float gyb = 0.0f, gzc = 0.0f;
+    float gxa[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    if (!mo) {
+      const float4 a1 = d[1], a2 = d[2], g4 = d[5];
+      As[0][0] = a1.x; As[0][1] = a1.y; As[0][2] = a1.z;
+      As[1][0] = a1.w; As[1][1] = a2.x; As[1][2] = a2.y;
+      As[2][0] = a2.z; As[2][1] = a2.w; As[2][2] = df[3 * 4];
+      gyb = df[7 * 4 + b];
+      gzc = df[9 * 4 + c];
+      gxa[0] = g4.x; gxa[1] = g4.y; gxa[2] = g4.z; gxa[3] = g4.w;
+    }
+    RowFactors f;
+    row_factors(d0.x, mvs, As, df[6 * 4 + b], gyb, df[8 * 4 + c], gzc, mo, f);
 #pragma unroll
     for (int a = 0; a < 4; a++) {
-      acc[a][0] += wxa[a] * mw;
+      acc[a][0] += (unsigned)fix_mass(wxa[a], f);
+      if (mo) continue;
 #pragma unroll
       for (int r = 0; r < 3; r++) {
-        acc[a][1 + r] += wxa[a] * pv[r];
-        acc[a][4 + r] += gxa[a] * kk[r] + wxa[a] * hh[r];
+        acc[a][1 + r] += (unsigned)fix_mom(wxa[a], f, r);
+        acc[a][4 + r] += (unsigned)fix_force(wxa[a], gxa[a], f, r);
       }
     }
   }
 }
 
 // Adds the 4 nodes of this lane's row (tile nodes t0 .. t0 + 3) to the
-// shared tile and clears them.
+// shared tile and clears them (float sums).
 template <int NF>
 __device__ __forceinline__ void row_flush(ItemShared& sh, int t0, float (&acc)[4][kAccFields]) {
 #pragma unroll
@@ -691,53 +911,85 @@ __device__ __forceinline__ void row_flush(ItemShared& sh, int t0, float (&acc)[4
     }
   }
 }
+// ... fixed-point sums: `base` = np kMagicBits, the offset every accumulator
+// carries (a cleared accumulator restarts at it).
+template <int NF>
+__device__ __forceinline__ void row_flush_fix(ItemShared& sh, int t0, unsigned (&acc)[4][kAccFields], unsigned base) {
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+#pragma unroll
+    for (int f = 0; f < NF; f++) {
+      atomicAdd(&sh.tilei[f * kTile3 + t0 + a], (int)(acc[a][f] - base));
+      acc[a][f] = base;
+    }
+  }
+}
 
 __device__ __forceinline__ int cell_row_node(int ci, int b, int c) {
   const int lx = ci % kCellsPerAxis, ly = (ci / kCellsPerAxis) % kCellsPerAxis, lz = ci / (kCellsPerAxis * kCellsPerAxis);
   return lx + kTile * (ly + b) + kTile * kTile * (lz + c);
 }
 
-// P2G of the item's particles into acc (every thread of the CTA calls it;
-// thread i holds particle i of the item when `have`):
-//   1. each particle inside the tile counts itself in its base cell (the
-//      others scatter straight to acc);
-//   2. a scan of the cell counts gives each cell's first slot and lists the
-//      occupied cells; each particle stores its mass, momentum, A and axis
-//      weights at its slot, so the particles lie in tile-cell order;
+// P2G of the item's particles into the shared tile (every thread of the CTA
+// calls it; thread i holds particle i of the item when `have`):
+//   1. each particle inside the tile whose contributions fit the fast
+//      path's range counts itself in its base cell; the others scatter
+//      straight to acc (scatter_fix; K u: scatter_force);
+//   2. a scan of the cell counts gives each cell its first slot and lists the
+//      occupied cells; each particle stores its (scaled) mass, momentum, A
+//      and axis weights at its slot, so the particles lie in tile-cell order;
 //   3. each half-warp owns one occupied cell at a time: lane l sums the
 //      x-row (b, c) = (l & 3, l >> 2) of the cell's stencil over the cell's
-//      particles in registers and adds the row to the shared tile;
-//   4. the tile's non-empty nodes are added to acc (row by row, vector
-//      atomics) and their blocks flagged. The caller separates this item's
-//      flush from the next item's use of the tile with a barrier.
-// `between` runs between steps 3 and 4, long after the staged G2P tile was
-// last read (the fused kernel issues the next item's copies there).
-// Returns false (at its first barrier, before any shared or global write
-// beyond the cell counts and fall-back scatters) when a copy wait of the CTA
-// ran out (sh.abort): the caller then stops the CTA.
-template <int KIND, class Between>
-__device__ __forceinline__ bool p2g_tile_pass(ItemShared& sh, const SceneDev& S, int bx, int by, int bz, bool have,
-                                              const P2GParticle& q, const AxisW& w, const int base[3],
-                                              Between between) {
+//      particles in registers and adds the row to the shared tile.
+// The tile keeps accumulating until p2g_tile_flush adds it to acc, so the
+// items of one home block can share it. Returns false (at its first barrier,
+// before any write beyond the cell counts and the straight scatters) when a
+// copy wait of the CTA ran out (sh.abort): the caller then stops the CTA.
+// Ends with a barrier.
+template <int KIND>
+__device__ __forceinline__ bool p2g_tile_accumulate(ItemShared& sh, const SceneDev& S, int bx, int by, int bz,
+                                                    bool have, const P2GParticle& q, const AxisW& w,
+                                                    const int base[3], const FixScale& sc) {
   constexpr int nf = P2gFields<KIND>::nf;
-  constexpr int f0 = P2gFields<KIND>::acc_first;
+  constexpr bool fix = KIND != kP2gForce;
   const int ox = 4 * bx - 2, oy = 4 * by - 2, oz = 4 * bz - 2;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int my_cell = -1, my_rank = 0;
+  // the particle's quantities as the tile stores them (fixed point: scaled)
+  float ms = 0.0f, mvs[3] = {0.0f, 0.0f, 0.0f}, As[3][3];
+#pragma unroll
+  for (int r = 0; r < 3; r++)
+#pragma unroll
+    for (int c = 0; c < 3; c++) As[r][c] = fix ? (q.force ? q.A[r][c] * sc.f : 0.0f) : q.A[r][c];
+  if (fix) {
+    ms = q.m * sc.m;
+#pragma unroll
+    for (int r = 0; r < 3; r++) mvs[r] = q.mv[r] * sc.p;
+  }
   if (have) {
+    const bool fast = !fix || fix_fits<KIND>(q, sc);
     const int lx = base[0] - 1 - ox, ly = base[1] - 1 - oy, lz = base[2] - 1 - oz;
-    if (lx >= 0 && ly >= 0 && lz >= 0 && lx < kCellsPerAxis && ly < kCellsPerAxis && lz < kCellsPerAxis) {
+    const bool inside = lx >= 0 && ly >= 0 && lz >= 0 && lx < kCellsPerAxis && ly < kCellsPerAxis && lz < kCellsPerAxis;
+    if (inside && fast) {
       my_cell = lx + kCellsPerAxis * ly + kCellsPerAxis * kCellsPerAxis * lz;
       my_rank = atomicAdd(&sh.ccount[my_cell], 1);
     } else {
-      // the particle drifted out of its home block's tile since the last binning
-      atomicAdd(&S.counters[CNT_FALLBACK], 1);
-      scatter_global<KIND>(S, q, w, base);
+      // the particle drifted out of its home block's tile since the last
+      // binning, or outgrew the fast path's range
+      if (!inside) atomicAdd(&S.counters[CNT_FALLBACK], 1);
+      if (!fix)
+        scatter_force(S, q, w, base);
+      else if (fast)
+        scatter_fix<KIND, true>(S, ms, mvs, As, w, base);
+      else {
+        atomicAdd(&S.fix->wide, 1u);
+        scatter_fix<KIND, false>(S, ms, mvs, As, w, base);
+      }
     }
   }
   __syncthreads();  // counts done
   if (sh.abort) return false;  // a copy wait ran out
-  if (threadIdx.x == 32) sh.nrows = 0;  // the previous item's flush is long done
+  if (threadIdx.x == 32) sh.nrows = 0;  // the previous flush is long done
   // exclusive scan of the cell counts and list of the occupied cells, one
   // cell per thread
   const int t = threadIdx.x;
@@ -772,12 +1024,12 @@ __device__ __forceinline__ bool p2g_tile_pass(ItemShared& sh, const SceneDev& S,
     float4* d = sh.pd[sh.cstart[my_cell] + my_rank];
     const bool f = KIND != kP2gMass && q.force;
     if (KIND == kP2gMass)
-      d[0] = make_float4(q.m, 0.0f, 0.0f, 0.0f);
+      d[0] = make_float4(ms, 0.0f, 0.0f, 0.0f);
     else if (KIND == kP2gFull)
-      d[0] = make_float4(q.m, q.mv[0], q.mv[1], q.mv[2]);
-    d[1] = f ? make_float4(q.A[0][0], q.A[0][1], q.A[0][2], q.A[1][0]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    d[2] = f ? make_float4(q.A[1][1], q.A[1][2], q.A[2][0], q.A[2][1]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    d[3] = make_float4(f ? q.A[2][2] : 0.0f, __int_as_float(my_cell), 0.0f, 0.0f);
+      d[0] = make_float4(ms, mvs[0], mvs[1], mvs[2]);
+    d[1] = f ? make_float4(As[0][0], As[0][1], As[0][2], As[1][0]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    d[2] = f ? make_float4(As[1][1], As[1][2], As[2][0], As[2][1]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    d[3] = make_float4(f ? As[2][2] : 0.0f, __int_as_float(my_cell), 0.0f, 0.0f);
     d[4] = make_float4(w.wx[0], w.wx[1], w.wx[2], w.wx[3]);
     d[5] = make_float4(w.gx[0], w.gx[1], w.gx[2], w.gx[3]);
     d[6] = make_float4(w.wy[0], w.wy[1], w.wy[2], w.wy[3]);
@@ -798,47 +1050,87 @@ __device__ __forceinline__ bool p2g_tile_pass(ItemShared& sh, const SceneDev& S,
     const int nhw = blockDim.x >> 4;
     const int ncells = sh.ncells;
     const int k0 = (ncells * hw) / nhw, k1 = (ncells * (hw + 1)) / nhw;
-    float acc[4][kAccFields];
-#pragma unroll
-    for (int a = 0; a < 4; a++)
-#pragma unroll
-      for (int f = 0; f < kAccFields; f++) acc[a][f] = 0.0f;
     int cur = -1;
-    for (int k = k0; k < k1; k++) {
-      const int ci = sh.cells[k];
-      if (cur >= 0) {
-        if (ci == cur + 1 && ci % kCellsPerAxis != 0) {
-          // only node 0 leaves the window: flush it, slide the rest
+    if (fix) {
+      unsigned acc[4][kAccFields];
 #pragma unroll
-          for (int f = 0; f < NF; f++) {
-            atomicAdd(&sh.tile[f * kTile3 + cell_row_node(cur, b, c)], acc[0][f]);
-            acc[0][f] = acc[1][f];
-            acc[1][f] = acc[2][f];
-            acc[2][f] = acc[3][f];
-            acc[3][f] = 0.0f;
+      for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int f = 0; f < kAccFields; f++) acc[a][f] = 0u;
+      int np = 0;
+      for (int k = k0; k < k1; k++) {
+        const int ci = sh.cells[k];
+        if (cur >= 0) {
+          const unsigned base_bits = (unsigned)np * (unsigned)kMagicBits;
+          if (ci == cur + 1 && ci % kCellsPerAxis != 0) {
+            // only node 0 leaves the window: flush it, slide the rest
+#pragma unroll
+            for (int f = 0; f < NF; f++) {
+              atomicAdd(&sh.tilei[f * kTile3 + cell_row_node(cur, b, c)], (int)(acc[0][f] - base_bits));
+              acc[0][f] = acc[1][f];
+              acc[1][f] = acc[2][f];
+              acc[2][f] = acc[3][f];
+              acc[3][f] = base_bits;
+            }
+          } else {
+            row_flush_fix<NF>(sh, cell_row_node(cur, b, c), acc, base_bits);
           }
-        } else {
-          row_flush<NF>(sh, cell_row_node(cur, b, c), acc);
         }
+        cell_sums_fix<KIND>(sh, sh.cstart[ci], sh.cstart[ci + 1], b, c, acc, np);
+        cur = ci;
       }
-      cell_sums<KIND>(sh, sh.cstart[ci], sh.cstart[ci + 1], b, c, acc);
-      cur = ci;
+      if (cur >= 0) row_flush_fix<NF>(sh, cell_row_node(cur, b, c), acc, (unsigned)np * (unsigned)kMagicBits);
+    } else {
+      float acc[4][kAccFields];
+#pragma unroll
+      for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int f = 0; f < kAccFields; f++) acc[a][f] = 0.0f;
+      for (int k = k0; k < k1; k++) {
+        const int ci = sh.cells[k];
+        if (cur >= 0) {
+          if (ci == cur + 1 && ci % kCellsPerAxis != 0) {
+#pragma unroll
+            for (int f = 0; f < NF; f++) {
+              atomicAdd(&sh.tile[f * kTile3 + cell_row_node(cur, b, c)], acc[0][f]);
+              acc[0][f] = acc[1][f];
+              acc[1][f] = acc[2][f];
+              acc[2][f] = acc[3][f];
+              acc[3][f] = 0.0f;
+            }
+          } else {
+            row_flush<NF>(sh, cell_row_node(cur, b, c), acc);
+          }
+        }
+        cell_sums_force(sh, sh.cstart[ci], sh.cstart[ci + 1], b, c, acc);
+        cur = ci;
+      }
+      if (cur >= 0) row_flush<NF>(sh, cell_row_node(cur, b, c), acc);
     }
-    if (cur >= 0) row_flush<NF>(sh, cell_row_node(cur, b, c), acc);
   }
   __syncthreads();
-  between();
-  // 4a. the tile rows (ty, tz) with nodes that hold mass (with KIND ==
-  // kP2gForce: a non-zero vector) and lie in the grid
+  return true;
+}
+
+// Adds the tile's non-zero nodes that lie in the grid to acc and flags
+// their blocks (fixed point: each node's sums as two packed int32 pairs and
+// three int64 words; K u: three float adds into the force words). Every
+// thread of the CTA calls it after p2g_tile_accumulate's closing barrier;
+// the caller separates it from the next use of the tile with a barrier.
+template <int KIND>
+__device__ __forceinline__ void p2g_tile_flush(ItemShared& sh, const SceneDev& S, int bx, int by, int bz) {
+  constexpr int nf = P2gFields<KIND>::nf;
+  const int ox = 4 * bx - 2, oy = 4 * by - 2, oz = 4 * bz - 2;
+  // the tile rows (ty, tz) in the grid, with their non-zero nodes in the grid
   for (int r = threadIdx.x; r < kTile * kTile; r += blockDim.x) {
     const int g1 = oy + r % kTile, g2 = oz + r / kTile;
     uint32_t mask = 0;
     if (g1 >= 0 && g2 >= 0 && g1 < S.dim[1] && g2 < S.dim[2]) {
-      const float* row = &sh.tile[r * kTile];
 #pragma unroll
       for (int x = 0; x < kTile; x++) {
-        bool nz = row[x] != 0.0f;
-        if (KIND == kP2gForce) nz = nz || row[kTile3 + x] != 0.0f || row[2 * kTile3 + x] != 0.0f;
+        int nz = 0;
+#pragma unroll
+        for (int f = 0; f < nf; f++) nz |= sh.tilei[f * kTile3 + r * kTile + x];  // float zero has zero bits too
         if (nz && ox + x >= 0 && ox + x < S.dim[0]) mask |= 1u << x;
       }
     }
@@ -849,39 +1141,35 @@ __device__ __forceinline__ bool p2g_tile_pass(ItemShared& sh, const SceneDev& S,
     }
   }
   __syncthreads();
-  // 4b. one (field, row) per thread: the row's nodes x = 4bx-2 .. 4bx+6 lie
-  // in blocks bx-1 (local x 2, 3), bx (0..3) and bx+1 (0..2); each part is one
-  // vector atomic into acc (nodes without mass or outside the grid add 0, as
-  // does the unused fourth lane of the last part).
+  // one node per thread: consecutive threads take consecutive x of a row
   const int nrows = sh.nrows;
-  for (int task = threadIdx.x; task < nf * nrows; task += blockDim.x) {
-    const int f = task / nrows, k = task % nrows;
+  for (int task = threadIdx.x; task < nrows * kTile; task += blockDim.x) {
+    const int k = task / kTile, x = task % kTile;
+    if (!((sh.rowmask[k] >> x) & 1u)) continue;
     const int r = sh.rows[k];
-    const uint32_t mask = sh.rowmask[k];
-    const float* row = &sh.tile[f * kTile3 + r * kTile];
-    float v[kTile];
+    const int t = r * kTile + x;
+    const int g0 = ox + x, g1 = oy + r % kTile, g2 = oz + r / kTile;
+    const int blk = block_id(S, g0 >> 2, g1 >> 2, g2 >> 2);
+    const int node = (g0 & 3) + 4 * (g1 & 3) + 16 * (g2 & 3);
+    unsigned long long* a = S.acc + (size_t)blk * kAccBlockWords + node;
+    if (KIND == kP2gForce) {
+      float* fw = reinterpret_cast<float*>(a + 2 * kBlockNodes);
 #pragma unroll
-    for (int x = 0; x < kTile; x++) v[x] = ((mask >> x) & 1u) ? row[x] : 0.0f;
-    const int g1 = oy + r % kTile, g2 = oz + r / kTile;
-    float* base = S.acc + (f0 + f) * kBlockNodes + 4 * (g1 & 3) + 16 * (g2 & 3);
-    const bool flag = KIND != kP2gForce && f == 0;  // K u lands only in blocks active already
-    if (mask & 0x3u) {
-      const int blk = block_id(S, bx - 1, g1 >> 2, g2 >> 2);
-      atomicAdd(reinterpret_cast<float2*>(base + (size_t)blk * kAccBlockFloats + 2), make_float2(v[0], v[1]));
-      if (flag) S.blk_flag[blk] = 1;
+      for (int f = 0; f < 3; f++) atomicAdd(fw + 2 * f * kBlockNodes, sh.tile[f * kTile3 + t]);
+      continue;  // K u lands only in blocks active already
     }
-    if (mask & 0x3cu) {
-      const int blk = block_id(S, bx, g1 >> 2, g2 >> 2);
-      atomicAdd(reinterpret_cast<float4*>(base + (size_t)blk * kAccBlockFloats), make_float4(v[2], v[3], v[4], v[5]));
-      if (flag) S.blk_flag[blk] = 1;
+    if (KIND == kP2gMass) {
+      atomicAdd(a, (unsigned long long)(long long)sh.tilei[t]);
+    } else {
+      const int* ti = sh.tilei + t;
+      atomicAdd(a, pack2(ti[kTile3], ti[0]));
+      atomicAdd(a + kBlockNodes, pack2(ti[3 * kTile3], ti[2 * kTile3]));
+#pragma unroll
+      for (int f = 0; f < 3; f++)
+        atomicAdd(a + (2 + f) * kBlockNodes, (unsigned long long)(long long)ti[(4 + f) * kTile3]);
     }
-    if (mask & 0x1c0u) {
-      const int blk = block_id(S, bx + 1, g1 >> 2, g2 >> 2);
-      atomicAdd(reinterpret_cast<float4*>(base + (size_t)blk * kAccBlockFloats), make_float4(v[6], v[7], v[8], 0.0f));
-      if (flag) S.blk_flag[blk] = 1;
-    }
+    S.blk_flag[blk] = 1;
   }
-  return true;
 }
 }  // namespace
 }  // namespace snow

@@ -3,9 +3,11 @@
 // quantisation, on a blocked grid.
 //
 // Grid layout in HBM. The grid is cut into 4x4x4-node blocks.
-//   acc      dense, one 1792-byte record per block: the P2G sums (m, p, f),
-//            field-major (7 x 64 floats). All zero between steps: the grid
-//            update clears what it consumes.
+//   acc      dense, one 2560-byte record per block: the P2G sums (m, p, f)
+//            as fixed-point integers (five 64-bit words per node, word-major:
+//            packed int32 pairs (m | p_x), (p_y | p_z); int64 f_x, f_y, f_z),
+//            so that they do not depend on the order they are added in. All
+//            zero between steps: the grid update clears what it consumes.
 //   blk_flag blocks that received P2G sums (set by the P2G tile flush).
 //   compact  turns the flags into the active-block list and gives each
 //            active block a slot in the output pool.
@@ -21,7 +23,10 @@
 //                the SVD clamp, J_p, velocity, colliders, position (particle
 //                advance), then scatter the updated particles (P2G of the
 //                next step) into a 9^3-node shared tile, cell by cell, and
-//                add the tile to acc.
+//                add the tile to acc. A CTA takes a contiguous range of
+//                items; consecutive items of one home block (a run) share
+//                the staged grid blocks and the tile, which is added to acc
+//                once per run.
 // Separate P2G and G2P kernels serve the first step after set-up and the
 // per-kernel dispatch entry point.
 #include "snow_internal.h"
@@ -60,6 +65,14 @@ __global__ void k_begin_step(const SceneDev* __restrict__ scenes, int nscenes, i
     S.counters[CNT_ACTIVE] = 0;
     S.counters[CNT_OVERFLOW] = 0;
     S.counters[CNT_BINNED] = 0;
+    // the magnitudes of the particles the pending P2G scattered become the
+    // ones this step's P2G chooses its fixed-point scales from
+    FixState& f = *S.fix;
+    f.m_prev = f.m_cur;
+    f.v_prev = f.v_cur;
+    f.a_prev = f.a_cur;
+    f.m_cur = f.v_cur = f.a_cur = 0u;
+    f.vstar = 0u;
   }
   if (rigid)  // rigidAdvance.glsl:14-18
     for (int i = threadIdx.x; i < S.ncoll; i += blockDim.x)
@@ -112,31 +125,73 @@ __global__ void k_compact(const SceneDev* __restrict__ scenes, const int* __rest
   }
 }
 
+// Largest mass, |v|, force-term bound and initial volume of the particles a
+// P2G of the stored state scatters (with_stress: A from an SVD of F_E, as
+// that P2G computes it), into FixState's *_prev and *_cur (zeroed before).
+__global__ void __launch_bounds__(256) k_fix_measure(const SceneDev* __restrict__ sd, int with_stress) {
+  const SceneDev& S = *sd;
+  float mm = 0.0f, vm = 0.0f, am = 0.0f, v0 = 0.0f;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < S.n; p += gridDim.x * blockDim.x) {
+    const float4 xm = S.xm[p];
+    if (!(fabsf(xm.w) <= 100.0f)) continue;  // not scattered (p2gTransfer.glsl:64-66)
+    const float4 vv = S.vv[p];
+    mm = fmaxf(mm, fabsf(xm.w));
+    vm = fmaxf(vm, sqrtf(vv.x * vv.x + vv.y * vv.y + vv.z * vv.z));
+    v0 = fmaxf(v0, vv.w);
+    if (with_stress) am = fmaxf(am, p2g_particle(S, p, xm, false).a);
+  }
+  const unsigned bm = __reduce_max_sync(0xffffffffu, __float_as_uint(mm));
+  const unsigned bv = __reduce_max_sync(0xffffffffu, __float_as_uint(vm));
+  const unsigned ba = __reduce_max_sync(0xffffffffu, __float_as_uint(am));
+  const unsigned b0 = __reduce_max_sync(0xffffffffu, __float_as_uint(v0));
+  if ((threadIdx.x & 31) == 0) {
+    FixState& f = *S.fix;
+    atomicMax(&f.m_prev, bm);
+    atomicMax(&f.m_cur, bm);
+    atomicMax(&f.v_prev, bv);
+    atomicMax(&f.v_cur, bv);
+    atomicMax(&f.a_prev, ba);
+    atomicMax(&f.a_cur, ba);
+    atomicMax(&f.v0max, b0);
+  }
+}
+
 // P2G of the stored particle state (p2gTransfer.glsl:44-151, or
-// gMassCompute.glsl:33-84 when MASS_ONLY).
+// gMassCompute.glsl:33-84 when MASS_ONLY), at the scales k_fix_measure's
+// magnitudes give; the CTA that takes a scene's first item records them for
+// the grid update.
 template <bool MASS_ONLY>
 __global__ void __launch_bounds__(kItemMax, 2) k_p2g(const SceneDev* __restrict__ scenes,
                                                   const int* __restrict__ item_prefix, int nscenes) {
   extern __shared__ float4 smem_raw[];
   ItemShared& sh = *reinterpret_cast<ItemShared*>(smem_raw);
   tile_init(sh);
+  constexpr int KIND = MASS_ONLY ? kP2gMass : kP2gFull;
   const int total = item_prefix[nscenes];
   for (int u = blockIdx.x; u < total; u += gridDim.x) {
     const int s = find_scene(item_prefix, nscenes, u);
     const SceneDev& S = scenes[s];
     const int4 it = S.items[u - item_prefix[s]];
-    tile_zero(sh, MASS_ONLY ? 1 : kAccFields);
+    const FixScale sc = measured_scales(S);
+    if (u == item_prefix[s] && threadIdx.x == 0) {
+      S.fix->scale[0] = sc.m;
+      S.fix->scale[1] = sc.p;
+      S.fix->scale[2] = sc.f;
+    }
+    tile_zero(sh, P2gFields<KIND>::nf);
     int bx, by, bz;
     home_coords(S, it.x, bx, by, bz);
     const int i = threadIdx.x;
     bool have = false;
     P2GParticle q;
+    q.force = false;
+    q.a = 0.0f;
     AxisW w;
     int base[3] = {0, 0, 0};
     if (i < min(it.z, kItemMax)) {
       const int p = it.y + i;
       const float4 xm = S.xm[p];
-      if (MASS_ONLY || fabsf(xm.w) <= 100.0f) {  // p2gTransfer.glsl:64-66
+      if (fabsf(xm.w) <= 100.0f) {  // p2gTransfer.glsl:64-66
         float pg[3];
         grid_coords(S, xm, pg, base);
         all_weights(pg, base, w);
@@ -144,7 +199,8 @@ __global__ void __launch_bounds__(kItemMax, 2) k_p2g(const SceneDev* __restrict_
         have = true;
       }
     }
-    p2g_tile_pass<MASS_ONLY ? kP2gMass : kP2gFull>(sh, S, bx, by, bz, have, q, w, base, [] {});
+    p2g_tile_accumulate<KIND>(sh, S, bx, by, bz, have, q, w, base, sc);
+    p2g_tile_flush<KIND>(sh, S, bx, by, bz);
     __syncthreads();
   }
 }
@@ -162,18 +218,31 @@ __global__ void __launch_bounds__(256) k_grid(const SceneDev* __restrict__ scene
     const SceneDev& S = scenes[s];
     const int slot = (int)(u - active_prefix[s]);
     const int b = S.active[slot];
-    float* acc = S.acc + (size_t)b * kAccBlockFloats + node;
-    float v[kAccFields];
+    unsigned long long* acc = S.acc + (size_t)b * kAccBlockWords + node;
+    unsigned long long w[kAccWords];
 #pragma unroll
-    for (int f = 0; f < kAccFields; f++) {
-      v[f] = acc[f * kBlockNodes];
-      acc[f * kBlockNodes] = 0.0f;
+    for (int k = 0; k < kAccWords; k++) {
+      w[k] = acc[k * kBlockNodes];
+      acc[k * kBlockNodes] = 0ull;
     }
     if (clear_only) continue;
+    // the fixed-point sums back to floats (the scales are powers of two)
+    const FixState& fx = *S.fix;
+    const float ism = 1.0f / fx.scale[0], isp = 1.0f / fx.scale[1], isf = 1.0f / fx.scale[2];
+    int mq, pxq, pyq, pzq;
+    unpack2(w[0], pxq, mq);
+    unpack2(w[1], pzq, pyq);
+    const float v[kAccFields] = {(float)mq * ism,
+                                 (float)pxq * isp,
+                                 (float)pyq * isp,
+                                 (float)pzq * isp,
+                                 (float)(long long)w[2] * isf,
+                                 (float)(long long)w[3] * isf,
+                                 (float)(long long)w[4] * isf};
     float2* out = reinterpret_cast<float2*>(S.gout + (size_t)slot * kOutBlockFloats + kOutFields * node);
     const float mi = v[0];
     float vs[3] = {0.0f, 0.0f, 0.0f}, d[3] = {0.0f, 0.0f, 0.0f};
-    if (mi > 0.0f) {
+    if (mq > 0) {
       const float inv = 1.0f / mi;
       const float vold[3] = {v[1] * inv, v[2] * inv, v[3] * inv};
 #pragma unroll
@@ -191,6 +260,10 @@ __global__ void __launch_bounds__(256) k_grid(const SceneDev* __restrict__ scene
     out[0] = make_float2(vs[0], vs[1]);
     out[1] = make_float2(vs[2], d[0]);
     out[2] = make_float2(d[1], d[2]);
+    // the largest |v*| bounds the next P2G's momenta (step_scales); a warp
+    // lies inside one block, so inside one scene
+    const unsigned vb = __reduce_max_sync(0xffffffffu, __float_as_uint(sqrtf(vs[0] * vs[0] + vs[1] * vs[1] + vs[2] * vs[2])));
+    if ((threadIdx.x & 31) == 0 && vb > *(volatile unsigned*)&S.fix->vstar) atomicMax(&S.fix->vstar, vb);
     if (S.crs) {  // semi-implicit: the solve starts from x = v* and applies K to v* first
       const size_t i = (size_t)slot * kBlockNodes + node;
       S.crv[i] = make_float4(vs[0], vs[1], vs[2], mi > 0.0f ? mi : 0.0f);
@@ -221,7 +294,9 @@ __global__ void __launch_bounds__(256) k_volume(const SceneDev* __restrict__ sd)
           const int g0 = base[0] - 1 + a, g1 = base[1] - 1 + b, g2 = base[2] - 1 + c;
           if (!node_in_grid(S, g0, g1, g2)) continue;
           const int blk = block_id(S, g0 >> 2, g1 >> 2, g2 >> 2);
-          const float mi = S.acc[(size_t)blk * kAccBlockFloats + (g0 & 3) + 4 * (g1 & 3) + 16 * (g2 & 3)];
+          int mq, hi;
+          unpack2(S.acc[(size_t)blk * kAccBlockWords + (g0 & 3) + 4 * (g1 & 3) + 16 * (g2 & 3)], hi, mq);
+          const float mi = (float)mq / S.fix->scale[0];
           rho += mi * (sel4(a, w.wx[0], w.wx[1], w.wx[2], w.wx[3]) * sel4(b, w.wy[0], w.wy[1], w.wy[2], w.wy[3]) *
                        sel4(c, w.wz[0], w.wz[1], w.wz[2], w.wz[3]));
         }
@@ -275,10 +350,15 @@ __global__ void __launch_bounds__(kItemMax) k_g2p_advance(const SceneDev* __rest
 // P2G of the next, in one pass over the item's particles. The P2G stress uses
 // the rotation R = W V^T of the advance's SVD: F_E' = W S' V^T with S'
 // diagonal up to the Jacobi residual, whose polar rotation is W V^T.
-// The pool blocks of the CTA's next item are copied into shared memory while
-// this item's P2G runs. BINNED: a step that re-binned some scene; such a
-// scene's particles are read from its binned copies (CNT_BINNED) and, like
-// every scene's, written to its streams.
+// A CTA takes a contiguous range of work items. Consecutive items of one
+// home block form a run: they share the staged pool blocks (copied once, by
+// bulk copies issued while the previous run's last item sums its P2G) and
+// the P2G tile (added to acc once, at the run's end). The P2G sums are fixed
+// point at the scales step_scales gives; the CTA that takes a scene's first
+// item records them for the next grid update, and every CTA records the
+// magnitudes of its particles for the next step's scales. BINNED: a step that
+// re-binned some scene; such a scene's particles are read from its binned
+// copies (CNT_BINNED) and, like every scene's, written to its streams.
 template <bool BINNED>
 __global__ void __launch_bounds__(kItemMax, 2) k_g2p2g(const SceneDev* __restrict__ scenes,
                                                        const int* __restrict__ item_prefix, int nscenes) {
@@ -286,43 +366,61 @@ __global__ void __launch_bounds__(kItemMax, 2) k_g2p2g(const SceneDev* __restric
   ItemShared& sh = *reinterpret_cast<ItemShared*>(smem_raw);
   tile_init(sh);
   const int total = item_prefix[nscenes];
-  if ((int)blockIdx.x >= total) return;
+  const int chunk = (total + (int)gridDim.x - 1) / (int)gridDim.x;
+  const int u0 = min(total, (int)blockIdx.x * chunk), u1 = min(total, u0 + chunk);
+  if (u0 >= u1) return;
   // The last warp, which holds the fewest particles of an item (items are
   // filled from thread 0), looks up the next item and its pool slots.
   const int lane = threadIdx.x & 31;
   const bool lastw = (threadIdx.x >> 5) == (blockDim.x >> 5) - 1;
   if (lastw) {
-    const int s0 = find_scene(item_prefix, nscenes, blockIdx.x);
-    const int4 it0 = scenes[s0].items[blockIdx.x - item_prefix[s0]];
+    const int s0 = find_scene(item_prefix, nscenes, u0);
+    const int4 it0 = scenes[s0].items[u0 - item_prefix[s0]];
     stage_issue(sh, scenes[s0], tile_slot(scenes[s0], it0, lane));
     if (lane == 0) {
       sh.item_q[0] = it0;
       sh.scene_q[0] = s0;
       sh.coll_scene = -1;
+      sh.next_same = 0;
     }
   }
   uint32_t phase = 0;
   int par = 0;
-  for (int u = blockIdx.x; u < total; u += gridDim.x, par ^= 1) {
+  for (int u = u0; u < u1; u++, par ^= 1) {
     __syncthreads();  // this item's queue entry is written; the last flush is done
-    tile_zero(sh, kAccFields);
+    const bool run_start = !sh.next_same;  // uniform across the CTA
     const int s = sh.scene_q[par];
     const SceneDev& S = scenes[s];
     if (s != sh.coll_scene) {  // uniform across the CTA
-      load_colliders(sh, S);
-      if (threadIdx.x == 0) sh.coll_scene = s;
+      if (threadIdx.x == 0) {
+        sh.fscale = step_scales(S);
+        sh.seen[0] = sh.seen[1] = sh.seen[2] = 0u;
+        sh.pushed[0] = sh.pushed[1] = sh.pushed[2] = 0u;
+      }
+      load_colliders(sh, S);  // its closing barrier publishes fscale as well
+      if (threadIdx.x == 0) {
+        sh.coll_scene = s;
+        if (u == item_prefix[s]) {
+          S.fix->scale[0] = sh.fscale.m;
+          S.fix->scale[1] = sh.fscale.p;
+          S.fix->scale[2] = sh.fscale.f;
+        }
+      }
     }
+    if (run_start) tile_zero(sh, kAccFields);
     const int4 it = sh.item_q[par];
-    const int un = u + gridDim.x;
+    const int un = u + 1;
     // the next item's descriptor and pool slots: loaded now, used (and put
     // in shared memory) after this item's per-cell sums, so the loads'
     // latency overlaps this item's work instead of delaying the last warp
     int sn = 0, slot = -1;
     int4 itn = make_int4(0, 0, 0, 0);
-    if (lastw && un < total) {
+    bool same = false;
+    if (lastw && un < u1) {
       sn = find_scene(item_prefix, nscenes, un);
       itn = scenes[sn].items[un - item_prefix[sn]];
-      slot = tile_slot(scenes[sn], itn, lane);
+      same = sn == s && itn.x == it.x;
+      if (!same) slot = tile_slot(scenes[sn], itn, lane);
     }
     int bx, by, bz;
     home_coords(S, it.x, bx, by, bz);
@@ -332,11 +430,14 @@ __global__ void __launch_bounds__(kItemMax, 2) k_g2p2g(const SceneDev* __restric
     PState ps;
     const bool binned = BINNED && particles_binned(S);
     if (mine) ps = load_state(S, p, binned);
-    const bool landed = stage_wait(sh, S, phase);
+    const bool landed = run_start ? stage_wait(sh, S, phase) : true;
     bool have = false;
     P2GParticle q;
+    q.force = false;
+    q.a = 0.0f;
     AxisW wn;
     int nbase[3] = {0, 0, 0};
+    float rec_v = 0.0f;
     if (mine && landed) {
       float pg[3];
       int base[3];
@@ -355,28 +456,46 @@ __global__ void __launch_bounds__(kItemMax, 2) k_g2p2g(const SceneDev* __restric
         q.mv[0] = q.m * adv.vv.x;
         q.mv[1] = q.m * adv.vv.y;
         q.mv[2] = q.m * adv.vv.z;
-        q.force = false;
+        rec_v = sqrtf(adv.vv.x * adv.vv.x + adv.vv.y * adv.vv.y + adv.vv.z * adv.vv.z);
         if (adv.vv.w > 0.0f) p2g_stress(S, adv.fe, adv.R, adv.jp, adv.vv.w, q);
         float npg[3];
         grid_coords(S, adv.xm, npg, nbase);
         all_weights(npg, nbase, wn);
       }
     }
-    const bool done = p2g_tile_pass<kP2gFull>(
-        sh, S, bx, by, bz, have, q, wn, nbase,
-        [&] {
-          if (lastw && un < total) {
-            if (lane == 0) {
-              sh.item_q[par ^ 1] = itn;
-              sh.scene_q[par ^ 1] = sn;
-            }
-            stage_issue(sh, scenes[sn], lane < 27 ? slot : -1);
-          }
-        });
-    if (!done) {  // a copy wait ran out: this item's particles keep their state, the CTA stops
-      stage_abort(sh, S);
+    {  // the magnitudes the next step's scales are chosen from (per warp, then per CTA)
+      const unsigned bm = __reduce_max_sync(0xffffffffu, have ? __float_as_uint(fabsf(q.m)) : 0u);
+      const unsigned bv = __reduce_max_sync(0xffffffffu, __float_as_uint(rec_v));
+      const unsigned ba = __reduce_max_sync(0xffffffffu, __float_as_uint(q.a));
+      if (lane == 0) {
+        atomicMax(&sh.seen[0], bm);
+        atomicMax(&sh.seen[1], bv);
+        atomicMax(&sh.seen[2], ba);
+      }
+    }
+    if (!p2g_tile_accumulate<kP2gFull>(sh, S, bx, by, bz, have, q, wn, nbase, sh.fscale)) {
+      stage_abort(sh, S);  // a copy wait ran out: this item's particles keep their state, the CTA stops
       return;
     }
+    if (lastw) {
+      if (lane == 0) {
+        sh.item_q[par ^ 1] = itn;
+        sh.scene_q[par ^ 1] = sn;
+        sh.next_same = same ? 1 : 0;
+      }
+      if (un < u1 && !same) stage_issue(sh, scenes[sn], lane < 27 ? slot : -1);  // uniform in the warp
+    }
+    if (threadIdx.x == 0) {  // only maxima above what this CTA already recorded go to HBM
+      unsigned* cur[3] = {&S.fix->m_cur, &S.fix->v_cur, &S.fix->a_cur};
+#pragma unroll
+      for (int k = 0; k < 3; k++)
+        if (sh.seen[k] > sh.pushed[k]) {
+          atomicMax(cur[k], sh.seen[k]);
+          sh.pushed[k] = sh.seen[k];
+        }
+    }
+    __syncthreads();  // next_same is visible
+    if (!sh.next_same) p2g_tile_flush<kP2gFull>(sh, S, bx, by, bz);
   }
 }
 
@@ -520,12 +639,19 @@ __global__ void k_download_grid(const SceneDev* __restrict__ sd, float* mass, fl
     const int gi = (int)(g % S.dim[0]), gj = (int)((g / S.dim[0]) % S.dim[1]),
               gk = (int)(g / ((long long)S.dim[0] * S.dim[1]));
     const int blk = block_id(S, gi >> 2, gj >> 2, gk >> 2);
-    const float* acc = S.acc + (size_t)blk * kAccBlockFloats + (gi & 3) + 4 * (gj & 3) + 16 * (gk & 3);
-    if (mass) mass[g] = acc[0];
-    for (int k = 0; k < 3; k++) {
-      if (mom) mom[3 * g + k] = acc[(1 + k) * kBlockNodes];
-      if (force) force[3 * g + k] = acc[(4 + k) * kBlockNodes];
+    const unsigned long long* acc = S.acc + (size_t)blk * kAccBlockWords + (gi & 3) + 4 * (gj & 3) + 16 * (gk & 3);
+    const FixState& fx = *S.fix;
+    int mq, pxq, pyq, pzq;
+    unpack2(acc[0], pxq, mq);
+    unpack2(acc[kBlockNodes], pzq, pyq);
+    if (mass) mass[g] = (float)mq / fx.scale[0];
+    if (mom) {
+      mom[3 * g] = (float)pxq / fx.scale[1];
+      mom[3 * g + 1] = (float)pyq / fx.scale[1];
+      mom[3 * g + 2] = (float)pzq / fx.scale[1];
     }
+    if (force)
+      for (int k = 0; k < 3; k++) force[3 * g + k] = (float)(long long)acc[(2 + k) * kBlockNodes] / fx.scale[2];
   }
 }
 
@@ -593,9 +719,16 @@ void fast_compact(const SceneDev* scenes, const int* block_prefix, int nscenes, 
   k_compact<<<(int)g, 256, 0, st>>>(scenes, block_prefix, nscenes, total_blocks, items_prefix, active_prefix);
 }
 
-void fast_p2g(const SceneDev* scenes, const int* item_prefix, int nscenes, int grid_ctas, bool mass_only,
-              cudaStream_t st) {
+void fast_p2g(const SceneDev* scenes, const SceneDev& sd_host, const int* item_prefix, int nscenes, int grid_ctas,
+              bool mass_only, cudaStream_t st) {
   const int smem = item_smem();
+  // the magnitudes of the particles, from which k_p2g chooses its scales
+  cudaMemsetAsync(&sd_host.fix->m_prev, 0, offsetof(FixState, wide) - offsetof(FixState, m_prev), st);
+  if (sd_host.n > 0) {
+    int g = (sd_host.n + 255) / 256;
+    if (g > num_sms() * 8) g = num_sms() * 8;
+    k_fix_measure<<<g, 256, 0, st>>>(scenes, mass_only ? 0 : 1);
+  }
   if (mass_only)
     k_p2g<true><<<grid_ctas, kItemMax, smem, st>>>(scenes, item_prefix, nscenes);
   else

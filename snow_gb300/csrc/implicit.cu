@@ -280,6 +280,7 @@ __global__ void __launch_bounds__(kItemMax, 2) k_hess(const SceneDev* __restrict
     bool have = false;
     P2GParticle q;
     q.force = false;
+    q.a = 0.0f;
     AxisW w;
     int base[3] = {0, 0, 0};
     if (mine && landed && fabsf(xm.w) <= 100.0f) {  // p2gTransfer.glsl:64-66
@@ -290,16 +291,13 @@ __global__ void __launch_bounds__(kItemMax, 2) k_hess(const SceneDev* __restrict
       hess_gather(sh, S, bx, by, bz, base, w, Gm);
       have = hess_particle(S, it.y + i, binned, Gm, q);
     }
-    const bool done = p2g_tile_pass<kP2gForce>(
-        sh, S, bx, by, bz, have, q, w, base,
-        [&] {
-          if (lastw && un < total)
-            stage_issue(sh, scenes[sn].cru, kImpBlockFloats, lane < 27 ? slot : -1, scenes[sn].tx_unsent);
-        });
-    if (!done) {  // a copy wait ran out: the CTA stops
-      stage_abort(sh, S);
+    if (!p2g_tile_accumulate<kP2gForce>(sh, S, bx, by, bz, have, q, w, base, FixScale{1.0f, 1.0f, 1.0f})) {
+      stage_abort(sh, S);  // a copy wait ran out: the CTA stops
       return;
     }
+    if (lastw && un < total)
+      stage_issue(sh, scenes[sn].cru, kImpBlockFloats, lane < 27 ? slot : -1, scenes[sn].tx_unsent);
+    p2g_tile_flush<kP2gForce>(sh, S, bx, by, bz);
     u = un;
     s = sn;
     it = itn;
@@ -358,13 +356,14 @@ __device__ __forceinline__ void for_active_nodes(const SceneDev* __restrict__ sc
   }
 }
 
-// K u of block `slot` at `node` from acc's force slots (cleared when `take`).
+// K u of block `slot` at `node`: floats in the low 4 bytes of acc's force
+// words (cleared, as whole words, when `take`).
 __device__ __forceinline__ void take_ku(const SceneDev& S, int slot, int node, bool take, float ku[3]) {
-  float* acc = S.acc + (size_t)S.active[slot] * kAccBlockFloats + node;
+  unsigned long long* acc = S.acc + (size_t)S.active[slot] * kAccBlockWords + 2 * kBlockNodes + node;
 #pragma unroll
   for (int k = 0; k < 3; k++) {
-    ku[k] = acc[(4 + k) * kBlockNodes];
-    if (take) acc[(4 + k) * kBlockNodes] = 0.0f;
+    ku[k] = *reinterpret_cast<const float*>(acc + k * kBlockNodes);
+    if (take) acc[k * kBlockNodes] = 0ull;
   }
 }
 
@@ -520,22 +519,29 @@ __global__ void __launch_bounds__(256) k_cr_end(const SceneDev* __restrict__ sce
       scenes, active_prefix, nscenes, [](const SceneDev& S) { return S.crs != nullptr; },
       [](const SceneDev& S, int slot, int node, double&, double&) {
         const float4 xm = S.crv[(size_t)slot * kBlockNodes + node];
-        if (!(xm.w > 0.0f)) return;
-        const int b = S.active[slot];
-        const int bx = b % S.bdim[0], by = (b / S.bdim[0]) % S.bdim[1], bz = b / (S.bdim[0] * S.bdim[1]);
-        const int gi = 4 * bx + (node & 3), gj = 4 * by + ((node >> 2) & 3), gk = 4 * bz + (node >> 4);
-        const float xi[3] = {__fadd_rn(S.gpos[0], __fmul_rn(S.h, (float)gi)),
-                             __fadd_rn(S.gpos[1], __fmul_rn(S.h, (float)gj)),
-                             __fadd_rn(S.gpos[2], __fmul_rn(S.h, (float)gk))};
-        float v[3] = {xm.x, xm.y, xm.z};
-        collide(S.coll, S.ncoll, xi, v);
-        float* o = S.gout + (size_t)slot * kOutBlockFloats + kOutFields * node;
-        const float vs[3] = {o[0], o[1], o[2]};
+        float speed = 0.0f;
+        if (xm.w > 0.0f) {
+          const int b = S.active[slot];
+          const int bx = b % S.bdim[0], by = (b / S.bdim[0]) % S.bdim[1], bz = b / (S.bdim[0] * S.bdim[1]);
+          const int gi = 4 * bx + (node & 3), gj = 4 * by + ((node >> 2) & 3), gk = 4 * bz + (node >> 4);
+          const float xi[3] = {__fadd_rn(S.gpos[0], __fmul_rn(S.h, (float)gi)),
+                               __fadd_rn(S.gpos[1], __fmul_rn(S.h, (float)gj)),
+                               __fadd_rn(S.gpos[2], __fmul_rn(S.h, (float)gk))};
+          float v[3] = {xm.x, xm.y, xm.z};
+          collide(S.coll, S.ncoll, xi, v);
+          float* o = S.gout + (size_t)slot * kOutBlockFloats + kOutFields * node;
+          const float vs[3] = {o[0], o[1], o[2]};
 #pragma unroll
-        for (int k = 0; k < 3; k++) {
-          o[3 + k] += v[k] - vs[k];
-          o[k] = v[k];
+          for (int k = 0; k < 3; k++) {
+            o[3 + k] += v[k] - vs[k];
+            o[k] = v[k];
+          }
+          speed = sqrtf(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
         }
+        // the solved velocity is what G2P reads: it bounds the next P2G's
+        // momenta (a warp lies inside one block, so inside one scene)
+        const unsigned vb = __reduce_max_sync(0xffffffffu, __float_as_uint(speed));
+        if ((threadIdx.x & 31) == 0) atomicMax(&S.fix->vstar, vb);
       },
       [](const SceneDev& S, double*& d0, double*& d1) {
         d0 = &S.crs->bb;  // nothing is added (both sums are zero)

@@ -304,7 +304,8 @@ snow_status fast_alloc_grid(snow_scene* s) {
   snow_status st;
   const size_t nb = (size_t)d.nblocks;
   if ((st = salloc(s, nb, &d.blk_slot)) || (st = salloc(s, nb, &d.blk_flag)) ||
-      (st = salloc(s, nb * kAccBlockFloats, &d.acc)) || (st = salloc(s, nb, &s->bin.bstart)) ||
+      (st = salloc(s, nb * kAccBlockWords, &d.acc)) || (st = salloc(s, (size_t)1, &d.fix)) ||
+      (st = salloc(s, nb, &s->bin.bstart)) ||
       (st = salloc(s, nb, &s->bin.bend)) || (st = salloc(s, nb, &s->bin.home)) ||
       (st = salloc(s, (size_t)kCounterStride, &d.counters)) || (st = salloc(s, (size_t)8, &s->d_prefix)) ||
       (st = salloc(s, (size_t)1, &s->sd_dev)))
@@ -313,7 +314,13 @@ snow_status fast_alloc_grid(snow_scene* s) {
   snow_ctx* ctx = s->ctx;
   CK(cudaMemsetAsync(d.blk_flag, 0, nb * sizeof(int), ctx->stream));
   CK(cudaMemsetAsync(d.blk_slot, 0xff, nb * sizeof(int), ctx->stream));
-  CK(cudaMemsetAsync(d.acc, 0, nb * kAccBlockFloats * sizeof(float), ctx->stream));
+  CK(cudaMemsetAsync(d.acc, 0, nb * kAccBlockWords * sizeof(unsigned long long), ctx->stream));
+  {
+    FixState f{};
+    f.scale[0] = f.scale[1] = f.scale[2] = 1.0f;
+    CK(cudaMemcpyAsync(d.fix, &f, sizeof f, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
   CK(cudaMemsetAsync(d.counters, 0, kCounterStride * sizeof(int), ctx->stream));
   return SNOW_OK;
 }
@@ -369,7 +376,7 @@ void fast_enqueue_compact(snow_scene* s, cudaStream_t st, bool counters_reset = 
   fast_compact(s->sd_dev, s->d_prefix + 6, 1, s->sd.nblocks, s->d_prefix + 0, s->d_prefix + 2, st);
 }
 void fast_enqueue_p2g(snow_scene* s, bool mass_only, cudaStream_t st) {
-  fast_p2g(s->sd_dev, s->d_prefix + 0, 1, item_ctas(s->tune), mass_only, st);
+  fast_p2g(s->sd_dev, s->sd, s->d_prefix + 0, 1, item_ctas(s->tune), mass_only, st);
 }
 void fast_enqueue_grid(snow_scene* s, bool clear_only, cudaStream_t st) {
   fast_grid(s->sd_dev, s->d_prefix + 2, 1, grid_ctas(), clear_only, st);
@@ -705,7 +712,7 @@ size_t snow_scene_footprint(const snow_params* p, size_t n) {
   // An upper bound: particle streams (xm, vv, fa, fb, vq: 16 B, fc: 8 B, pid: 4 B)
   // + binning scratch (2 key + 2 value words, 5 x 16 B + 8 B + 4 B permutation
   // targets, radix histograms) + work items (16 B each) + per block the dense
-  // P2G sums (448 floats), flags, slot and bin tables (5 ints) + the output
+  // fixed-point P2G sums (320 64-bit words), flags, slot and bin tables (5 ints) + the output
   // pool at its largest (every block: 384 floats + 1 int) + the upload's
   // staging copy of the caller's arrays (x, v, m, F_E, F_P: 100 B).
   const double tiles = (double)radix_tiles(n);
@@ -713,7 +720,7 @@ size_t snow_scene_footprint(const snow_params* p, size_t n) {
   // A semi-implicit scene adds per pool block its solver planes (64 nodes x
   // (3 float4 + 3 floats)) and one scalar record.
   const double solver = is_implicit(*p) ? nb * (64 * (48.0 + 12.0)) + sizeof(CrScalars) : 0.0;
-  return (size_t)(n * (92.0 + 108.0 + 100.0) + tiles * 256 * 4.0 + 4096.0 + items * 16.0 + nb * (448 * 4.0 + 5 * 4.0) +
+  return (size_t)(n * (92.0 + 108.0 + 100.0) + tiles * 256 * 4.0 + 4096.0 + items * 16.0 + nb * (kAccBlockWords * 8.0 + 5 * 4.0) +
                   nb * (384 * 4.0 + 4.0) + solver + 1024.0);
 }
 

@@ -48,8 +48,29 @@ void ref_advance(const RefArgs& a, float dt, cudaStream_t st);
 constexpr int kBlockNodes = 64;            // 4 x 4 x 4 nodes per grid block
 constexpr int kAccFields = 7;              // m, p (3), f (3)
 constexpr int kOutFields = 6;              // v* (3), d = v* - alpha p/m (3)
-constexpr int kAccBlockFloats = kAccFields * kBlockNodes;  // 448
+// acc holds the P2G sums as integers (fixed point at per-scene power-of-two
+// scales): per node five 64-bit words, (m | p_x) and (p_y | p_z) as packed
+// pairs of int32 sums (hi * 2^32 + lo) and f_x, f_y, f_z as int64, stored
+// word-major per block.
+constexpr int kAccWords = 5;
+constexpr int kAccBlockWords = kAccWords * kBlockNodes;    // 320 (2560 bytes)
 constexpr int kOutBlockFloats = kOutFields * kBlockNodes;  // 384
+
+// Fixed-point state of one scene's P2G sums. Magnitudes are the bits of
+// non-negative floats (they order like unsigned ints, so atomicMax records
+// maxima); every value here is an order-independent function of the state.
+struct FixState {
+  float scale[3];     // s_m, s_p, s_f of the sums now in acc (integer = round(contribution * s))
+  uint32_t m_prev;    // largest particle mass, |v| and force-term bound a of the particles the
+  uint32_t v_prev;    //   previous P2G scattered (a = max over rows r of max(|A_r0|, |A_r1| + |A_r2|))
+  uint32_t a_prev;
+  uint32_t m_cur;     // the same, recorded by the P2G in flight (moved to *_prev at each step's start)
+  uint32_t v_cur;
+  uint32_t a_cur;
+  uint32_t vstar;     // largest |v*| of this step's grid update (after the semi-implicit solve, if any)
+  uint32_t v0max;     // largest initial particle volume
+  uint32_t wide;      // particles scattered with int64 contributions (outgrew the fast range), cumulative
+};
 
 // Per-scene counters (int32), one row of kCounterStride per scene.
 enum {
@@ -119,7 +140,8 @@ struct SceneDev {
   // blocked grid
   int* blk_slot;    // nblocks: pool slot of the block this step, -1 if inactive
   int* blk_flag;    // nblocks: block received P2G sums since the last compaction
-  float* acc;       // nblocks x 448: P2G sums, field-major per block (dense)
+  unsigned long long* acc;  // nblocks x 320 words: the fixed-point P2G sums, word-major per block (dense)
+  FixState* fix;            // their scales and the magnitudes the next scales are chosen from
   int* active;      // pool_cap: block id of each slot
   float* gout;      // pool_cap x 384: grid-update output, per node (v*, d) as 6 floats
   int pool_cap;
@@ -164,8 +186,11 @@ void fast_gather_counters(const SceneDev* scenes, int nscenes, int* out, cudaStr
 void fast_compact(const SceneDev* scenes, const int* block_prefix, int nscenes, long long total_blocks,
                   int* items_prefix, int* active_prefix,
                   cudaStream_t st);
-void fast_p2g(const SceneDev* scenes, const int* item_prefix, int nscenes, int grid_ctas, bool mass_only,
-              cudaStream_t st);
+// P2G of the stored particle state (set-up, per-kernel dispatches), after a
+// pass over the particles that measures the magnitudes its fixed-point
+// scales are chosen from.
+void fast_p2g(const SceneDev* scenes, const SceneDev& sd_host, const int* item_prefix, int nscenes, int grid_ctas,
+              bool mass_only, cudaStream_t st);
 void fast_grid(const SceneDev* scenes, const int* active_prefix, int nscenes, int grid_ctas, bool clear_only,
                cudaStream_t st);
 void fast_volume(const SceneDev* sd_dev, int n, cudaStream_t st);
