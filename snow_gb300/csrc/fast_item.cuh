@@ -223,22 +223,32 @@ __device__ __forceinline__ void collide_packed(const snow_collider* coll, const 
 // A contribution y (|y| < 2^22 after scaling) is rounded by one FMA against
 // kMagic = 1.5 * 2^23: fma(w, x, kMagic) lies in [2^23, 2^24), where floats
 // are spaced by 1, so its bits minus kMagicBits are round(w x). A force
-// contribution g_x kk + w_x hh is rounded as round(g_x kk + round(w_x hh)).
-// The scales put the largest expected term near 2^20; a particle whose terms
-// reach 2^21 (it outgrew the magnitudes the scale was chosen from) is
-// scattered with int64 contributions rounded in double precision ("wide"),
-// which depends only on the particle itself, so it is as deterministic.
+// contribution g_x kk + w_x hh is rounded as round(g_x kk + round(w_x hh)),
+// each of its two terms below 2^21. The scales put the largest expected
+// mass and momentum contribution near 2^21 and the largest force term near
+// 2^20; a particle whose contributions reach the fast range's limit (it
+// outgrew the magnitudes the scale was chosen from) is scattered with int64
+// contributions rounded in double precision ("wide"), which depends only on
+// the particle itself, so it is as deterministic.
 constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
 constexpr int kMagicBits = 0x4B400000;
 constexpr float kWmax = 0.2962963f;       // (2/3)^3 >= any weight or weight-gradient product
-constexpr float kFastLimit = 2095104.0f;  // 2^21 (1 - 2^-11): bound of one fast-path term
+constexpr float kFastLimit1 = 4190208.0f; // 2^22 (1 - 2^-11): bound of a mass or momentum contribution
+constexpr float kFastLimit2 = 2095104.0f; // 2^21 (1 - 2^-11): bound of one of a force contribution's two terms
 
-// The largest power of two s with x s <= 2^20 (1 for x <= 0 or not finite).
-__device__ __forceinline__ float pow2_scale(float x) {
+// The largest power of two s with x s <= 2^bits (1 for x <= 0 or not finite).
+__device__ __forceinline__ float pow2_scale(float x, int bits) {
   if (!(x > 0.0f) || !isfinite(x)) return 1.0f;
   int e;
-  frexpf(x, &e);  // x = f 2^e, f in [0.5, 1): x 2^(20 - e) in [2^19, 2^20)
-  return ldexpf(1.0f, max(-126, min(127, 20 - e)));
+  frexpf(x, &e);  // x = f 2^e, f in [0.5, 1): x 2^(bits - e) in [2^(bits-1), 2^bits)
+  return ldexpf(1.0f, max(-126, min(127, bits - e)));
+}
+
+// The largest |v*| of the grid update (over FixState::vstar's slots).
+__device__ __forceinline__ float fix_vstar(const FixState& f) {
+  uint32_t m = 0u;
+  for (int k = 0; k < kFixSlots; k++) m = max(m, f.vstar[k]);
+  return __uint_as_float(m);
 }
 
 struct FixScale {
@@ -249,14 +259,14 @@ __device__ __forceinline__ float bits_float(uint32_t b) { return __uint_as_float
 
 // Scales of a P2G that follows a grid update in the same step (the fused
 // kernel): from the magnitudes of the particles the previous P2G scattered
-// (FixState::*_prev) and the grid update's largest |v*|. The momentum scale
-// is a bound, not an estimate: a G2P gives v' = alpha v_p + sum_i w_i (v*_i -
-// alpha p_i/m_i) with sum_i w_i <= 1 and |p_i/m_i| <= max |v_p|, and a
-// collider projection adds at most twice the collider's speed, so
-// |v'| <= 2 alpha max|v_p| + max|v*| + 2 max|v_collider|. The force scale
-// leaves a factor 2 for the growth of the stresses in one step (a particle
-// that outgrows it takes the wide path); the floor 1e-9 E0 V0max keeps it
-// finite for a scene without stress.
+// (FixState::*_prev) and the grid update's largest |v*|. A G2P gives
+// v' = alpha (v_p - sum_i w_i p_i/m_i) + sum_i w_i v*_i, where the first term
+// is the particle's deviation from its grid's old velocity and
+// |sum_i w_i v*_i| <= max |v*|; a collider projection adds at most twice the
+// collider's speed. The momentum scale allows |v'| up to
+// 1.25 max(|v_p|, |v*|) + 2 max|v_collider|, the force scale twice the
+// previous largest stress term (the floor 1e-9 E0 V0max keeps it finite for
+// a scene without stress); a particle beyond either takes the wide path.
 __device__ __forceinline__ FixScale step_scales(const SceneDev& S) {
   const FixState& f = *S.fix;
   const float mmax = bits_float(f.m_prev);
@@ -265,12 +275,12 @@ __device__ __forceinline__ FixScale step_scales(const SceneDev& S) {
     const float* cv = S.coll[i].vel;
     vcoll = fmaxf(vcoll, sqrtf(cv[0] * cv[0] + cv[1] * cv[1] + cv[2] * cv[2]));
   }
-  const float vb = 2.0f * S.alpha * bits_float(f.v_prev) + bits_float(f.vstar) + 2.0f * vcoll;
+  const float vb = 1.25f * fmaxf(bits_float(f.v_prev), fix_vstar(f)) + 2.0f * vcoll;
   const float afloor = 1e-9f * S.young * bits_float(f.v0max);
   FixScale sc;
-  sc.m = pow2_scale(mmax * kWmax);
-  sc.p = pow2_scale(mmax * vb * kWmax);
-  sc.f = pow2_scale(fmaxf(2.0f * bits_float(f.a_prev), afloor) * kWmax);
+  sc.m = pow2_scale(mmax * kWmax, 21);
+  sc.p = pow2_scale(mmax * vb * kWmax, 21);
+  sc.f = pow2_scale(fmaxf(2.0f * bits_float(f.a_prev), afloor) * kWmax, 20);
   return sc;
 }
 
@@ -281,9 +291,9 @@ __device__ __forceinline__ FixScale measured_scales(const SceneDev& S) {
   const float mmax = bits_float(f.m_prev);
   const float afloor = 1e-9f * S.young * bits_float(f.v0max);
   FixScale sc;
-  sc.m = pow2_scale(mmax * kWmax);
-  sc.p = pow2_scale(mmax * bits_float(f.v_prev) * kWmax);
-  sc.f = pow2_scale(fmaxf(bits_float(f.a_prev), afloor) * kWmax);
+  sc.m = pow2_scale(mmax * kWmax, 21);
+  sc.p = pow2_scale(mmax * bits_float(f.v_prev) * kWmax, 21);
+  sc.f = pow2_scale(fmaxf(bits_float(f.a_prev), afloor) * kWmax, 20);
   return sc;
 }
 
@@ -373,10 +383,10 @@ __device__ __forceinline__ P2GParticle p2g_particle(const SceneDev& S, int p, fl
 // range at scales sc (KIND kP2gMass: the mass alone).
 template <int KIND>
 __device__ __forceinline__ bool fix_fits(const P2GParticle& q, const FixScale& sc) {
-  bool ok = fabsf(q.m) * sc.m * kWmax < kFastLimit;
+  bool ok = fabsf(q.m) * sc.m * kWmax < kFastLimit1;
   if (KIND == kP2gFull) {
     const float mv = fmaxf(fabsf(q.mv[0]), fmaxf(fabsf(q.mv[1]), fabsf(q.mv[2])));
-    ok = ok && mv * sc.p * kWmax < kFastLimit && (!q.force || q.a * sc.f * kWmax < kFastLimit);
+    ok = ok && mv * sc.p * kWmax < kFastLimit1 && (!q.force || q.a * sc.f * kWmax < kFastLimit2);
   }
   return ok;  // false for non-finite values as well
 }
@@ -479,6 +489,7 @@ __device__ __forceinline__ void scatter_force(const SceneDev& S, const P2GPartic
         const float gzc = sel4(c, w.gz[0], w.gz[1], w.gz[2], w.gz[3]);
         const float gw[3] = {gxa * wyb * wzc, wxa * gyb * wzc, wxa * wyb * gzc};
         const int blk = block_id(S, g0 >> 2, g1 >> 2, g2 >> 2);
+        if (__ldg(&S.blk_slot[blk]) < 0) continue;  // only active blocks' words are read and cleared by the solve
         float* dst = reinterpret_cast<float*>(S.acc + (size_t)blk * kAccBlockWords + 2 * kBlockNodes +
                                               (g0 & 3) + 4 * (g1 & 3) + 16 * (g2 & 3));
 #pragma unroll
@@ -1153,10 +1164,14 @@ __device__ __forceinline__ void p2g_tile_flush(ItemShared& sh, const SceneDev& S
     const int node = (g0 & 3) + 4 * (g1 & 3) + 16 * (g2 & 3);
     unsigned long long* a = S.acc + (size_t)blk * kAccBlockWords + node;
     if (KIND == kP2gForce) {
+      // K u goes only to blocks active in this step: the solve's node passes
+      // read and clear the words of those alone (a block whose fixed-point
+      // sums all rounded to zero is not active, although its K u may not be)
+      if (__ldg(&S.blk_slot[blk]) < 0) continue;
       float* fw = reinterpret_cast<float*>(a + 2 * kBlockNodes);
 #pragma unroll
       for (int f = 0; f < 3; f++) atomicAdd(fw + 2 * f * kBlockNodes, sh.tile[f * kTile3 + t]);
-      continue;  // K u lands only in blocks active already
+      continue;
     }
     if (KIND == kP2gMass) {
       atomicAdd(a, (unsigned long long)(long long)sh.tilei[t]);

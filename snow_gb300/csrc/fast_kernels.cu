@@ -72,8 +72,8 @@ __global__ void k_begin_step(const SceneDev* __restrict__ scenes, int nscenes, i
     f.v_prev = f.v_cur;
     f.a_prev = f.a_cur;
     f.m_cur = f.v_cur = f.a_cur = 0u;
-    f.vstar = 0u;
   }
+  if (threadIdx.x < kFixSlots) S.fix->vstar[threadIdx.x] = 0u;
   if (rigid)  // rigidAdvance.glsl:14-18
     for (int i = threadIdx.x; i < S.ncoll; i += blockDim.x)
       for (int k = 0; k < 3; k++) S.coll[i].pos[k] = S.coll[i].pos[k] + S.dt * S.coll[i].vel[k];
@@ -263,7 +263,8 @@ __global__ void __launch_bounds__(256) k_grid(const SceneDev* __restrict__ scene
     // the largest |v*| bounds the next P2G's momenta (step_scales); a warp
     // lies inside one block, so inside one scene
     const unsigned vb = __reduce_max_sync(0xffffffffu, __float_as_uint(sqrtf(vs[0] * vs[0] + vs[1] * vs[1] + vs[2] * vs[2])));
-    if ((threadIdx.x & 31) == 0 && vb > *(volatile unsigned*)&S.fix->vstar) atomicMax(&S.fix->vstar, vb);
+    unsigned* slot_max = &S.fix->vstar[blockIdx.x % kFixSlots];
+    if ((threadIdx.x & 31) == 0 && vb > *(volatile unsigned*)slot_max) atomicMax(slot_max, vb);
     if (S.crs) {  // semi-implicit: the solve starts from x = v* and applies K to v* first
       const size_t i = (size_t)slot * kBlockNodes + node;
       S.crv[i] = make_float4(vs[0], vs[1], vs[2], mi > 0.0f ? mi : 0.0f);

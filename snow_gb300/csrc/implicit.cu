@@ -541,7 +541,8 @@ __global__ void __launch_bounds__(256) k_cr_end(const SceneDev* __restrict__ sce
         // the solved velocity is what G2P reads: it bounds the next P2G's
         // momenta (a warp lies inside one block, so inside one scene)
         const unsigned vb = __reduce_max_sync(0xffffffffu, __float_as_uint(speed));
-        if ((threadIdx.x & 31) == 0) atomicMax(&S.fix->vstar, vb);
+        unsigned* slot_max = &S.fix->vstar[blockIdx.x % kFixSlots];
+        if ((threadIdx.x & 31) == 0 && vb > *(volatile unsigned*)slot_max) atomicMax(slot_max, vb);
       },
       [](const SceneDev& S, double*& d0, double*& d1) {
         d0 = &S.crs->bb;  // nothing is added (both sums are zero)

@@ -59,6 +59,7 @@ constexpr int kOutBlockFloats = kOutFields * kBlockNodes;  // 384
 // Fixed-point state of one scene's P2G sums. Magnitudes are the bits of
 // non-negative floats (they order like unsigned ints, so atomicMax records
 // maxima); every value here is an order-independent function of the state.
+constexpr int kFixSlots = 32;
 struct FixState {
   float scale[3];     // s_m, s_p, s_f of the sums now in acc (integer = round(contribution * s))
   uint32_t m_prev;    // largest particle mass, |v| and force-term bound a of the particles the
@@ -67,7 +68,8 @@ struct FixState {
   uint32_t m_cur;     // the same, recorded by the P2G in flight (moved to *_prev at each step's start)
   uint32_t v_cur;
   uint32_t a_cur;
-  uint32_t vstar;     // largest |v*| of this step's grid update (after the semi-implicit solve, if any)
+  uint32_t vstar[kFixSlots];  // largest |v*| of this step's grid update (after the semi-implicit solve,
+                              // if any), spread over slots (CTA index mod kFixSlots) against contention
   uint32_t v0max;     // largest initial particle volume
   uint32_t wide;      // particles scattered with int64 contributions (outgrew the fast range), cumulative
 };
