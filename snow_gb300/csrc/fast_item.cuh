@@ -211,8 +211,10 @@ __device__ __forceinline__ void collide_packed(const snow_collider* coll, const 
 // Every contribution of a particle to a grid node (mass m w, momentum m v w,
 // force A grad w) is rounded to an integer at a per-scene power-of-two scale
 // (s_m, s_p, s_f), and integers are summed: in registers and in the shared
-// tile as int32, into acc as int64 ((m, p_x) and (p_y, p_z) as packed pairs
-// of int32 sums, f_x, f_y, f_z as int64). Integer sums do not depend on the
+// tile as int32 (modulo 2^32; each particle adds a bound of its largest
+// contribution to its item, and a tile is added to acc before the bounds of
+// the particles it holds could reach 2^31, so its sums never wrap), into
+// acc as int64. Integer sums do not depend on the
 // order in which they are formed, so the grid a particle state produces does
 // not depend on how particles are grouped into work items, on the binning
 // schedule, on CTA scheduling or on the other scenes of a batch. The rounding
@@ -223,18 +225,19 @@ __device__ __forceinline__ void collide_packed(const snow_collider* coll, const 
 // A contribution y (|y| < 2^22 after scaling) is rounded by one FMA against
 // kMagic = 1.5 * 2^23: fma(w, x, kMagic) lies in [2^23, 2^24), where floats
 // are spaced by 1, so its bits minus kMagicBits are round(w x). A force
-// contribution g_x kk + w_x hh is rounded as round(g_x kk + round(w_x hh)),
-// each of its two terms below 2^21. The scales put the largest expected
-// mass and momentum contribution near 2^21 and the largest force term near
-// 2^20; a particle whose contributions reach the fast range's limit (it
-// outgrew the magnitudes the scale was chosen from) is scattered with int64
-// contributions rounded in double precision ("wide"), which depends only on
-// the particle itself, so it is as deterministic.
+// contribution g_x kk + w_x hh is rounded as round(g_x kk + round(w_x hh));
+// with a = max over rows r of |A_r0| + |A_r1| + |A_r2|, both terms and their
+// sum are at most a (2/3)^3 s_f. The scales put the largest expected
+// contribution of each kind near 2^21, half the fast range's limit of 2^22;
+// a particle whose contributions reach the limit (it outgrew the magnitudes
+// the scale was chosen from) is scattered with int64 contributions rounded
+// in double precision ("wide"), which depends only on the particle itself,
+// so it is as deterministic.
 constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
 constexpr int kMagicBits = 0x4B400000;
 constexpr float kWmax = 0.2962963f;       // (2/3)^3 >= any weight or weight-gradient product
-constexpr float kFastLimit1 = 4190208.0f; // 2^22 (1 - 2^-11): bound of a mass or momentum contribution
-constexpr float kFastLimit2 = 2095104.0f; // 2^21 (1 - 2^-11): bound of one of a force contribution's two terms
+constexpr float kFastLimit = 4190208.0f;       // 2^22 (1 - 2^-11): bound of a fast-path contribution
+constexpr float kTileSumBound = 2126008832.0f;  // 0.99 * 2^31: bound of a tile's sums of contribution bounds
 
 // The largest power of two s with x s <= 2^bits (1 for x <= 0 or not finite).
 __device__ __forceinline__ float pow2_scale(float x, int bits) {
@@ -242,13 +245,6 @@ __device__ __forceinline__ float pow2_scale(float x, int bits) {
   int e;
   frexpf(x, &e);  // x = f 2^e, f in [0.5, 1): x 2^(bits - e) in [2^(bits-1), 2^bits)
   return ldexpf(1.0f, max(-126, min(127, bits - e)));
-}
-
-// The largest |v*| of the grid update (over FixState::vstar's slots).
-__device__ __forceinline__ float fix_vstar(const FixState& f) {
-  uint32_t m = 0u;
-  for (int k = 0; k < kFixSlots; k++) m = max(m, f.vstar[k]);
-  return __uint_as_float(m);
 }
 
 struct FixScale {
@@ -259,14 +255,16 @@ __device__ __forceinline__ float bits_float(uint32_t b) { return __uint_as_float
 
 // Scales of a P2G that follows a grid update in the same step (the fused
 // kernel): from the magnitudes of the particles the previous P2G scattered
-// (FixState::*_prev) and the grid update's largest |v*|. A G2P gives
-// v' = alpha (v_p - sum_i w_i p_i/m_i) + sum_i w_i v*_i, where the first term
-// is the particle's deviation from its grid's old velocity and
-// |sum_i w_i v*_i| <= max |v*|; a collider projection adds at most twice the
-// collider's speed. The momentum scale allows |v'| up to
-// 1.25 max(|v_p|, |v*|) + 2 max|v_collider|, the force scale twice the
-// previous largest stress term (the floor 1e-9 E0 V0max keeps it finite for
-// a scene without stress); a particle beyond either takes the wide path.
+// (FixState::*_prev). The momentum scale allows particle speeds up to
+// 1.25 max|v_p| + 2 max|v_collider| + 2 |g| dt (a collider projection adds
+// at most twice the collider's speed; the last term keeps the scale finite
+// for a scene at rest, which gravity moves by |g| dt a step).
+// It is taken from particle speeds alone: v* = p/m + dt (f/m + g) of a node
+// that holds a sliver of mass can exceed every particle's speed by orders of
+// magnitude, while the G2P weights such a node by as small a sliver. The
+// force scale allows twice the previous largest stress term (the floor
+// 1e-9 E0 V0max keeps it finite for a scene without stress). A particle
+// beyond either takes the wide path.
 __device__ __forceinline__ FixScale step_scales(const SceneDev& S) {
   const FixState& f = *S.fix;
   const float mmax = bits_float(f.m_prev);
@@ -275,12 +273,13 @@ __device__ __forceinline__ FixScale step_scales(const SceneDev& S) {
     const float* cv = S.coll[i].vel;
     vcoll = fmaxf(vcoll, sqrtf(cv[0] * cv[0] + cv[1] * cv[1] + cv[2] * cv[2]));
   }
-  const float vb = 1.25f * fmaxf(bits_float(f.v_prev), fix_vstar(f)) + 2.0f * vcoll;
+  const float g = sqrtf(S.grav[0] * S.grav[0] + S.grav[1] * S.grav[1] + S.grav[2] * S.grav[2]);
+  const float vb = 1.25f * bits_float(f.v_prev) + 2.0f * vcoll + 2.0f * g * S.dt;
   const float afloor = 1e-9f * S.young * bits_float(f.v0max);
   FixScale sc;
   sc.m = pow2_scale(mmax * kWmax, 21);
   sc.p = pow2_scale(mmax * vb * kWmax, 21);
-  sc.f = pow2_scale(fmaxf(2.0f * bits_float(f.a_prev), afloor) * kWmax, 20);
+  sc.f = pow2_scale(fmaxf(2.0f * bits_float(f.a_prev), afloor) * kWmax, 21);
   return sc;
 }
 
@@ -293,38 +292,25 @@ __device__ __forceinline__ FixScale measured_scales(const SceneDev& S) {
   FixScale sc;
   sc.m = pow2_scale(mmax * kWmax, 21);
   sc.p = pow2_scale(mmax * bits_float(f.v_prev) * kWmax, 21);
-  sc.f = pow2_scale(fmaxf(bits_float(f.a_prev), afloor) * kWmax, 20);
+  sc.f = pow2_scale(fmaxf(bits_float(f.a_prev), afloor) * kWmax, 21);
   return sc;
 }
 
-// Packed pair of int32 sums in one 64-bit word: hi * 2^32 + lo (mod 2^64).
-// Sums of packed words unpack to the sums of the halves whenever those fit
-// in int32, whatever the intermediate carries.
-__device__ __forceinline__ unsigned long long pack2(int hi, int lo) {
-  return ((unsigned long long)(unsigned)hi << 32) + (unsigned long long)(long long)lo;
-}
-__device__ __forceinline__ void unpack2(unsigned long long w, int& hi, int& lo) {
-  lo = (int)(unsigned)(w & 0xffffffffull);
-  hi = (int)(unsigned)((w - (unsigned long long)(long long)lo) >> 32);
-}
-
-// Adds one node's seven integer sums (m, p, f) into acc.
-__device__ __forceinline__ void acc_add(const SceneDev& S, int blk, int node, long long m, long long px, long long py,
-                                        long long pz, long long fx, long long fy, long long fz, bool mass_only) {
+// Adds one node's integer sums v[0..6] (m, p, f; mass_only: v[0]) into acc
+// (two's complement adds: a sum of int64 values, whatever the order).
+__device__ __forceinline__ void acc_add(const SceneDev& S, int blk, int node, const long long v[7], bool mass_only) {
   unsigned long long* a = S.acc + (size_t)blk * kAccBlockWords + node;
-  atomicAdd(a, ((unsigned long long)px << 32) + (unsigned long long)m);
-  if (mass_only) return;
-  atomicAdd(a + kBlockNodes, ((unsigned long long)pz << 32) + (unsigned long long)py);
-  atomicAdd(a + 2 * kBlockNodes, (unsigned long long)fx);
-  atomicAdd(a + 3 * kBlockNodes, (unsigned long long)fy);
-  atomicAdd(a + 4 * kBlockNodes, (unsigned long long)fz);
+  const int nw = mass_only ? 1 : kAccWords;
+  for (int f = 0; f < nw; f++)
+    if (v[f]) atomicAdd(a + f * kBlockNodes, (unsigned long long)v[f]);
 }
 
 // ---- P2G quantities of one particle -----------------------------------------
 // mass, momentum and A = -V0 * stress, stress = 2 mu(Jp) (FE - R) FE^T +
 // lambda(Jp) (JE - 1) JE I with R the polar rotation of FE
-// (p2gTransfer.glsl:109-141); V0 = m / rho0. `a` bounds the two terms of a
-// force contribution: max over rows r of max(|A_r0|, |A_r1| + |A_r2|).
+// (p2gTransfer.glsl:109-141); V0 = m / rho0. `a` = max over rows r of
+// |A_r0| + |A_r1| + |A_r2| bounds a force contribution and both its terms
+// (in units of the weight products' bound (2/3)^3).
 struct P2GParticle {
   float m, mv[3];
   float A[3][3];  // A[r][c]
@@ -350,7 +336,7 @@ __device__ __forceinline__ void p2g_stress(const SceneDev& S, const M3& F, const
   for (int r = 0; r < 3; r++) {
 #pragma unroll
     for (int c = 0; c < 3; c++) q.A[r][c] = -vol * (2.0f * mu * P.m[c][r] + (r == c ? s2 : 0.0f));
-    a = fmaxf(a, fmaxf(fabsf(q.A[r][0]), fabsf(q.A[r][1]) + fabsf(q.A[r][2])));
+    a = fmaxf(a, fabsf(q.A[r][0]) + fabsf(q.A[r][1]) + fabsf(q.A[r][2]));
   }
   q.a = a;
   q.force = true;
@@ -379,16 +365,18 @@ __device__ __forceinline__ P2GParticle p2g_particle(const SceneDev& S, int p, fl
   return q;
 }
 
-// Whether every term of the particle's contributions fits the fast path's
-// range at scales sc (KIND kP2gMass: the mass alone).
+// The largest magnitude any of the particle's scaled contributions (and
+// contribution terms) can take at scales sc (KIND kP2gMass: the mass alone);
+// not finite for a non-finite particle.
 template <int KIND>
-__device__ __forceinline__ bool fix_fits(const P2GParticle& q, const FixScale& sc) {
-  bool ok = fabsf(q.m) * sc.m * kWmax < kFastLimit1;
+__device__ __forceinline__ float fix_bound(const P2GParticle& q, const FixScale& sc) {
+  float b = fabsf(q.m) * sc.m;
   if (KIND == kP2gFull) {
     const float mv = fmaxf(fabsf(q.mv[0]), fmaxf(fabsf(q.mv[1]), fabsf(q.mv[2])));
-    ok = ok && mv * sc.p * kWmax < kFastLimit1 && (!q.force || q.a * sc.f * kWmax < kFastLimit2);
+    b = fmaxf(b, mv * sc.p);
+    if (q.force) b = fmaxf(b, q.a * sc.f);
   }
-  return ok;  // false for non-finite values as well
+  return b * kWmax;
 }
 
 // The per-lane factors of one particle's contributions in stencil row
@@ -465,7 +453,7 @@ __device__ __forceinline__ void scatter_fix(const SceneDev& S, float ms, const f
         }
         if (!(v[0] | v[1] | v[2] | v[3] | v[4] | v[5] | v[6])) continue;
         const int blk = block_id(S, g0 >> 2, g1 >> 2, g2 >> 2);
-        acc_add(S, blk, (g0 & 3) + 4 * (g1 & 3) + 16 * (g2 & 3), v[0], v[1], v[2], v[3], v[4], v[5], v[6], mo);
+        acc_add(S, blk, (g0 & 3) + 4 * (g1 & 3) + 16 * (g2 & 3), v, mo);
         S.blk_flag[blk] = 1;
       }
     }
@@ -490,7 +478,7 @@ __device__ __forceinline__ void scatter_force(const SceneDev& S, const P2GPartic
         const float gw[3] = {gxa * wyb * wzc, wxa * gyb * wzc, wxa * wyb * gzc};
         const int blk = block_id(S, g0 >> 2, g1 >> 2, g2 >> 2);
         if (__ldg(&S.blk_slot[blk]) < 0) continue;  // only active blocks' words are read and cleared by the solve
-        float* dst = reinterpret_cast<float*>(S.acc + (size_t)blk * kAccBlockWords + 2 * kBlockNodes +
+        float* dst = reinterpret_cast<float*>(S.acc + (size_t)blk * kAccBlockWords + 4 * kBlockNodes +
                                               (g0 & 3) + 4 * (g1 & 3) + 16 * (g2 & 3));
 #pragma unroll
         for (int r = 0; r < 3; r++)
@@ -522,6 +510,8 @@ struct ItemShared {
   unsigned seen[3];                  // largest mass, |v|, force-term bound of coll_scene's particles (bits) ...
   unsigned pushed[3];                // ... and the part of them already recorded in FixState
   int next_same;                     // the CTA's next work item continues this item's home-block run
+  float run_bound;                   // sum of the contribution bounds of the particles in the tile's sums
+  float item_bound;                  // ... and of this item's particles headed for the tile
   int abort;                         // 1 + parity of a copy wait that ran out, else 0
   uint64_t bar;
   snow_collider coll[kShColliders];
@@ -644,6 +634,7 @@ __device__ __forceinline__ void tile_init(ItemShared& sh) {
   if (threadIdx.x == 0) {
     mbar_init(&sh.bar, 1);
     sh.abort = 0;
+    sh.run_bound = sh.item_bound = 0.0f;
   }
   __syncthreads();
 }
@@ -956,8 +947,12 @@ __device__ __forceinline__ int cell_row_node(int ci, int b, int c) {
 // items of one home block can share it. Returns false (at its first barrier,
 // before any write beyond the cell counts and the straight scatters) when a
 // copy wait of the CTA ran out (sh.abort): the caller then stops the CTA.
-// Ends with a barrier.
+// RUN: the tile may already hold earlier items' sums (sh.run_bound bounds
+// them); when this item's particles could take a sum past kTileSumBound, the
+// tile is first added to acc and cleared. Ends with a barrier.
 template <int KIND>
+__device__ __forceinline__ void p2g_tile_flush(ItemShared& sh, const SceneDev& S, int bx, int by, int bz);
+template <int KIND, bool RUN = false>
 __device__ __forceinline__ bool p2g_tile_accumulate(ItemShared& sh, const SceneDev& S, int bx, int by, int bz,
                                                     bool have, const P2GParticle& q, const AxisW& w,
                                                     const int base[3], const FixScale& sc) {
@@ -978,12 +973,14 @@ __device__ __forceinline__ bool p2g_tile_accumulate(ItemShared& sh, const SceneD
     for (int r = 0; r < 3; r++) mvs[r] = q.mv[r] * sc.p;
   }
   if (have) {
-    const bool fast = !fix || fix_fits<KIND>(q, sc);
+    const float bound = fix ? fix_bound<KIND>(q, sc) : 0.0f;
+    const bool fast = !fix || bound < kFastLimit;  // false for a non-finite particle as well
     const int lx = base[0] - 1 - ox, ly = base[1] - 1 - oy, lz = base[2] - 1 - oz;
     const bool inside = lx >= 0 && ly >= 0 && lz >= 0 && lx < kCellsPerAxis && ly < kCellsPerAxis && lz < kCellsPerAxis;
     if (inside && fast) {
       my_cell = lx + kCellsPerAxis * ly + kCellsPerAxis * kCellsPerAxis * lz;
       my_rank = atomicAdd(&sh.ccount[my_cell], 1);
+      if (RUN) atomicAdd(&sh.item_bound, bound);
     } else {
       // the particle drifted out of its home block's tile since the last
       // binning, or outgrew the fast path's range
@@ -998,9 +995,18 @@ __device__ __forceinline__ bool p2g_tile_accumulate(ItemShared& sh, const SceneD
       }
     }
   }
+  if (threadIdx.x == 32) sh.nrows = 0;  // the previous flush is long done
   __syncthreads();  // counts done
   if (sh.abort) return false;  // a copy wait ran out
-  if (threadIdx.x == 32) sh.nrows = 0;  // the previous flush is long done
+  if (RUN && sh.run_bound + sh.item_bound > kTileSumBound) {  // uniform across the CTA
+    // this item's sums could wrap the tile's int32 sums: the earlier items'
+    // go to acc first (integer sums: the split changes no bit of the result)
+    p2g_tile_flush<KIND>(sh, S, bx, by, bz);
+    __syncthreads();
+    if (threadIdx.x == 32) sh.nrows = 0;
+    if (threadIdx.x == 0) sh.run_bound = 0.0f;
+    tile_zero(sh, nf);
+  }
   // exclusive scan of the cell counts and list of the occupied cells, one
   // cell per thread
   const int t = threadIdx.x;
@@ -1029,6 +1035,10 @@ __device__ __forceinline__ bool p2g_tile_accumulate(ItemShared& sh, const SceneD
   }
   if (t == kCells - 1) sh.cstart[kCells] = off + incl;
   if (t == blockDim.x - 1) sh.ncells = ooff + __popc(occ);
+  if (RUN && t == 0) {  // every thread has read both bounds (two barriers ago)
+    sh.run_bound += sh.item_bound;
+    sh.item_bound = 0.0f;
+  }
   __syncthreads();
   if (my_cell >= 0) {
     // the particle's P2G data, stored in tile-cell order
@@ -1124,8 +1134,8 @@ __device__ __forceinline__ bool p2g_tile_accumulate(ItemShared& sh, const SceneD
 }
 
 // Adds the tile's non-zero nodes that lie in the grid to acc and flags
-// their blocks (fixed point: each node's sums as two packed int32 pairs and
-// three int64 words; K u: three float adds into the force words). Every
+// their blocks (fixed point: each node's non-zero sums into its int64
+// words; K u: three float adds into the force words). Every
 // thread of the CTA calls it after p2g_tile_accumulate's closing barrier;
 // the caller separates it from the next use of the tile with a barrier.
 template <int KIND>
@@ -1168,20 +1178,15 @@ __device__ __forceinline__ void p2g_tile_flush(ItemShared& sh, const SceneDev& S
       // read and clear the words of those alone (a block whose fixed-point
       // sums all rounded to zero is not active, although its K u may not be)
       if (__ldg(&S.blk_slot[blk]) < 0) continue;
-      float* fw = reinterpret_cast<float*>(a + 2 * kBlockNodes);
+      float* fw = reinterpret_cast<float*>(a + 4 * kBlockNodes);
 #pragma unroll
       for (int f = 0; f < 3; f++) atomicAdd(fw + 2 * f * kBlockNodes, sh.tile[f * kTile3 + t]);
       continue;
     }
-    if (KIND == kP2gMass) {
-      atomicAdd(a, (unsigned long long)(long long)sh.tilei[t]);
-    } else {
-      const int* ti = sh.tilei + t;
-      atomicAdd(a, pack2(ti[kTile3], ti[0]));
-      atomicAdd(a + kBlockNodes, pack2(ti[3 * kTile3], ti[2 * kTile3]));
 #pragma unroll
-      for (int f = 0; f < 3; f++)
-        atomicAdd(a + (2 + f) * kBlockNodes, (unsigned long long)(long long)ti[(4 + f) * kTile3]);
+    for (int f = 0; f < nf; f++) {
+      const int v = sh.tilei[f * kTile3 + t];
+      if (v) atomicAdd(a + f * kBlockNodes, (unsigned long long)(long long)v);
     }
     S.blk_flag[blk] = 1;
   }

@@ -3,11 +3,11 @@
 // quantisation, on a blocked grid.
 //
 // Grid layout in HBM. The grid is cut into 4x4x4-node blocks.
-//   acc      dense, one 2560-byte record per block: the P2G sums (m, p, f)
-//            as fixed-point integers (five 64-bit words per node, word-major:
-//            packed int32 pairs (m | p_x), (p_y | p_z); int64 f_x, f_y, f_z),
-//            so that they do not depend on the order they are added in. All
-//            zero between steps: the grid update clears what it consumes.
+//   acc      dense, one 3584-byte record per block: the P2G sums (m, p, f)
+//            as fixed-point integers (seven int64 words per node,
+//            word-major), so that they do not depend on the order they are
+//            added in. All zero between steps: the grid update clears what
+//            it consumes.
 //   blk_flag blocks that received P2G sums (set by the P2G tile flush).
 //   compact  turns the flags into the active-block list and gives each
 //            active block a slot in the output pool.
@@ -73,7 +73,6 @@ __global__ void k_begin_step(const SceneDev* __restrict__ scenes, int nscenes, i
     f.a_prev = f.a_cur;
     f.m_cur = f.v_cur = f.a_cur = 0u;
   }
-  if (threadIdx.x < kFixSlots) S.fix->vstar[threadIdx.x] = 0u;
   if (rigid)  // rigidAdvance.glsl:14-18
     for (int i = threadIdx.x; i < S.ncoll; i += blockDim.x)
       for (int k = 0; k < 3; k++) S.coll[i].pos[k] = S.coll[i].pos[k] + S.dt * S.coll[i].vel[k];
@@ -229,16 +228,14 @@ __global__ void __launch_bounds__(256) k_grid(const SceneDev* __restrict__ scene
     // the fixed-point sums back to floats (the scales are powers of two)
     const FixState& fx = *S.fix;
     const float ism = 1.0f / fx.scale[0], isp = 1.0f / fx.scale[1], isf = 1.0f / fx.scale[2];
-    int mq, pxq, pyq, pzq;
-    unpack2(w[0], pxq, mq);
-    unpack2(w[1], pzq, pyq);
+    const long long mq = (long long)w[0];
     const float v[kAccFields] = {(float)mq * ism,
-                                 (float)pxq * isp,
-                                 (float)pyq * isp,
-                                 (float)pzq * isp,
-                                 (float)(long long)w[2] * isf,
-                                 (float)(long long)w[3] * isf,
-                                 (float)(long long)w[4] * isf};
+                                 (float)(long long)w[1] * isp,
+                                 (float)(long long)w[2] * isp,
+                                 (float)(long long)w[3] * isp,
+                                 (float)(long long)w[4] * isf,
+                                 (float)(long long)w[5] * isf,
+                                 (float)(long long)w[6] * isf};
     float2* out = reinterpret_cast<float2*>(S.gout + (size_t)slot * kOutBlockFloats + kOutFields * node);
     const float mi = v[0];
     float vs[3] = {0.0f, 0.0f, 0.0f}, d[3] = {0.0f, 0.0f, 0.0f};
@@ -260,11 +257,6 @@ __global__ void __launch_bounds__(256) k_grid(const SceneDev* __restrict__ scene
     out[0] = make_float2(vs[0], vs[1]);
     out[1] = make_float2(vs[2], d[0]);
     out[2] = make_float2(d[1], d[2]);
-    // the largest |v*| bounds the next P2G's momenta (step_scales); a warp
-    // lies inside one block, so inside one scene
-    const unsigned vb = __reduce_max_sync(0xffffffffu, __float_as_uint(sqrtf(vs[0] * vs[0] + vs[1] * vs[1] + vs[2] * vs[2])));
-    unsigned* slot_max = &S.fix->vstar[blockIdx.x % kFixSlots];
-    if ((threadIdx.x & 31) == 0 && vb > *(volatile unsigned*)slot_max) atomicMax(slot_max, vb);
     if (S.crs) {  // semi-implicit: the solve starts from x = v* and applies K to v* first
       const size_t i = (size_t)slot * kBlockNodes + node;
       S.crv[i] = make_float4(vs[0], vs[1], vs[2], mi > 0.0f ? mi : 0.0f);
@@ -295,8 +287,7 @@ __global__ void __launch_bounds__(256) k_volume(const SceneDev* __restrict__ sd)
           const int g0 = base[0] - 1 + a, g1 = base[1] - 1 + b, g2 = base[2] - 1 + c;
           if (!node_in_grid(S, g0, g1, g2)) continue;
           const int blk = block_id(S, g0 >> 2, g1 >> 2, g2 >> 2);
-          int mq, hi;
-          unpack2(S.acc[(size_t)blk * kAccBlockWords + (g0 & 3) + 4 * (g1 & 3) + 16 * (g2 & 3)], hi, mq);
+          const long long mq = (long long)S.acc[(size_t)blk * kAccBlockWords + (g0 & 3) + 4 * (g1 & 3) + 16 * (g2 & 3)];
           const float mi = (float)mq / S.fix->scale[0];
           rho += mi * (sel4(a, w.wx[0], w.wx[1], w.wx[2], w.wx[3]) * sel4(b, w.wy[0], w.wy[1], w.wy[2], w.wy[3]) *
                        sel4(c, w.wz[0], w.wz[1], w.wz[2], w.wz[3]));
@@ -352,9 +343,10 @@ __global__ void __launch_bounds__(kItemMax) k_g2p_advance(const SceneDev* __rest
 // the rotation R = W V^T of the advance's SVD: F_E' = W S' V^T with S'
 // diagonal up to the Jacobi residual, whose polar rotation is W V^T.
 // A CTA takes a contiguous range of work items. Consecutive items of one
-// home block form a run: they share the staged pool blocks (copied once, by
-// bulk copies issued while the previous run's last item sums its P2G) and
-// the P2G tile (added to acc once, at the run's end). The P2G sums are fixed
+// home block form a run: they share
+// the staged pool blocks (copied once, by bulk copies issued while the
+// previous run's last item sums its P2G) and the P2G tile (added to acc
+// once, at the run's end). The P2G sums are fixed
 // point at the scales step_scales gives; the CTA that takes a scene's first
 // item records them for the next grid update, and every CTA records the
 // magnitudes of its particles for the next step's scales. BINNED: a step that
@@ -408,7 +400,10 @@ __global__ void __launch_bounds__(kItemMax, 2) k_g2p2g(const SceneDev* __restric
         }
       }
     }
-    if (run_start) tile_zero(sh, kAccFields);
+    if (run_start) {
+      tile_zero(sh, kAccFields);
+      if (threadIdx.x == 0) sh.run_bound = 0.0f;
+    }
     const int4 it = sh.item_q[par];
     const int un = u + 1;
     // the next item's descriptor and pool slots: loaded now, used (and put
@@ -474,7 +469,7 @@ __global__ void __launch_bounds__(kItemMax, 2) k_g2p2g(const SceneDev* __restric
         atomicMax(&sh.seen[2], ba);
       }
     }
-    if (!p2g_tile_accumulate<kP2gFull>(sh, S, bx, by, bz, have, q, wn, nbase, sh.fscale)) {
+    if (!p2g_tile_accumulate<kP2gFull, true>(sh, S, bx, by, bz, have, q, wn, nbase, sh.fscale)) {
       stage_abort(sh, S);  // a copy wait ran out: this item's particles keep their state, the CTA stops
       return;
     }
@@ -642,17 +637,11 @@ __global__ void k_download_grid(const SceneDev* __restrict__ sd, float* mass, fl
     const int blk = block_id(S, gi >> 2, gj >> 2, gk >> 2);
     const unsigned long long* acc = S.acc + (size_t)blk * kAccBlockWords + (gi & 3) + 4 * (gj & 3) + 16 * (gk & 3);
     const FixState& fx = *S.fix;
-    int mq, pxq, pyq, pzq;
-    unpack2(acc[0], pxq, mq);
-    unpack2(acc[kBlockNodes], pzq, pyq);
-    if (mass) mass[g] = (float)mq / fx.scale[0];
-    if (mom) {
-      mom[3 * g] = (float)pxq / fx.scale[1];
-      mom[3 * g + 1] = (float)pyq / fx.scale[1];
-      mom[3 * g + 2] = (float)pzq / fx.scale[1];
+    if (mass) mass[g] = (float)(long long)acc[0] / fx.scale[0];
+    for (int k = 0; k < 3; k++) {
+      if (mom) mom[3 * g + k] = (float)(long long)acc[(1 + k) * kBlockNodes] / fx.scale[1];
+      if (force) force[3 * g + k] = (float)(long long)acc[(4 + k) * kBlockNodes] / fx.scale[2];
     }
-    if (force)
-      for (int k = 0; k < 3; k++) force[3 * g + k] = (float)(long long)acc[(2 + k) * kBlockNodes] / fx.scale[2];
   }
 }
 

@@ -359,7 +359,7 @@ __device__ __forceinline__ void for_active_nodes(const SceneDev* __restrict__ sc
 // K u of block `slot` at `node`: floats in the low 4 bytes of acc's force
 // words (cleared, as whole words, when `take`).
 __device__ __forceinline__ void take_ku(const SceneDev& S, int slot, int node, bool take, float ku[3]) {
-  unsigned long long* acc = S.acc + (size_t)S.active[slot] * kAccBlockWords + 2 * kBlockNodes + node;
+  unsigned long long* acc = S.acc + (size_t)S.active[slot] * kAccBlockWords + 4 * kBlockNodes + node;
 #pragma unroll
   for (int k = 0; k < 3; k++) {
     ku[k] = *reinterpret_cast<const float*>(acc + k * kBlockNodes);
@@ -519,7 +519,6 @@ __global__ void __launch_bounds__(256) k_cr_end(const SceneDev* __restrict__ sce
       scenes, active_prefix, nscenes, [](const SceneDev& S) { return S.crs != nullptr; },
       [](const SceneDev& S, int slot, int node, double&, double&) {
         const float4 xm = S.crv[(size_t)slot * kBlockNodes + node];
-        float speed = 0.0f;
         if (xm.w > 0.0f) {
           const int b = S.active[slot];
           const int bx = b % S.bdim[0], by = (b / S.bdim[0]) % S.bdim[1], bz = b / (S.bdim[0] * S.bdim[1]);
@@ -536,13 +535,7 @@ __global__ void __launch_bounds__(256) k_cr_end(const SceneDev* __restrict__ sce
             o[3 + k] += v[k] - vs[k];
             o[k] = v[k];
           }
-          speed = sqrtf(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
         }
-        // the solved velocity is what G2P reads: it bounds the next P2G's
-        // momenta (a warp lies inside one block, so inside one scene)
-        const unsigned vb = __reduce_max_sync(0xffffffffu, __float_as_uint(speed));
-        unsigned* slot_max = &S.fix->vstar[blockIdx.x % kFixSlots];
-        if ((threadIdx.x & 31) == 0 && vb > *(volatile unsigned*)slot_max) atomicMax(slot_max, vb);
       },
       [](const SceneDev& S, double*& d0, double*& d1) {
         d0 = &S.crs->bb;  // nothing is added (both sums are zero)

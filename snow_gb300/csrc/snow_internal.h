@@ -49,17 +49,17 @@ constexpr int kBlockNodes = 64;            // 4 x 4 x 4 nodes per grid block
 constexpr int kAccFields = 7;              // m, p (3), f (3)
 constexpr int kOutFields = 6;              // v* (3), d = v* - alpha p/m (3)
 // acc holds the P2G sums as integers (fixed point at per-scene power-of-two
-// scales): per node five 64-bit words, (m | p_x) and (p_y | p_z) as packed
-// pairs of int32 sums (hi * 2^32 + lo) and f_x, f_y, f_z as int64, stored
-// word-major per block.
-constexpr int kAccWords = 5;
-constexpr int kAccBlockWords = kAccWords * kBlockNodes;    // 320 (2560 bytes)
+// scales): per node seven int64 words (m, p_x, p_y, p_z, f_x, f_y, f_z),
+// stored word-major per block. No node sum can leave the int64 range (each
+// contribution is below 2^21 or, on the wide path, 2^62), however many
+// particles pile into a cell.
+constexpr int kAccWords = kAccFields;
+constexpr int kAccBlockWords = kAccWords * kBlockNodes;    // 448 (3584 bytes)
 constexpr int kOutBlockFloats = kOutFields * kBlockNodes;  // 384
 
 // Fixed-point state of one scene's P2G sums. Magnitudes are the bits of
 // non-negative floats (they order like unsigned ints, so atomicMax records
 // maxima); every value here is an order-independent function of the state.
-constexpr int kFixSlots = 32;
 struct FixState {
   float scale[3];     // s_m, s_p, s_f of the sums now in acc (integer = round(contribution * s))
   uint32_t m_prev;    // largest particle mass, |v| and force-term bound a of the particles the
@@ -68,8 +68,6 @@ struct FixState {
   uint32_t m_cur;     // the same, recorded by the P2G in flight (moved to *_prev at each step's start)
   uint32_t v_cur;
   uint32_t a_cur;
-  uint32_t vstar[kFixSlots];  // largest |v*| of this step's grid update (after the semi-implicit solve,
-                              // if any), spread over slots (CTA index mod kFixSlots) against contention
   uint32_t v0max;     // largest initial particle volume
   uint32_t wide;      // particles scattered with int64 contributions (outgrew the fast range), cumulative
 };
