@@ -961,6 +961,7 @@ __device__ __forceinline__ bool p2g_tile_accumulate(ItemShared& sh, const SceneD
   const int ox = 4 * bx - 2, oy = 4 * by - 2, oz = 4 * bz - 2;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int my_cell = -1, my_rank = 0;
+  float tile_bound = 0.0f;  // the particle's contribution bound, if it goes to the tile
   // the particle's quantities as the tile stores them (fixed point: scaled)
   float ms = 0.0f, mvs[3] = {0.0f, 0.0f, 0.0f}, As[3][3];
 #pragma unroll
@@ -980,7 +981,7 @@ __device__ __forceinline__ bool p2g_tile_accumulate(ItemShared& sh, const SceneD
     if (inside && fast) {
       my_cell = lx + kCellsPerAxis * ly + kCellsPerAxis * kCellsPerAxis * lz;
       my_rank = atomicAdd(&sh.ccount[my_cell], 1);
-      if (RUN) atomicAdd(&sh.item_bound, bound);
+      tile_bound = bound;
     } else {
       // the particle drifted out of its home block's tile since the last
       // binning, or outgrew the fast path's range
@@ -994,6 +995,11 @@ __device__ __forceinline__ bool p2g_tile_accumulate(ItemShared& sh, const SceneD
         scatter_fix<KIND, false>(S, ms, mvs, As, w, base);
       }
     }
+  }
+  if (RUN) {  // per warp: its tile particles times their largest bound (no lower than their sum)
+    const uint32_t in = __ballot_sync(0xffffffffu, my_cell >= 0);
+    const float bmax = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(tile_bound)));
+    if (lane == 0 && in) atomicAdd(&sh.item_bound, (float)__popc(in) * bmax);
   }
   if (threadIdx.x == 32) sh.nrows = 0;  // the previous flush is long done
   __syncthreads();  // counts done
