@@ -498,9 +498,6 @@ struct ItemShared {
   int ccount[kCells];                // particles per tile cell (zero between items)
   int wsum[kItemMax / 32];
   int wocc[kItemMax / 32];
-  short rows[kTile * kTile];         // flush: tile rows holding mass ...
-  uint32_t rowmask[kTile * kTile];   // ... and which of their nodes do
-  int nrows;
   short cells[kCells];               // occupied tile cells
   int ncells;
   int4 item_q[2];                    // this and the next work item of the CTA
@@ -630,7 +627,6 @@ __device__ __forceinline__ void tile_zero(ItemShared& sh, int nf) {
 // __syncthreads.
 __device__ __forceinline__ void tile_init(ItemShared& sh) {
   for (int i = threadIdx.x; i < kCells; i += blockDim.x) sh.ccount[i] = 0;
-  if (threadIdx.x == 32) sh.nrows = 0;
   if (threadIdx.x == 0) {
     mbar_init(&sh.bar, 1);
     sh.abort = 0;
@@ -1001,7 +997,6 @@ __device__ __forceinline__ bool p2g_tile_accumulate(ItemShared& sh, const SceneD
     const float bmax = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(tile_bound)));
     if (lane == 0 && in) atomicAdd(&sh.item_bound, (float)__popc(in) * bmax);
   }
-  if (threadIdx.x == 32) sh.nrows = 0;  // the previous flush is long done
   __syncthreads();  // counts done
   if (sh.abort) return false;  // a copy wait ran out
   if (RUN && sh.run_bound + sh.item_bound > kTileSumBound) {  // uniform across the CTA
@@ -1009,7 +1004,6 @@ __device__ __forceinline__ bool p2g_tile_accumulate(ItemShared& sh, const SceneD
     // go to acc first (integer sums: the split changes no bit of the result)
     p2g_tile_flush<KIND>(sh, S, bx, by, bz);
     __syncthreads();
-    if (threadIdx.x == 32) sh.nrows = 0;
     if (threadIdx.x == 0) sh.run_bound = 0.0f;
     tile_zero(sh, nf);
   }
@@ -1141,44 +1135,29 @@ __device__ __forceinline__ bool p2g_tile_accumulate(ItemShared& sh, const SceneD
 
 // Adds the tile's non-zero nodes that lie in the grid to acc and flags
 // their blocks (fixed point: each node's non-zero sums into its int64
-// words; K u: three float adds into the force words). Every
-// thread of the CTA calls it after p2g_tile_accumulate's closing barrier;
-// the caller separates it from the next use of the tile with a barrier.
+// words; K u: three float adds into the force words of blocks active in
+// this step). One tile node per thread, x fastest, so consecutive threads
+// add to consecutive words. Every thread of the CTA calls it after
+// p2g_tile_accumulate's closing barrier; the caller separates it from the
+// next use of the tile with a barrier.
 template <int KIND>
 __device__ __forceinline__ void p2g_tile_flush(ItemShared& sh, const SceneDev& S, int bx, int by, int bz) {
   constexpr int nf = P2gFields<KIND>::nf;
   const int ox = 4 * bx - 2, oy = 4 * by - 2, oz = 4 * bz - 2;
-  // the tile rows (ty, tz) in the grid, with their non-zero nodes in the grid
-  for (int r = threadIdx.x; r < kTile * kTile; r += blockDim.x) {
-    const int g1 = oy + r % kTile, g2 = oz + r / kTile;
-    uint32_t mask = 0;
-    if (g1 >= 0 && g2 >= 0 && g1 < S.dim[1] && g2 < S.dim[2]) {
+  for (int t = threadIdx.x; t < kTile3; t += blockDim.x) {
+    const int x = t % kTile, y = (t / kTile) % kTile, z = t / (kTile * kTile);
+    const int g0 = ox + x, g1 = oy + y, g2 = oz + z;
+    if (g0 < 0 || g1 < 0 || g2 < 0 || g0 >= S.dim[0] || g1 >= S.dim[1] || g2 >= S.dim[2]) continue;
+    int v[nf];
+    int any = 0;
 #pragma unroll
-      for (int x = 0; x < kTile; x++) {
-        int nz = 0;
-#pragma unroll
-        for (int f = 0; f < nf; f++) nz |= sh.tilei[f * kTile3 + r * kTile + x];  // float zero has zero bits too
-        if (nz && ox + x >= 0 && ox + x < S.dim[0]) mask |= 1u << x;
-      }
+    for (int f = 0; f < nf; f++) {
+      v[f] = sh.tilei[f * kTile3 + t];  // float K u: its bits (zero for 0.0f)
+      any |= v[f];
     }
-    if (mask) {
-      const int k = atomicAdd(&sh.nrows, 1);
-      sh.rows[k] = r;
-      sh.rowmask[k] = mask;
-    }
-  }
-  __syncthreads();
-  // one node per thread: consecutive threads take consecutive x of a row
-  const int nrows = sh.nrows;
-  for (int task = threadIdx.x; task < nrows * kTile; task += blockDim.x) {
-    const int k = task / kTile, x = task % kTile;
-    if (!((sh.rowmask[k] >> x) & 1u)) continue;
-    const int r = sh.rows[k];
-    const int t = r * kTile + x;
-    const int g0 = ox + x, g1 = oy + r % kTile, g2 = oz + r / kTile;
+    if (!any) continue;
     const int blk = block_id(S, g0 >> 2, g1 >> 2, g2 >> 2);
-    const int node = (g0 & 3) + 4 * (g1 & 3) + 16 * (g2 & 3);
-    unsigned long long* a = S.acc + (size_t)blk * kAccBlockWords + node;
+    unsigned long long* a = S.acc + (size_t)blk * kAccBlockWords + (g0 & 3) + 4 * (g1 & 3) + 16 * (g2 & 3);
     if (KIND == kP2gForce) {
       // K u goes only to blocks active in this step: the solve's node passes
       // read and clear the words of those alone (a block whose fixed-point
@@ -1186,14 +1165,12 @@ __device__ __forceinline__ void p2g_tile_flush(ItemShared& sh, const SceneDev& S
       if (__ldg(&S.blk_slot[blk]) < 0) continue;
       float* fw = reinterpret_cast<float*>(a + 4 * kBlockNodes);
 #pragma unroll
-      for (int f = 0; f < 3; f++) atomicAdd(fw + 2 * f * kBlockNodes, sh.tile[f * kTile3 + t]);
+      for (int f = 0; f < 3; f++) atomicAdd(fw + 2 * f * kBlockNodes, __int_as_float(v[f]));
       continue;
     }
 #pragma unroll
-    for (int f = 0; f < nf; f++) {
-      const int v = sh.tilei[f * kTile3 + t];
-      if (v) atomicAdd(a + f * kBlockNodes, (unsigned long long)(long long)v);
-    }
+    for (int f = 0; f < nf; f++)
+      if (v[f]) atomicAdd(a + f * kBlockNodes, (unsigned long long)(long long)v[f]);
     S.blk_flag[blk] = 1;
   }
 }
