@@ -310,7 +310,7 @@ def _events(stream, n):
     return [torch.cuda.Event(enable_timing=True) for _ in range(n)]
 
 
-def bench_batched(args, local_rank, at_scale=False):
+def bench_batched(args, local_rank, at_scale=False, n_scenes=None, steps=None, tuning=None):
     """Many independent scenes of uneven size: the plain per-scene loop (each
     scene's own step, scenes one after another) against the batched step (one
     launch per phase for all scenes, CUDA graph, autotuned work split). Both
@@ -319,20 +319,23 @@ def bench_batched(args, local_rank, at_scale=False):
       default:   64 scenes, 10k-500k particles log-uniform, 64^3-192^3 grids,
                  per-scene E0 and xi (~10M particles, ~1.7 GB of state);
       at_scale:  16 snow blocks of 2M-8M particles dropped onto a sphere
-                 collider, 384^3-512^3 grids (~80M particles)."""
+                 collider, 384^3-512^3 grids (~80M particles).
+    `tuning` (sort interval, particles per item, CTAs per SM) replaces the
+    autotuner, whose ~3,200 steps take minutes on the 80M-particle batch."""
     import torch
 
     from snow_gb300 import api, scenes
 
     torch.cuda.set_device(local_rank)
     t0 = time.time()
-    scs = scenes.cfg4_batch(n_scenes=args.batch_scenes) if at_scale else scenes.cfg3_batch(n_scenes=args.batch_scenes)
+    n_scenes = n_scenes or args.batch_scenes
+    scs = scenes.cfg4_batch(n_scenes=n_scenes) if at_scale else scenes.cfg3_batch(n_scenes=n_scenes)
     gen_s = time.time() - t0
     ntot = sum(s.n for s in scs)
     dts = [s.dt for s in scs]
     ctx = api.Context(local_rank)
     stream = torch.cuda.ExternalStream(ctx.stream)
-    K, W = args.batch_steps, args.warmup
+    K, W = steps or args.batch_steps, args.warmup
 
     def timed(fn):
         ev = _events(stream, 2)
@@ -367,13 +370,17 @@ def bench_batched(args, local_rank, at_scale=False):
 
     # the work split is tuned on scratch copies (autotuning takes real steps),
     # so the timed batch covers the same steps as the per-scene loop
-    scratch = [api.SimScene(ctx, s).upload().init() for s in scs]
-    tb = api.Batch(ctx, scratch)
-    tuning = tb.autotune(dts)
-    tb.close()
-    for sim in scratch:
-        sim.close()
-    del scratch
+    if tuning is None:
+        scratch = [api.SimScene(ctx, s).upload().init() for s in scs]
+        tb = api.Batch(ctx, scratch)
+        tuning = tb.autotune(dts)
+        tb.close()
+        for sim in scratch:
+            sim.close()
+        del scratch
+    else:
+        si, im, cp = tuning
+        tuning = dict(sort_interval=si, items_max=im, ctas_per_sm=cp, ms_per_step=None, steps_taken=0)
     sims = [api.SimScene(ctx, s).upload().init() for s in scs]
     batch = api.Batch(ctx, sims).set_tuning(tuning["sort_interval"], tuning["items_max"], tuning["ctas_per_sm"])
     for _ in range(W):
@@ -725,11 +732,13 @@ def main():
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=16)
     ap.add_argument("--no-batched", action="store_true")
-    ap.add_argument("--serve-seconds", type=float, default=5.0)
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
+    ap.add_argument("--no-batched-at-scale", action="store_true",
+                    help="skip the 16-scene batch of 2M-8M particles (384^3-512^3) in the default run")
     ap.add_argument("--serve-rate", type=float, default=20.0)
     ap.add_argument("--serve-pool", type=int, default=24)
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
-    ap.add_argument("--serve-drain-s", type=float, default=180.0)
+    ap.add_argument("--serve-drain-s", type=float, default=300.0)
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--serve-policy", default="srpt", choices=["fifo", "srpt"])
     ap.add_argument("--serve-cap", type=int, default=4 << 20, help="particles stepped together (0 = all)")
@@ -836,11 +845,15 @@ def main():
         "gpu_launches": res["launches"],
         "step_ms_p50": statistics.median(res["step_ms"]), "step_ms_max": max(res["step_ms"]),
     }
-    if not args.no_batched:
+    side = world == 1  # the side legs run on a single GPU only (a replica run times the headline alone)
+    if side and not args.no_batched:
         line["batched"] = bench_batched(args, local_rank)
-    if not args.no_serving:
+    if side and not args.no_batched_at_scale:
+        line["batched_at_scale"] = bench_batched(args, local_rank, at_scale=True, n_scenes=16, steps=8,
+                                                 tuning=(8, 256, 2))
+    if side and not args.no_serving:
         line["serving"] = bench_serving(args, local_rank)
-    if not args.no_cpu_baseline:
+    if side and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_port(res["scene"], steps=2)
         # the same leg checks the timed workload's next step against the
         # oracle, and one batched step at the size of the 16-scene batch's
