@@ -77,8 +77,13 @@ __global__ void k_begin_step(const SceneDev* __restrict__ scenes, int nscenes, i
     for (int i = threadIdx.x; i < S.ncoll; i += blockDim.x)
       for (int k = 0; k < 3; k++) S.coll[i].pos[k] = S.coll[i].pos[k] + S.dt * S.coll[i].vel[k];
   if (S.crs) {  // the semi-implicit solve's scalars start from zero each step
-    double* c = reinterpret_cast<double*>(S.crs);
-    for (int i = threadIdx.x; i < (int)(sizeof(CrScalars) / sizeof(double)); i += blockDim.x) c[i] = 0.0;
+    int* c = reinterpret_cast<int*>(S.crs);
+    for (int i = threadIdx.x; i < (int)(offsetof(CrScalars, skipping) / sizeof(int)); i += blockDim.x) c[i] = 0;
+    if (threadIdx.x == 0) {  // a step within kCrSkipSteps of a start below kCrSkipFactor * tol skips the solve
+      CrScalars& cs = *S.crs;
+      cs.skipping = cs.skip_left > 0 ? 1 : 0;
+      if (cs.skip_left > 0) cs.skip_left--;
+    }
   }
 }
 
@@ -204,67 +209,131 @@ __global__ void __launch_bounds__(kItemMax, 2) k_p2g(const SceneDev* __restrict_
   }
 }
 
-// gForceCompute.glsl:57-103 on the active blocks: one 64-thread group per
-// block. The P2G sums are consumed (zeroed) here.
-__global__ void __launch_bounds__(256) k_grid(const SceneDev* __restrict__ scenes, const int* __restrict__ active_prefix,
-                                              int nscenes, int clear_only) {
-  const int groups = blockDim.x / kBlockNodes;
-  const int node = threadIdx.x % kBlockNodes;
+// gForceCompute.glsl:57-103 for one node of active block b (pool slot
+// `slot`) from its seven fixed-point sums w.
+__device__ __forceinline__ void grid_node(const SceneDev& S, int slot, int b, int node,
+                                          const unsigned long long (&w)[kAccWords]) {
+  // the fixed-point sums back to floats (the scales are powers of two)
+  const FixState& fx = *S.fix;
+  const float ism = 1.0f / fx.scale[0], isp = 1.0f / fx.scale[1], isf = 1.0f / fx.scale[2];
+  const long long mq = (long long)w[0];
+  const float v[kAccFields] = {(float)mq * ism,
+                               (float)(long long)w[1] * isp,
+                               (float)(long long)w[2] * isp,
+                               (float)(long long)w[3] * isp,
+                               (float)(long long)w[4] * isf,
+                               (float)(long long)w[5] * isf,
+                               (float)(long long)w[6] * isf};
+  float2* out = reinterpret_cast<float2*>(S.gout + (size_t)slot * kOutBlockFloats + kOutFields * node);
+  const float mi = v[0];
+  float vs[3] = {0.0f, 0.0f, 0.0f}, d[3] = {0.0f, 0.0f, 0.0f};
+  if (mq > 0) {
+    const float inv = 1.0f / mi;
+    const float vold[3] = {v[1] * inv, v[2] * inv, v[3] * inv};
+#pragma unroll
+    for (int k = 0; k < 3; k++) vs[k] = vold[k] + S.dt * (v[4 + k] * inv + S.grav[k]);
+    const int bx = b % S.bdim[0], by = (b / S.bdim[0]) % S.bdim[1], bz = b / (S.bdim[0] * S.bdim[1]);
+    const int gi = 4 * bx + (node & 3), gj = 4 * by + ((node >> 2) & 3), gk = 4 * bz + (node >> 4);
+    // node position as Grid::initSSBO forms it: x_off + h * (float)i
+    const float xi[3] = {__fadd_rn(S.gpos[0], __fmul_rn(S.h, (float)gi)),
+                         __fadd_rn(S.gpos[1], __fmul_rn(S.h, (float)gj)),
+                         __fadd_rn(S.gpos[2], __fmul_rn(S.h, (float)gk))};
+    collide(S.coll, S.ncoll, xi, vs);
+#pragma unroll
+    for (int k = 0; k < 3; k++) d[k] = vs[k] - S.alpha * vold[k];
+  }
+  out[0] = make_float2(vs[0], vs[1]);
+  out[1] = make_float2(vs[2], d[0]);
+  out[2] = make_float2(d[1], d[2]);
+  if (S.crs) {  // semi-implicit: the solve starts from x = v* and applies K to v* first
+    const size_t i = (size_t)slot * kBlockNodes + node;
+    S.crv[i] = make_float4(vs[0], vs[1], vs[2], mi > 0.0f ? mi : 0.0f);
+    float* u = S.cru + (size_t)slot * kImpBlockFloats + 3 * node;
+    u[0] = vs[0];
+    u[1] = vs[1];
+    u[2] = vs[2];
+  }
+}
+
+// The grid update on the active blocks, one 64-thread group per block (a
+// warp lies inside one group, so inside one scene). Each group's blocks are
+// staged by TMA: a block's fixed-point record is one contiguous 3,584-byte
+// bulk copy into the group's shared buffer, and the group's next block is
+// copied while it converts, updates and writes the current one. The P2G
+// sums are consumed (zeroed) here. clear_only: the sums are zeroed and
+// nothing is staged or written (scene set-up).
+constexpr int kGridGroups = 4;  // 64-thread groups per CTA
+__global__ void __launch_bounds__(kGridGroups * kBlockNodes) k_grid(const SceneDev* __restrict__ scenes,
+                                                                    const int* __restrict__ active_prefix,
+                                                                    int nscenes, int clear_only) {
+  __shared__ __align__(128) unsigned long long buf[kGridGroups][kAccBlockWords];
+  __shared__ uint64_t bar[kGridGroups];
+  __shared__ int gabort[kGridGroups];
+  const int g = threadIdx.x / kBlockNodes, node = threadIdx.x % kBlockNodes;
   const long long total = active_prefix[nscenes];
-  for (long long u = (long long)blockIdx.x * groups + threadIdx.x / kBlockNodes; u < total;
-       u += (long long)gridDim.x * groups) {
-    const int s = find_scene(active_prefix, nscenes, u);
+  const long long stride = (long long)gridDim.x * kGridGroups;
+  long long u = (long long)blockIdx.x * kGridGroups + g;
+  if (clear_only) {
+    for (; u < total; u += stride) {
+      const int s = find_scene(active_prefix, nscenes, u);
+      const SceneDev& S = scenes[s];
+      unsigned long long* acc = S.acc + (size_t)S.active[(int)(u - active_prefix[s])] * kAccBlockWords + node;
+#pragma unroll
+      for (int k = 0; k < kAccWords; k++) acc[k * kBlockNodes] = 0ull;
+    }
+    return;
+  }
+  constexpr uint32_t kBytes = kAccBlockWords * sizeof(unsigned long long);
+  static_assert(kBytes % 16 == 0, "bulk copies move multiples of 16 bytes");
+  if (node == 0) {
+    mbar_init(&bar[g], 1);
+    gabort[g] = 0;
+  }
+  __syncthreads();
+  // the block of work unit uu: its scene, pool slot and block id
+  auto locate = [&](long long uu, int& s, int& slot, int& b) {
+    s = find_scene(active_prefix, nscenes, uu);
+    slot = (int)(uu - active_prefix[s]);
+    b = scenes[s].active[slot];
+  };
+  auto issue = [&](long long uu) {  // by the group's thread 0
+    int s, slot, b;
+    locate(uu, s, slot, b);
     const SceneDev& S = scenes[s];
-    const int slot = (int)(u - active_prefix[s]);
-    const int b = S.active[slot];
-    unsigned long long* acc = S.acc + (size_t)b * kAccBlockWords + node;
+    mbar_arrive_expect_tx(&bar[g], kBytes + S.tx_unsent);
+    fence_proxy_async_smem();
+    bulk_g2s(buf[g], S.acc + (size_t)b * kAccBlockWords, kBytes, &bar[g]);
+  };
+  if (u < total && node == 0) issue(u);
+  uint32_t phase = 0;
+  for (; u < total; u += stride) {
+    int s, slot, b;
+    locate(u, s, slot, b);
+    const SceneDev& S = scenes[s];
     unsigned long long w[kAccWords];
+    const bool landed = mbar_wait(&bar[g], phase, S.wait_ns);
+    if (landed) {
 #pragma unroll
-    for (int k = 0; k < kAccWords; k++) {
-      w[k] = acc[k * kBlockNodes];
-      acc[k * kBlockNodes] = 0ull;
+      for (int k = 0; k < kAccWords; k++) w[k] = buf[g][k * kBlockNodes + node];
+    } else {
+      gabort[g] = 1 + (int)phase;
     }
-    if (clear_only) continue;
-    // the fixed-point sums back to floats (the scales are powers of two)
-    const FixState& fx = *S.fix;
-    const float ism = 1.0f / fx.scale[0], isp = 1.0f / fx.scale[1], isf = 1.0f / fx.scale[2];
-    const long long mq = (long long)w[0];
-    const float v[kAccFields] = {(float)mq * ism,
-                                 (float)(long long)w[1] * isp,
-                                 (float)(long long)w[2] * isp,
-                                 (float)(long long)w[3] * isp,
-                                 (float)(long long)w[4] * isf,
-                                 (float)(long long)w[5] * isf,
-                                 (float)(long long)w[6] * isf};
-    float2* out = reinterpret_cast<float2*>(S.gout + (size_t)slot * kOutBlockFloats + kOutFields * node);
-    const float mi = v[0];
-    float vs[3] = {0.0f, 0.0f, 0.0f}, d[3] = {0.0f, 0.0f, 0.0f};
-    if (mq > 0) {
-      const float inv = 1.0f / mi;
-      const float vold[3] = {v[1] * inv, v[2] * inv, v[3] * inv};
+    asm volatile("bar.sync %0, %1;" ::"r"(g + 1), "r"(kBlockNodes) : "memory");  // the group has read its buffer
+    if (gabort[g]) {
+      // the copy did not land in time: counted, one more bounded wait for it
+      // (the CTA must not exit while it may still land), and the group stops
+      if (node == 0) {
+        atomicAdd(&S.counters[CNT_TIMEOUT], 1);
+        mbar_wait(&bar[g], (uint32_t)(gabort[g] - 1), S.wait_ns);
+      }
+      return;
+    }
+    phase ^= 1u;
+    if (node == 0 && u + stride < total) issue(u + stride);
+    unsigned long long* acc = S.acc + (size_t)b * kAccBlockWords + node;
 #pragma unroll
-      for (int k = 0; k < 3; k++) vs[k] = vold[k] + S.dt * (v[4 + k] * inv + S.grav[k]);
-      const int bx = b % S.bdim[0], by = (b / S.bdim[0]) % S.bdim[1], bz = b / (S.bdim[0] * S.bdim[1]);
-      const int gi = 4 * bx + (node & 3), gj = 4 * by + ((node >> 2) & 3), gk = 4 * bz + (node >> 4);
-      // node position as Grid::initSSBO forms it: x_off + h * (float)i
-      const float xi[3] = {__fadd_rn(S.gpos[0], __fmul_rn(S.h, (float)gi)),
-                           __fadd_rn(S.gpos[1], __fmul_rn(S.h, (float)gj)),
-                           __fadd_rn(S.gpos[2], __fmul_rn(S.h, (float)gk))};
-      collide(S.coll, S.ncoll, xi, vs);
-#pragma unroll
-      for (int k = 0; k < 3; k++) d[k] = vs[k] - S.alpha * vold[k];
-    }
-    out[0] = make_float2(vs[0], vs[1]);
-    out[1] = make_float2(vs[2], d[0]);
-    out[2] = make_float2(d[1], d[2]);
-    if (S.crs) {  // semi-implicit: the solve starts from x = v* and applies K to v* first
-      const size_t i = (size_t)slot * kBlockNodes + node;
-      S.crv[i] = make_float4(vs[0], vs[1], vs[2], mi > 0.0f ? mi : 0.0f);
-      float* u = S.cru + (size_t)slot * kImpBlockFloats + 3 * node;
-      u[0] = vs[0];
-      u[1] = vs[1];
-      u[2] = vs[2];
-    }
+    for (int k = 0; k < kAccWords; k++) acc[k * kBlockNodes] = 0ull;
+    grid_node(S, slot, b, node, w);
   }
 }
 
@@ -727,7 +796,7 @@ void fast_p2g(const SceneDev* scenes, const SceneDev& sd_host, const int* item_p
 
 void fast_grid(const SceneDev* scenes, const int* active_prefix, int nscenes, int grid_ctas, bool clear_only,
                cudaStream_t st) {
-  k_grid<<<grid_ctas, 256, 0, st>>>(scenes, active_prefix, nscenes, clear_only ? 1 : 0);
+  k_grid<<<grid_ctas, kGridGroups * kBlockNodes, 0, st>>>(scenes, active_prefix, nscenes, clear_only ? 1 : 0);
 }
 
 void fast_volume(const SceneDev* sd_dev, int n, cudaStream_t st) {

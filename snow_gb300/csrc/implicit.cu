@@ -40,12 +40,14 @@ namespace snow {
 namespace {
 
 // Iteration k (k >= 1) of scene S runs while iteration k - 1 left a residual
-// above the tolerance; iteration 0 is the K v* pass of every implicit scene.
+// above the tolerance; iteration 0 is the K v* pass of every implicit scene
+// that does not skip this step's solve (CrScalars::skipping).
 __device__ __forceinline__ bool cr_running(const SceneDev& S, int k) {
   if (!S.crs) return false;
+  const CrScalars& c = *S.crs;
+  if (c.skipping) return false;
   if (k == 0) return true;
   if (k > S.imp_maxit) return false;
-  const CrScalars& c = *S.crs;
   const double tol = (double)S.imp_tol;
   return c.rr[k - 1] > tol * tol * c.bb;
 }
@@ -544,12 +546,21 @@ __global__ void __launch_bounds__(256) k_cr_end(const SceneDev* __restrict__ sce
 }
 
 // Advances the iteration counter (first: to 1) and, inside a graph, sets the
-// WHILE node's condition: whether any scene runs the new iteration.
+// WHILE node's condition: whether any scene runs the new iteration. The
+// first call also starts kCrSkipSteps skipped steps for each scene whose
+// initial residual is below kCrSkipFactor * its tolerance.
 __global__ void k_cr_cond(const SceneDev* __restrict__ scenes, int nscenes, int* iter, int first,
                           cudaGraphConditionalHandle cond, int use_cond) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const int k = first ? 1 : *iter + 1;
   *iter = k;
+  if (first)
+    for (int s = 0; s < nscenes; s++) {
+      const SceneDev& S = scenes[s];
+      if (!S.crs || S.crs->skipping) continue;
+      const double t = kCrSkipFactor * (double)S.imp_tol;
+      if (S.crs->rr[0] <= t * t * S.crs->bb) S.crs->skip_left = kCrSkipSteps;
+    }
   if (use_cond) cudaGraphSetConditional(cond, any_running(scenes, nscenes, k) ? 1u : 0u);
 }
 

@@ -312,6 +312,7 @@ snow_status fast_alloc_grid(snow_scene* s) {
     return st;
   if (is_implicit(s->p) && (st = salloc(s, (size_t)1, &d.crs))) return st;
   snow_ctx* ctx = s->ctx;
+  if (d.crs) CK(cudaMemsetAsync(d.crs, 0, sizeof(CrScalars), ctx->stream));
   CK(cudaMemsetAsync(d.blk_flag, 0, nb * sizeof(int), ctx->stream));
   CK(cudaMemsetAsync(d.blk_slot, 0xff, nb * sizeof(int), ctx->stream));
   CK(cudaMemsetAsync(d.acc, 0, nb * kAccBlockWords * sizeof(unsigned long long), ctx->stream));

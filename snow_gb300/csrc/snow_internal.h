@@ -88,15 +88,23 @@ enum {
 
 // Semi-implicit velocity solve: conjugate residuals on the mass-scaled form
 // of (M + beta dt^2 K) v = M v* over the active nodes, one record per scene,
-// cleared at the start of each step. Iteration k (1-based) forms
-// rAr[k] = (r_{k-1}, A r_{k-1}), ApAp[k] = |A p_{k-1}|^2 and rr[k] = |r_k|^2.
+// cleared (up to `skipping`) at the start of each step. Iteration k
+// (1-based) forms rAr[k] = (r_{k-1}, A r_{k-1}), ApAp[k] = |A p_{k-1}|^2 and
+// rr[k] = |r_k|^2. A step whose initial residual is below
+// kCrSkipFactor * tolerance makes the next kCrSkipSteps steps skip the
+// solve: they take v = v*, which is what a solve that exits at iteration 0
+// gives, without evaluating K v*; the step after them checks again.
 constexpr int kCrMaxIters = 128;
+constexpr int kCrSkipSteps = 15;
+constexpr double kCrSkipFactor = 1e-3;
 struct CrScalars {
   double bb;                   // |M^1/2 v*|^2
   double rr[kCrMaxIters + 1];  // rr[0]: the initial residual
   double rAr[kCrMaxIters + 1];
   double ApAp[kCrMaxIters + 1];
   int iters;                   // iterations taken
+  int skipping;                // 1: this step skips the solve
+  int skip_left;               // steps still to skip (kept across steps)
   int pad;
 };
 constexpr int kImpBlockFloats = 3 * kBlockNodes;  // 192: one 3-vector per node
