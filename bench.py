@@ -198,7 +198,8 @@ def bench_ours(args, local_rank, barrier=lambda: None):
     # particles leave their tiles), so the window carries at least its share
     # of the binning cost
     sim.set_tuning(tuning["sort_interval"], tuning["items_max"], tuning["ctas_per_sm"])
-    binnings0 = sim.phase_times()["binnings"]
+    pt0 = sim.phase_times()
+    binnings0, wide0 = pt0["binnings"], pt0["wide"]
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     with ClockSampler(local_rank) as clocks:
@@ -215,7 +216,8 @@ def bench_ours(args, local_rank, barrier=lambda: None):
         barrier()
     step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
     total_ms = sum(step_ms)
-    binnings = sim.phase_times()["binnings"] - binnings0
+    pt1 = sim.phase_times()
+    binnings, wide = pt1["binnings"] - binnings0, pt1["wide"] - wide0
     st = sim.stats()
     if st["nonfinite"]:
         raise RuntimeError("non-finite particle state in the timed run")
@@ -302,7 +304,8 @@ def bench_ours(args, local_rank, barrier=lambda: None):
     res = dict(total_ms=total_ms, step_ms=step_ms, n=n, A=A, per=per, dominant=dominant, alg_bytes=alg_bytes,
                achieved=achieved, peak=peak, peak_kind=peak_kind, clocks=clocks.summary(), e2e_s=e2e_s,
                e2e_steps=e2e_steps, e2e_split=split, h2d=h2d, d2h=d2h_stats + d2h_final / e2e_steps, launches=launches,
-               gen_s=gen_s, stats=st, scene=s, tuning=tuning, check_states=check_states, binnings=binnings)
+               gen_s=gen_s, stats=st, scene=s, tuning=tuning, check_states=check_states, binnings=binnings,
+               wide=wide)
     ctx.close()
     return res
 
@@ -845,6 +848,9 @@ def main():
                         "statistics, one step behind) + download into pinned host memory, through the C ABI",
                 "split_ms": res["e2e_split"]},
         "gpu_launches": res["launches"],
+        "wide_particles": {"value": res["wide"], "steps": args.steps,
+                           "note": "particles whose P2G contributions outgrew the fixed-point scales' fast range "
+                                   "in the timed steps (scattered with int64 contributions)"},
         "step_ms_p50": statistics.median(res["step_ms"]), "step_ms_max": max(res["step_ms"]),
     }
     side = world == 1  # the side legs run on a single GPU only (a replica run times the headline alone)

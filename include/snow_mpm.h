@@ -128,11 +128,15 @@ typedef struct snow_stats {
 
 /* Device-timed phases of snow_scene_step when profiling is on (ms, summed
  * over steps since the last reset). `binnings` counts the steps that
- * re-binned the particles (profiling on or off). */
+ * re-binned the particles (profiling on or off); `wide` the particles whose
+ * P2G contributions outgrew the fixed-point scales' fast range and were
+ * scattered with int64 contributions (FAST; reading it waits for the
+ * stream). */
 typedef struct snow_phase_times {
   double sort_ms, p2g_ms, grid_ms, g2p_ms, other_ms, total_ms;
   uint64_t steps;
   uint64_t binnings;
+  uint64_t wide;
 } snow_phase_times;
 
 typedef struct snow_ctx snow_ctx;

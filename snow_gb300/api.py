@@ -242,7 +242,8 @@ class SimScene:
         t = N.SnowPhaseTimes()
         self.ctx.check(self.L.snow_scene_phase_times(self.h, C.byref(t), int(bool(reset))))
         return dict(sort_ms=t.sort_ms, p2g_ms=t.p2g_ms, grid_ms=t.grid_ms, g2p_ms=t.g2p_ms,
-                    solve_ms=t.other_ms, total_ms=t.total_ms, steps=int(t.steps), binnings=int(t.binnings))
+                    solve_ms=t.other_ms, total_ms=t.total_ms, steps=int(t.steps), binnings=int(t.binnings),
+                    wide=int(t.wide))
 
     def check(self):
         """Waits for the queued work; raises SnowError for a condition the

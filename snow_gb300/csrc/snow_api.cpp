@@ -102,6 +102,7 @@ struct snow_scene {
   cudaGraphExec_t g_plain = nullptr, g_sort = nullptr;
   float g_dt = NAN;
   snow_phase_times times{};
+  uint32_t wide_base = 0;  // FixState::wide at the last phase-times reset
   float last_dt = 1e-3f;
   // bounded copy waits of the FAST kernels (snow_scene_set_wait_limit)
   uint32_t wait_ns = kDefaultWaitNs;
@@ -1337,6 +1338,14 @@ snow_status snow_scene_cell_keys(snow_scene* s, uint32_t* keys, uint32_t* perm) 
 snow_status snow_scene_phase_times(snow_scene* s, snow_phase_times* out, int reset) {
   if (!s || !out) return SNOW_EINVAL;
   *out = s->times;
+  if (s->mode == SNOW_MODE_FAST && s->sd.fix) {  // the device's cumulative count, relative to the last reset
+    snow_ctx* ctx = s->ctx;
+    uint32_t wide = 0;
+    CK(cudaMemcpyAsync(&wide, &s->sd.fix->wide, sizeof wide, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    out->wide = (uint32_t)(wide - s->wide_base);
+    if (reset) s->wide_base = wide;
+  }
   if (reset) s->times = snow_phase_times{};
   return SNOW_OK;
 }

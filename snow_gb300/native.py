@@ -58,7 +58,7 @@ class SnowStats(C.Structure):
 class SnowPhaseTimes(C.Structure):
     _fields_ = [("sort_ms", C.c_double), ("p2g_ms", C.c_double), ("grid_ms", C.c_double), ("g2p_ms", C.c_double),
                 ("other_ms", C.c_double), ("total_ms", C.c_double), ("steps", C.c_uint64),
-                ("binnings", C.c_uint64)]
+                ("binnings", C.c_uint64), ("wide", C.c_uint64)]
 
 
 class SnowSolverReport(C.Structure):
