@@ -546,7 +546,11 @@ def _check_report(scene, y0, y1, tol, start):
     return {"oracle": "EXACT64 (FP64, OpenMP)", "particles": len(y0["x"]), "steps": 1, "tolerance": tol,
             "start": start, "max": e["max"], "p99": e["p99"], "median": e["median"],
             "within_tolerance": bool(bound <= tol), "strict_v_within_tolerance": bool(e["max"]["v"] <= tol),
-            "particles_above_strict_v": stopped, "v_worst": e["v_worst"], "oracle_s": oracle_s,
+            "particles_above_strict_v": stopped, "v_worst": e["v_worst"], "v_flip_worst": e["v_flip_worst"],
+            "particles_above_v_flip": int(np.count_nonzero(
+                np.linalg.norm(np.asarray(y1["v"], np.float64) - ref["v"], axis=1) >
+                tol * np.maximum(np.maximum(np.linalg.norm(ref["v"], axis=1), 1e-3), flip))),
+            "oracle_s": oracle_s,
             "threads": threads}
 
 

@@ -393,7 +393,8 @@ def parity_errors(got, ref, flip_scale=None):
     any single-precision evaluation of the update resolves v' only to a few
     ulps of S_p there, so for such particles the strict floor cannot be met
     and v_flip is the bound that FP32 arithmetic allows.
-    Returns the max, p99 and median of each and the worst particle's data."""
+    Returns the max, p99 and median of each and the data of the particles
+    with the largest v and v_flip errors."""
     x, v = np.asarray(got["x"], np.float64), np.asarray(got["v"], np.float64)
     speed = np.linalg.norm(ref["v"], axis=1)
     dv = np.linalg.norm(v - ref["v"], axis=1)
@@ -411,4 +412,8 @@ def parity_errors(got, ref, flip_scale=None):
     w = int(np.argmax(err["v"]))
     out["v_worst"] = {"ref": ref["v"][w].tolist(), "got": v[w].tolist(), "x": ref["x"][w].tolist(),
                       "flip_scale": None if flip_scale is None else float(flip_scale[w])}
+    if flip_scale is not None:
+        w = int(np.argmax(err["v_flip"]))
+        out["v_flip_worst"] = {"ref": ref["v"][w].tolist(), "got": v[w].tolist(), "x": ref["x"][w].tolist(),
+                               "flip_scale": float(flip_scale[w])}
     return out

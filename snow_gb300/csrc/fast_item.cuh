@@ -227,12 +227,14 @@ __device__ __forceinline__ void collide_packed(const snow_collider* coll, const 
 // are spaced by 1, so its bits minus kMagicBits are round(w x). A force
 // contribution g_x kk + w_x hh is rounded as round(g_x kk + round(w_x hh));
 // with a = max over rows r of |A_r0| + |A_r1| + |A_r2|, both terms and their
-// sum are at most a (2/3)^3 s_f. The scales put the largest expected
-// contribution of each kind near 2^21, half the fast range's limit of 2^22;
-// a particle whose contributions reach the limit (it outgrew the magnitudes
-// the scale was chosen from) is scattered with int64 contributions rounded
-// in double precision ("wide"), which depends only on the particle itself,
-// so it is as deterministic.
+// sum are at most a (2/3)^3 s_f. The mass scale puts the largest
+// contribution near 2^21; the momentum and force scales put bounds that
+// already carry a growth margin (1.25 max|v| + margins, twice the largest
+// stress term) into [2^21, 2^22), the fast range's limit. A particle whose
+// contributions reach the limit (it outgrew the magnitudes the scales were
+// chosen from) is scattered with int64 contributions rounded in double
+// precision ("wide"), which depends only on the particle itself, so it is
+// as deterministic.
 constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
 constexpr int kMagicBits = 0x4B400000;
 constexpr float kWmax = 0.2962963f;       // (2/3)^3 >= any weight or weight-gradient product
@@ -278,8 +280,8 @@ __device__ __forceinline__ FixScale step_scales(const SceneDev& S) {
   const float afloor = 1e-9f * S.young * bits_float(f.v0max);
   FixScale sc;
   sc.m = pow2_scale(mmax * kWmax, 21);
-  sc.p = pow2_scale(mmax * vb * kWmax, 21);
-  sc.f = pow2_scale(fmaxf(2.0f * bits_float(f.a_prev), afloor) * kWmax, 21);
+  sc.p = pow2_scale(mmax * vb * kWmax, 22);
+  sc.f = pow2_scale(fmaxf(2.0f * bits_float(f.a_prev), afloor) * kWmax, 22);
   return sc;
 }
 
@@ -291,8 +293,8 @@ __device__ __forceinline__ FixScale measured_scales(const SceneDev& S) {
   const float afloor = 1e-9f * S.young * bits_float(f.v0max);
   FixScale sc;
   sc.m = pow2_scale(mmax * kWmax, 21);
-  sc.p = pow2_scale(mmax * bits_float(f.v_prev) * kWmax, 21);
-  sc.f = pow2_scale(fmaxf(bits_float(f.a_prev), afloor) * kWmax, 21);
+  sc.p = pow2_scale(mmax * bits_float(f.v_prev) * kWmax, 22);
+  sc.f = pow2_scale(fmaxf(bits_float(f.a_prev), afloor) * kWmax, 22);
   return sc;
 }
 

@@ -245,7 +245,7 @@ __device__ __forceinline__ void grid_node(const SceneDev& S, int slot, int b, in
   out[0] = make_float2(vs[0], vs[1]);
   out[1] = make_float2(vs[2], d[0]);
   out[2] = make_float2(d[1], d[2]);
-  if (S.crs) {  // semi-implicit: the solve starts from x = v* and applies K to v* first
+  if (S.crs && !S.crs->skipping) {  // semi-implicit: the solve starts from x = v* and applies K to v* first
     const size_t i = (size_t)slot * kBlockNodes + node;
     S.crv[i] = make_float4(vs[0], vs[1], vs[2], mi > 0.0f ? mi : 0.0f);
     float* u = S.cru + (size_t)slot * kImpBlockFloats + 3 * node;

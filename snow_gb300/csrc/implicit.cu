@@ -514,11 +514,12 @@ __global__ void __launch_bounds__(256) k_cr_update(const SceneDev* __restrict__ 
 }
 
 // The colliders on the solved v (gForceCompute.glsl:72-93 at the node), then
-// gout's (v*, d) becomes (v, d + v - v*) so that d = v - alpha p/m.
+// gout's (v*, d) becomes (v, d + v - v*) so that d = v - alpha p/m. A scene
+// that skips this step's solve keeps v = v*, already in gout.
 __global__ void __launch_bounds__(256) k_cr_end(const SceneDev* __restrict__ scenes,
                                                 const int* __restrict__ active_prefix, int nscenes) {
   for_active_nodes(
-      scenes, active_prefix, nscenes, [](const SceneDev& S) { return S.crs != nullptr; },
+      scenes, active_prefix, nscenes, [](const SceneDev& S) { return S.crs != nullptr && !S.crs->skipping; },
       [](const SceneDev& S, int slot, int node, double&, double&) {
         const float4 xm = S.crv[(size_t)slot * kBlockNodes + node];
         if (xm.w > 0.0f) {
@@ -579,9 +580,18 @@ int hess_smem() {
 
 void fast_implicit_setup() { hess_smem(); }
 
-void fast_implicit_solve(const SceneDev* scenes, const int* item_prefix, const int* active_prefix, int nscenes,
-                         int max_iters, int item_ctas, int grid_ctas, int* d_iter, cudaStream_t body,
-                         cudaStream_t st) {
+namespace {
+// The gate of a captured solve: taken when any scene solves in this step
+// (a scene within its skipped steps leaves v = v* in place).
+__global__ void k_cr_gate(const SceneDev* __restrict__ scenes, int nscenes, cudaGraphConditionalHandle gate) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  bool any = false;
+  for (int s = 0; s < nscenes && !any; s++) any = scenes[s].crs && !scenes[s].crs->skipping;
+  cudaGraphSetConditional(gate, any ? 1u : 0u);
+}
+
+void solve_body(const SceneDev* scenes, const int* item_prefix, const int* active_prefix, int nscenes,
+                int max_iters, int item_ctas, int grid_ctas, int* d_iter, cudaStream_t body, cudaStream_t st) {
   const int smem = hess_smem();
   auto iteration = [&](cudaStream_t s) {
     k_hess<<<item_ctas, kItemMax, smem, s>>>(scenes, item_prefix, nscenes, d_iter);
@@ -609,6 +619,22 @@ void fast_implicit_solve(const SceneDev* scenes, const int* item_prefix, const i
     }
   }
   k_cr_end<<<grid_ctas, 256, 0, st>>>(scenes, active_prefix, nscenes);
+}
+}  // namespace
+
+void fast_implicit_solve(const SceneDev* scenes, const int* item_prefix, const int* active_prefix, int nscenes,
+                         int max_iters, int item_ctas, int grid_ctas, int* d_iter, cudaStream_t body,
+                         cudaStream_t gate, cudaStream_t st) {
+  cudaGraphConditionalHandle taken;
+  if (capture_handle(st, &taken)) {
+    k_cr_gate<<<1, 32, 0, st>>>(scenes, nscenes, taken);
+    // a failure invalidates the capture, which then fails at its end
+    capture_conditional(st, taken, cudaGraphCondTypeIf, gate, [&](cudaStream_t g) {
+      solve_body(scenes, item_prefix, active_prefix, nscenes, max_iters, item_ctas, grid_ctas, d_iter, body, g);
+    });
+    return;
+  }
+  solve_body(scenes, item_prefix, active_prefix, nscenes, max_iters, item_ctas, grid_ctas, d_iter, body, st);
 }
 
 }  // namespace snow

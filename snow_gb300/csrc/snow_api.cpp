@@ -52,6 +52,7 @@ struct snow_ctx {
   // body is captured from (all solves of a context run on `stream`, in order)
   int* d_iter = nullptr;
   cudaStream_t body_stream = nullptr;
+  cudaStream_t gate_stream = nullptr;  // ... and the one the solve itself is captured from (inside its gate)
   // live children, destroyed with the context if the caller did not
   std::set<snow_scene*> scenes;
   std::set<snow_batch*> batches;
@@ -387,7 +388,7 @@ void fast_enqueue_grid(snow_scene* s, bool clear_only, cudaStream_t st) {
 void fast_enqueue_solve(snow_scene* s, cudaStream_t st) {
   if (s->sd.crs)
     fast_implicit_solve(s->sd_dev, s->d_prefix + 0, s->d_prefix + 2, 1, s->sd.imp_maxit, item_ctas(s->tune),
-                        grid_ctas(), s->ctx->d_iter, s->ctx->body_stream, st);
+                        grid_ctas(), s->ctx->d_iter, s->ctx->body_stream, s->ctx->gate_stream, st);
 }
 // One step of a scene whose P2G sums of the current state are pending in
 // acc: rigid advance, [binning], grid update, G2P + advance + next P2G.
@@ -647,6 +648,7 @@ snow_status snow_ctx_create(int device, size_t hbm_budget_bytes, snow_ctx** out)
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc(&ctx->d_iter, sizeof(int));
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->body_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->gate_stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     cudaGetLastError();
     snow_ctx_destroy(ctx);
@@ -672,6 +674,7 @@ void snow_ctx_destroy(snow_ctx* ctx) {
   }
   if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
   if (ctx->body_stream) cudaStreamDestroy(ctx->body_stream);
+  if (ctx->gate_stream) cudaStreamDestroy(ctx->gate_stream);
   if (ctx->d_iter) cudaFree(ctx->d_iter);
   for (int i = 0; i < SNOW_STATS_SLOTS; i++)
     if (ctx->stat_ev[i]) cudaEventDestroy(ctx->stat_ev[i]);
@@ -1503,7 +1506,7 @@ void batch_enqueue_step(snow_batch* b, int phase, int interval, cudaStream_t st)
     if (s->sd.crs) iters = std::max(iters, s->sd.imp_maxit);
   if (iters > 0)
     fast_implicit_solve(b->d_scenes, items, active, n, iters, item_ctas(b->scenes[0]->tune), grid_ctas(),
-                        b->ctx->d_iter, b->ctx->body_stream, st);
+                        b->ctx->d_iter, b->ctx->body_stream, b->ctx->gate_stream, st);
   fast_g2p2g(b->d_scenes, items, n, item_ctas(b->scenes[0]->tune), !bins.empty(), st);
 }
 

@@ -213,12 +213,14 @@ void fast_g2p2g(const SceneDev* scenes, const int* item_prefix, int nscenes, int
 // nodes) until every scene has converged or reached its cap, then the
 // colliders on v and v, d written back into gout. Scenes without a solver
 // record are left alone. d_iter is a device int (the iteration counter).
-// When `st` is capturing a graph the iterations become a conditional WHILE
-// node whose body is captured on `body` (a stream not otherwise in use);
-// otherwise max_iters iterations are launched.
+// When `st` is capturing a graph the whole solve is the body of a
+// conditional IF node (captured on `gate`), taken when any scene solves in
+// this step, and its iterations a conditional WHILE node inside it (body
+// captured on `body`; both streams not otherwise in use); otherwise
+// max_iters iterations are launched.
 void fast_implicit_solve(const SceneDev* scenes, const int* item_prefix, const int* active_prefix, int nscenes,
                          int max_iters, int item_ctas, int grid_ctas, int* d_iter, cudaStream_t body,
-                         cudaStream_t st);
+                         cudaStream_t gate, cudaStream_t st);
 // Kernel attributes of the solve (outside any stream capture).
 void fast_implicit_setup();
 
