@@ -254,9 +254,10 @@ snow_status snow_scene_phase_times(snow_scene* s, snow_phase_times* out, int res
  * relative residuals |r|/|M^1/2 v*| of the mass-scaled system before and
  * after (waits for the stream; SNOW_EUNSUPPORTED for an explicit scene).
  * A step whose solve starts below 1e-3 of its tolerance (it exits at once:
- * v = v*) makes the next 15 steps take v = v* without evaluating the
- * stiffness; those steps report 0 iterations and residuals 0, and the step
- * after them checks again. */
+ * v = v*) makes the next steps take v = v* without evaluating the
+ * stiffness: 15 steps, doubled for each further factor of 10 below, up to
+ * 240. Those steps report 0 iterations and residuals 0, and the step after
+ * them checks again. */
 typedef struct snow_solver_report {
   int iterations;
   int max_iters;

@@ -548,8 +548,8 @@ __global__ void __launch_bounds__(256) k_cr_end(const SceneDev* __restrict__ sce
 
 // Advances the iteration counter (first: to 1) and, inside a graph, sets the
 // WHILE node's condition: whether any scene runs the new iteration. The
-// first call also starts kCrSkipSteps skipped steps for each scene whose
-// initial residual is below kCrSkipFactor * its tolerance.
+// first call also starts skipped steps for each scene whose initial
+// residual is below kCrSkipFactor * its tolerance (CrScalars).
 __global__ void k_cr_cond(const SceneDev* __restrict__ scenes, int nscenes, int* iter, int first,
                           cudaGraphConditionalHandle cond, int use_cond) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -559,8 +559,16 @@ __global__ void k_cr_cond(const SceneDev* __restrict__ scenes, int nscenes, int*
     for (int s = 0; s < nscenes; s++) {
       const SceneDev& S = scenes[s];
       if (!S.crs || S.crs->skipping) continue;
-      const double t = kCrSkipFactor * (double)S.imp_tol;
-      if (S.crs->rr[0] <= t * t * S.crs->bb) S.crs->skip_left = kCrSkipSteps;
+      double t = kCrSkipFactor * (double)S.imp_tol;
+      if (S.crs->rr[0] <= t * t * S.crs->bb) {
+        int skip = kCrSkipSteps;
+        for (int d = 0; d < kCrSkipDoublings; d++) {
+          t *= 0.1;
+          if (S.crs->rr[0] > t * t * S.crs->bb) break;
+          skip *= 2;
+        }
+        S.crs->skip_left = skip;
+      }
     }
   if (use_cond) cudaGraphSetConditional(cond, any_running(scenes, nscenes, k) ? 1u : 0u);
 }

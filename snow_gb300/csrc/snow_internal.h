@@ -91,11 +91,14 @@ enum {
 // cleared (up to `skipping`) at the start of each step. Iteration k
 // (1-based) forms rAr[k] = (r_{k-1}, A r_{k-1}), ApAp[k] = |A p_{k-1}|^2 and
 // rr[k] = |r_k|^2. A step whose initial residual is below
-// kCrSkipFactor * tolerance makes the next kCrSkipSteps steps skip the
-// solve: they take v = v*, which is what a solve that exits at iteration 0
-// gives, without evaluating K v*; the step after them checks again.
+// kCrSkipFactor * tolerance makes the next steps skip the solve: they take
+// v = v*, which is what a solve that exits at iteration 0 gives, without
+// evaluating K v*; the step after them checks again. The skip lasts
+// kCrSkipSteps steps, doubled for each further factor of 10 the residual
+// lies below the threshold, up to kCrSkipSteps * 2^kCrSkipDoublings.
 constexpr int kCrMaxIters = 128;
 constexpr int kCrSkipSteps = 15;
+constexpr int kCrSkipDoublings = 4;
 constexpr double kCrSkipFactor = 1e-3;
 struct CrScalars {
   double bb;                   // |M^1/2 v*|^2
