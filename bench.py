@@ -566,19 +566,21 @@ def oracle_check(scene, states, tol=1e-5):
                          "the workload's state after the timed steps (GPU state, warm SVD frames)")
 
 
-def oracle_check_batched_at_scale(local_rank, n=2_097_152, edge=384, warm=3, tol=1e-5):
+def oracle_check_batched_at_scale(local_rank, n=2_097_152, edge=384, warm=3, tol=1e-5, gap=-0.01):
     """The batched path at the size of the 16-scene batch's scenes: a snow
-    block of n particles on a 384^3 grid, its bottom layer resting in a
-    static sphere collider and moving down at 2 m/s, stepped by
-    snow_batch_step together with a small scene, `warm` batched steps and
-    then one more, which the FP64 oracle repeats from the GPU's state."""
+    block of n particles on a 384^3 grid moving down at 2 m/s onto a static
+    sphere collider, stepped by snow_batch_step together with a small scene,
+    `warm` batched steps and then one more, which the FP64 oracle repeats
+    from the GPU's state. gap < 0 sinks the sphere's top that far into the
+    block (its bottom layer starts inside the collider, where the grid stops
+    it); gap = 0 starts the block touching the sphere."""
     import torch
 
     from snow_gb300 import api, scenes
 
     torch.cuda.set_device(local_rank)
     t0 = time.perf_counter()
-    big = scenes.snow_block_on_sphere(0x5EED0014, n, edge, gap=-0.01, v0=(0.0, -2.0, 0.0))
+    big = scenes.snow_block_on_sphere(0x5EED0014, n, edge, gap=gap, v0=(0.0, -2.0, 0.0))
     small = scenes.small_scene(n=20000, grid_edge=64, seed=0x5EED0015, v0=(1.0, -2.0, 0.5))
     gen_s = time.perf_counter() - t0
     ctx = api.Context(local_rank)
@@ -594,9 +596,11 @@ def oracle_check_batched_at_scale(local_rank, n=2_097_152, edge=384, warm=3, tol
         g.close()
     ctx.close()
     r = _check_report(big, y0, y1, tol, f"after {warm} batched steps (GPU state, warm SVD frames)")
-    r.update(workload=f"snow block of {big.n} particles on a {edge}^3 grid, bottom layer inside a static sphere "
-                      f"collider (radius {big.colliders[-1].radius:.4f}), moving at 2 m/s, stepped by "
-                      f"snow_batch_step beside a 20,000-particle scene", scene_generation_s=gen_s)
+    where = (f"bottom layer inside a static sphere collider (its top {-gap:g} m into the block)" if gap < 0 else
+             "touching a static sphere collider")
+    r.update(workload=f"snow block of {big.n} particles on a {edge}^3 grid, {where} (radius "
+                      f"{big.colliders[-1].radius:.4f}), moving at 2 m/s, stepped by snow_batch_step beside a "
+                      f"20,000-particle scene", scene_generation_s=gen_s)
     return r
 
 
@@ -874,6 +878,7 @@ def main():
             line["oracle_check"] = oracle_check(res["scene"], res["check_states"])
         if not args.no_scale_check:
             line["oracle_check_batched_at_scale"] = oracle_check_batched_at_scale(local_rank)
+            line["oracle_check_batched_at_scale_contact"] = oracle_check_batched_at_scale(local_rank, gap=0.0)
     print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
