@@ -121,9 +121,9 @@ __device__ __forceinline__ void load_fe(const SceneDev& S, int p, M3& F, float& 
   jp = c.y;
 }
 __device__ __forceinline__ void store_fe(const SceneDev& S, int p, const M3& F, float jp) {
-  S.fa[p] = make_float4(F.m[0][0], F.m[0][1], F.m[0][2], F.m[1][0]);
-  S.fb[p] = make_float4(F.m[1][1], F.m[1][2], F.m[2][0], F.m[2][1]);
-  S.fc[p] = make_float2(F.m[2][2], jp);
+  __stcs(&S.fa[p], make_float4(F.m[0][0], F.m[0][1], F.m[0][2], F.m[1][0]));
+  __stcs(&S.fb[p], make_float4(F.m[1][1], F.m[1][2], F.m[2][0], F.m[2][1]));
+  __stcs(&S.fc[p], make_float2(F.m[2][2], jp));
 }
 
 __device__ __forceinline__ int block_id(const SceneDev& S, int bx, int by, int bz) {
@@ -509,6 +509,8 @@ struct ItemShared {
   unsigned seen[3];                  // largest mass, |v|, force-term bound of coll_scene's particles (bits) ...
   unsigned pushed[3];                // ... and the part of them already recorded in FixState
   int next_same;                     // the CTA's next work item continues this item's home-block run
+  int next_issue;                    // ... or starts a run whose pool blocks the last warp copies
+  int next_slot[32];                 // the pool slots of those blocks (lane k: tile block k)
   float run_bound;                   // sum of the contribution bounds of the particles in the tile's sums
   float item_bound;                  // ... and of this item's particles headed for the tile
   int abort;                         // 1 + parity of a copy wait that ran out, else 0
@@ -727,8 +729,8 @@ struct PState {
 
 __device__ __forceinline__ PState load_state(const SceneDev& S, int p, bool binned) {
   PState t;
-  t.xm = (binned ? S.bxm : S.xm)[p];
-  t.vv = (binned ? S.bvv : S.vv)[p];
+  t.xm = __ldcs((binned ? S.bxm : S.xm) + p);
+  t.vv = __ldcs((binned ? S.bvv : S.vv) + p);
   return t;
 }
 
@@ -748,10 +750,10 @@ struct PDef {
 
 __device__ __forceinline__ PDef load_def(const SceneDev& S, int p, bool binned) {
   PDef d;
-  d.fa = (binned ? S.bfa : S.fa)[p];
-  d.fb = (binned ? S.bfb : S.fb)[p];
-  d.vq = (binned ? S.bvq : S.vq)[p];
-  d.fc = (binned ? S.bfc : S.fc)[p];
+  d.fa = __ldcs((binned ? S.bfa : S.fa) + p);
+  d.fb = __ldcs((binned ? S.bfb : S.fb) + p);
+  d.vq = __ldcs((binned ? S.bvq : S.vq) + p);
+  d.fc = __ldcs((binned ? S.bfc : S.fc) + p);
   return d;
 }
 
@@ -774,7 +776,7 @@ __device__ __forceinline__ void advance_particle(const SceneDev& S, int p, const
   float lam[3];
   float q[4] = {def.vq.x, def.vq.y, def.vq.z, def.vq.w};
   eigen_warm(fe_trial, q, V, lam);
-  S.vq[p] = make_float4(q[0], q[1], q[2], q[3]);
+  __stcs(&S.vq[p], make_float4(q[0], q[1], q[2], q[3]));
   // With FE_trial = W S V^T and B = FE_trial V = W S (columns of norm
   // sigma_i), the clamped F_E' = W clamp(S) V^T = B diag(clamp(sigma)/sigma) V^T
   // and the polar rotation R = W V^T = B diag(1/sigma) V^T: the sort and QR
@@ -816,8 +818,8 @@ __device__ __forceinline__ void advance_particle(const SceneDev& S, int p, const
   vv.x = v[0];
   vv.y = v[1];
   vv.z = v[2];
-  S.xm[p] = xm;
-  S.vv[p] = vv;
+  __stcs(&S.xm[p], xm);
+  __stcs(&S.vv[p], vv);
   store_fe(S, p, out.fe, out.jp);
   out.xm = xm;
   out.vv = vv;

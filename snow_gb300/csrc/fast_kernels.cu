@@ -448,9 +448,10 @@ __global__ void __launch_bounds__(kItemMax, 2) k_g2p2g(const SceneDev* __restric
   }
   uint32_t phase = 0;
   int par = 0;
+  bool run_start = true;  // uniform across the CTA
   for (int u = u0; u < u1; u++, par ^= 1) {
     __syncthreads();  // this item's queue entry is written; the last flush is done
-    const bool run_start = !sh.next_same;  // uniform across the CTA
+
     const int s = sh.scene_q[par];
     const SceneDev& S = scenes[s];
     if (s != sh.coll_scene) {  // uniform across the CTA
@@ -538,18 +539,24 @@ __global__ void __launch_bounds__(kItemMax, 2) k_g2p2g(const SceneDev* __restric
         atomicMax(&sh.seen[2], ba);
       }
     }
-    if (!p2g_tile_accumulate<kP2gFull, true>(sh, S, bx, by, bz, have, q, wn, nbase, sh.fscale)) {
-      stage_abort(sh, S);  // a copy wait ran out: this item's particles keep their state, the CTA stops
-      return;
-    }
-    if (lastw) {
+    // the next item's queue entry: every thread read this one's at the loop
+    // top, and the accumulation's barriers publish it before the flush
+    // decision below
+    if (lastw) {  // kept in shared memory, not registers, across the accumulation
+      sh.next_slot[lane] = slot;
       if (lane == 0) {
         sh.item_q[par ^ 1] = itn;
         sh.scene_q[par ^ 1] = sn;
         sh.next_same = same ? 1 : 0;
+        sh.next_issue = un < u1 && !same ? 1 : 0;
       }
-      if (un < u1 && !same) stage_issue(sh, scenes[sn], lane < 27 ? slot : -1);  // uniform in the warp
     }
+    if (!p2g_tile_accumulate<kP2gFull, true>(sh, S, bx, by, bz, have, q, wn, nbase, sh.fscale)) {
+      stage_abort(sh, S);  // a copy wait ran out: this item's particles keep their state, the CTA stops
+      return;
+    }
+    if (lastw && sh.next_issue)  // uniform in the warp
+      stage_issue(sh, scenes[sh.scene_q[par ^ 1]], lane < 27 ? sh.next_slot[lane] : -1);
     if (threadIdx.x == 0) {  // only maxima above what this CTA already recorded go to HBM
       unsigned* cur[3] = {&S.fix->m_cur, &S.fix->v_cur, &S.fix->a_cur};
 #pragma unroll
@@ -559,8 +566,9 @@ __global__ void __launch_bounds__(kItemMax, 2) k_g2p2g(const SceneDev* __restric
           sh.pushed[k] = sh.seen[k];
         }
     }
-    __syncthreads();  // next_same is visible
-    if (!sh.next_same) p2g_tile_flush<kP2gFull>(sh, S, bx, by, bz);
+    const bool cont = sh.next_same != 0;  // uniform across the CTA
+    if (!cont) p2g_tile_flush<kP2gFull>(sh, S, bx, by, bz);
+    run_start = !cont;
   }
 }
 

@@ -118,7 +118,7 @@ struct snow_batch {
   std::vector<int> versions;
   long long total_blocks = 0;
   int step_count = 0;
-  std::map<int, cudaGraphExec_t> graphs;  // phase (step % sort_interval) -> graph
+  std::map<int, cudaGraphExec_t> graphs;  // 0: the step that re-bins every scene, 1: the others
   std::vector<float> g_dt;
   int g_threads = 0;
   size_t bytes = 0;
@@ -1473,19 +1473,23 @@ snow_status batch_refresh(snow_batch* b, const double* dt) {
   return SNOW_OK;
 }
 
-void batch_enqueue_step(snow_batch* b, int phase, int interval, cudaStream_t st) {
+void batch_enqueue_step(snow_batch* b, bool bin_all, cudaStream_t st) {
   const int n = (int)b->scenes.size();
   int* pre = b->d_prefix;
   int* items = pre;
   int* active = pre + (n + 1);
   int* blocks = pre + 3 * (n + 1);
   fast_begin_step(b->d_scenes, n, true, st);
-  // re-bin a staggered subset of scenes each step; the scenes' binnings are
-  // independent, so they run on side streams (parallel branches of the
-  // step's graph) and join before the compaction
+  // every scene re-binned in the same step, every sort_interval steps, so
+  // the other steps run the fused kernel's plain instantiation (re-binning a
+  // staggered subset of the scenes each step made every step take the
+  // binned one: 3% slower on 16 scenes of 2M-8M particles and on 64 of
+  // 10k-500k, A/B on one GPU); the scenes' binnings are independent, so they
+  // run on side streams (parallel branches of the step's graph) and join
+  // before the compaction
   std::vector<int> bins;
-  for (int i = 0; i < n; i++)
-    if ((i % interval) == phase) bins.push_back(i);
+  if (bin_all)
+    for (int i = 0; i < n; i++) bins.push_back(i);
   snow_ctx* ctx = b->ctx;
   if (bins.size() < 2) {
     for (int i : bins) fast_bin(b->scenes[i], st, true);
@@ -1551,16 +1555,17 @@ snow_status snow_batch_step(snow_batch* b, const double* dt, int n_steps) {
       r = batch_refresh(b, dt);
       if (r) return r;
     }
-    auto it = b->graphs.find(phase);
+    const int key = phase == 0 ? 0 : 1;  // a step that re-bins every scene, or none
+    auto it = b->graphs.find(key);
     if (it == b->graphs.end()) {
       cudaGraph_t graph;
       cudaGraphExec_t exec;
       CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-      batch_enqueue_step(b, phase, interval, st);
+      batch_enqueue_step(b, phase == 0, st);
       CK(cudaStreamEndCapture(st, &graph));
       CK(cudaGraphInstantiate(&exec, graph, 0));
       cudaGraphDestroy(graph);
-      it = b->graphs.emplace(phase, exec).first;
+      it = b->graphs.emplace(key, exec).first;
     }
     CK(cudaGraphLaunch(it->second, st));
     b->step_count++;
