@@ -152,6 +152,18 @@ snow_status cuda_fail(snow_ctx* c, cudaError_t e, const char* what) {
     if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #x); \
   } while (0)
 
+// The device address of page-locked host memory (the caller pinned it: the
+// GPU reads and writes it directly over the CPU-GPU link), or nullptr for
+// pageable memory, which goes through a device staging buffer.
+void* pinned_device_ptr(const void* host) {
+  cudaPointerAttributes a{};
+  if (!host || cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 snow_status dalloc(snow_ctx* ctx, std::vector<std::pair<void*, size_t>>& owner, size_t& owner_bytes, size_t bytes,
                    void** out) {
   *out = nullptr;
@@ -828,29 +840,33 @@ snow_status snow_scene_upload(snow_scene* s, const float* x, const float* v, con
     s->uploaded = true;
     return SNOW_OK;
   }
-  // the caller's arrays go to a staging buffer as they are (one copy each,
-  // straight from pinned memory when the caller's is) and are packed into
-  // the particle streams on the device
+  // the pack kernel reads the caller's arrays where they lie when they are
+  // pinned; pageable ones are first copied as they are to a staging buffer
   s->sd.n = (int)n;
   if (n > 0) {
-    const size_t words = n * (3 + 3 + 1 + (FE ? 9 : 0) + (FP ? 9 : 0));
+    const float* in[5] = {x, v, m, FE, FP};
+    const size_t width[5] = {3, 3, 1, 9, 9};
+    const float* dev[5] = {};
+    size_t words = 0;
+    for (int k = 0; k < 5; k++) {
+      if (!in[k]) continue;
+      dev[k] = static_cast<const float*>(pinned_device_ptr(in[k]));
+      if (!dev[k]) words += width[k] * n;
+    }
     std::vector<std::pair<void*, size_t>> tmp;
     size_t tmp_bytes = 0;
     float* stage = nullptr;
     st = dalloc(ctx, tmp, tmp_bytes, words * sizeof(float), (void**)&stage);
     if (st) return st;
-    float* dx = stage;
-    float* dv = dx + 3 * n;
-    float* dm = dv + 3 * n;
-    float* dfe = FE ? dm + n : nullptr;
-    float* dfp = FP ? (FE ? dfe + 9 * n : dm + n) : nullptr;
-    cudaError_t e = cudaMemcpyAsync(dx, x, 3 * n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(dv, v, 3 * n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(dm, m, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
-    if (e == cudaSuccess && FE) e = cudaMemcpyAsync(dfe, FE, 9 * n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
-    if (e == cudaSuccess && FP) e = cudaMemcpyAsync(dfp, FP, 9 * n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < 5 && e == cudaSuccess; k++) {
+      if (!in[k] || dev[k]) continue;
+      e = cudaMemcpyAsync(stage, in[k], width[k] * n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+      dev[k] = stage;
+      stage += width[k] * n;
+    }
     if (e == cudaSuccess) {
-      fast_pack(dx, dv, dm, dfe, dfp, n, s->sd, ctx->stream);
+      fast_pack(dev[0], dev[1], dev[2], dev[3], dev[4], n, s->sd, ctx->stream);
       e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);  // the caller may reuse its arrays
@@ -1143,33 +1159,33 @@ snow_status snow_scene_download(snow_scene* s, float* x, float* v, float* FE, fl
   }
   if (FP) return fail(ctx, SNOW_EUNSUPPORTED, "F_P is not kept in SNOW_MODE_FAST (J_p is)");
   if (n == 0) return SNOW_OK;
-  // unpacked on the device into upload order, then one copy per requested
-  // array straight into the caller's memory (a DMA when it is pinned)
-  const size_t words = n * ((x ? 3 : 0) + (v ? 3 : 0) + (FE ? 9 : 0) + (Jp ? 1 : 0) + (volume ? 1 : 0));
-  if (words == 0) return SNOW_OK;
+  // unpacked on the device into upload order in a staging buffer, then one
+  // copy per requested array into the caller's memory (a DMA when it is
+  // pinned; the unpack kernel writing pinned memory directly was 6x slower:
+  // its per-particle stores cross the CPU-GPU link in small pieces; the
+  // copies spread over several streams were no faster than in one)
+  if (!x && !v && !FE && !Jp && !volume) return SNOW_OK;
+  float* out[5] = {x, v, FE, Jp, volume};
+  const size_t width[5] = {3, 3, 9, 1, 1};
+  float* dev[5] = {};
+  size_t words = 0;
+  for (int k = 0; k < 5; k++)
+    if (out[k]) words += width[k] * n;
   std::vector<std::pair<void*, size_t>> tmp;
   size_t tmp_bytes = 0;
   float* stage = nullptr;
   snow_status st = dalloc(ctx, tmp, tmp_bytes, words * sizeof(float), (void**)&stage);
   if (st) return st;
-  float* p = stage;
-  float* dx = x ? p : nullptr;
-  p += x ? 3 * n : 0;
-  float* dv = v ? p : nullptr;
-  p += v ? 3 * n : 0;
-  float* dfe = FE ? p : nullptr;
-  p += FE ? 9 * n : 0;
-  float* djp = Jp ? p : nullptr;
-  p += Jp ? n : 0;
-  float* dvol = volume ? p : nullptr;
-  fast_unpack(s->sd_dev, n, dx, dv, dfe, djp, dvol, ctx->stream);
+  for (int k = 0; k < 5; k++) {
+    if (!out[k]) continue;
+    dev[k] = stage;
+    stage += width[k] * n;
+  }
+  fast_unpack(s->sd_dev, n, dev[0], dev[1], dev[2], dev[3], dev[4], ctx->stream);
   cudaError_t e = cudaGetLastError();
-  const std::pair<float*, float*> out[5] = {{x, dx}, {v, dv}, {FE, dfe}, {Jp, djp}, {volume, dvol}};
-  const size_t width[5] = {3, 3, 9, 1, 1};
   for (int k = 0; k < 5 && e == cudaSuccess; k++)
-    if (out[k].first)
-      e = cudaMemcpyAsync(out[k].first, out[k].second, width[k] * n * sizeof(float), cudaMemcpyDeviceToHost,
-                          ctx->stream);
+    if (out[k])
+      e = cudaMemcpyAsync(out[k], dev[k], width[k] * n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   dfree_all(ctx, tmp, tmp_bytes);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "snow_scene_download");
