@@ -50,8 +50,7 @@ BYTES_GRID = (0, 40)
 TRAFFIC_MEASURED = {(1 << 20, 256): 143.3e6}
 INSTRUCTIONS_MEASURED = {(1 << 20, 256): 173.9e6}
 TRAFFIC_SOURCE = ("not counted in this run: a separate ncu --set full capture of one k_g2p2g launch of this "
-                  "workload (sort interval 8, 256 particles per item, 2 CTAs per SM; "
-                  "profiles/k_g2p2g_two_snowballs_1M_256.md)")
+                  "workload (sort interval 8, 256 particles per item, 2 CTAs per SM)")
 # warp-instruction issue peak: 152 SMs x 4 schedulers x 2.07 GHz
 ISSUE_PEAK = 152 * 4 * 2.07e9
 # FP32 peak: 152 SMs x 128 lanes x 2 flops per FMA x 2.07 GHz; the algorithmic
