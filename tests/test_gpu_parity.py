@@ -148,6 +148,29 @@ def test_fast_single_step_with_sphere_and_moving_colliders_within_1e5(ctx):
     assert np.abs(g.colliders() - o.colliders()).max() <= 1e-6
 
 
+@gpu
+def test_fast_step_with_particles_on_the_wide_path_within_1e5(ctx):
+    """A snow block moving down at 2 m/s whose bottom layer starts inside a
+    static sphere collider: in the first step the collider stops that
+    snow, whose stress jumps from nothing to far past what the set-up's
+    magnitudes allowed, so its particles' force contributions outgrow the
+    fixed-point scales' fast range and are scattered with int64
+    contributions rounded in double precision (the wide path;
+    snow_phase_times.wide counts them). The step matches the FP64 oracle
+    within the single-step bound."""
+    from snow_gb300 import native as N
+    s = scenes.snow_block_on_sphere(0x5EED0021, 32768, 64, gap=-3.0 / 64, v0=(0.0, -2.0, 0.0))
+    g = sim(ctx, s, N.MODE_FAST).upload().init()
+    y0 = g.download()
+    g.phase_times(reset=True)
+    y1 = g.step(s.dt, 1).download()
+    wide = g.phase_times(reset=True)["wide"]
+    o = _oracle_from_gpu_state(s, y0)
+    flip = o.step_with_flip_scale()
+    check_step(y1, o.state(), flip, strict=False)
+    assert wide > 100, wide
+
+
 def _deformed_restart(ctx, warm_steps, seed=41):
     """The FP64 oracle advanced `warm_steps` through an impact on the floor,
     then both the oracle and a FAST GPU scene restarted from its state
