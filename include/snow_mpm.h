@@ -174,7 +174,9 @@ void snow_scene_destroy(snow_scene* s);
 size_t snow_scene_footprint(const snow_params* p, size_t n);
 
 /* x, v: N x 3; m: N; FE, FP: N x 9 row-major or NULL for identity; N >= 1
- * (SNOW_EINVAL otherwise). */
+ * (SNOW_EINVAL otherwise). FAST mode reads arrays in page-locked (pinned)
+ * host memory in place; pageable ones are copied to a device staging buffer
+ * first. The arrays may be reused once the call returns. */
 snow_status snow_scene_upload(snow_scene* s, const float* x, const float* v, const float* m, const float* FE,
                               const float* FP, size_t n);
 /* The reference's buffers as ParticleSystem::initSSBO fills them: pxm N x
