@@ -47,8 +47,8 @@ BYTES_GRID = (0, 40)
 # work split named in TRAFFIC_SOURCE, keyed by (particles, grid edge); other
 # workloads report null: DRAM bytes (read + write) per launch, and warp
 # instructions per launch for the issue roofline.
-TRAFFIC_MEASURED = {(1 << 20, 256): 143.3e6}
-INSTRUCTIONS_MEASURED = {(1 << 20, 256): 173.9e6}
+TRAFFIC_MEASURED = {(1 << 20, 256): 144.3e6}
+INSTRUCTIONS_MEASURED = {(1 << 20, 256): 173.2e6}
 TRAFFIC_SOURCE = ("not counted in this run: a separate ncu --set full capture of one k_g2p2g launch of this "
                   "workload (sort interval 8, 256 particles per item, 2 CTAs per SM)")
 # warp-instruction issue peak: 152 SMs x 4 schedulers x 2.07 GHz
