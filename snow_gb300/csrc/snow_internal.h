@@ -51,7 +51,7 @@ constexpr int kOutFields = 6;              // v* (3), d = v* - alpha p/m (3)
 // acc holds the P2G sums as integers (fixed point at per-scene power-of-two
 // scales): per node seven int64 words (m, p_x, p_y, p_z, f_x, f_y, f_z),
 // stored word-major per block. No node sum can leave the int64 range (each
-// contribution is below 2^21 or, on the wide path, 2^62), however many
+// contribution is below 2^22 or, on the wide path, 2^62), however many
 // particles pile into a cell.
 constexpr int kAccWords = kAccFields;
 constexpr int kAccBlockWords = kAccWords * kBlockNodes;    // 448 (3584 bytes)
@@ -63,7 +63,7 @@ constexpr int kOutBlockFloats = kOutFields * kBlockNodes;  // 384
 struct FixState {
   float scale[3];     // s_m, s_p, s_f of the sums now in acc (integer = round(contribution * s))
   uint32_t m_prev;    // largest particle mass, |v| and force-term bound a of the particles the
-  uint32_t v_prev;    //   previous P2G scattered (a = max over rows r of max(|A_r0|, |A_r1| + |A_r2|))
+  uint32_t v_prev;    //   previous P2G scattered (a = max over rows r of |A_r0| + |A_r1| + |A_r2|)
   uint32_t a_prev;
   uint32_t m_cur;     // the same, recorded by the P2G in flight (moved to *_prev at each step's start)
   uint32_t v_cur;
