@@ -451,7 +451,6 @@ __global__ void __launch_bounds__(kItemMax, 2) k_g2p2g(const SceneDev* __restric
   bool run_start = true;  // uniform across the CTA
   for (int u = u0; u < u1; u++, par ^= 1) {
     __syncthreads();  // this item's queue entry is written; the last flush is done
-
     const int s = sh.scene_q[par];
     const SceneDev& S = scenes[s];
     if (s != sh.coll_scene) {  // uniform across the CTA
@@ -476,9 +475,9 @@ __global__ void __launch_bounds__(kItemMax, 2) k_g2p2g(const SceneDev* __restric
     }
     const int4 it = sh.item_q[par];
     const int un = u + 1;
-    // the next item's descriptor and pool slots: loaded now, used (and put
-    // in shared memory) after this item's per-cell sums, so the loads'
-    // latency overlaps this item's work instead of delaying the last warp
+    // the next item's descriptor and pool slots: loaded now, so that the
+    // loads' latency overlaps this item's G2P instead of delaying the last
+    // warp, and put in shared memory before this item's P2G
     int sn = 0, slot = -1;
     int4 itn = make_int4(0, 0, 0, 0);
     bool same = false;
