@@ -49,8 +49,8 @@ BYTES_GRID = (0, 40)
 # instructions per launch for the issue roofline.
 TRAFFIC_MEASURED = {(1 << 20, 256): 144.3e6}
 INSTRUCTIONS_MEASURED = {(1 << 20, 256): 173.2e6}
-TRAFFIC_SOURCE = ("not counted in this run: a separate ncu --set full capture of one k_g2p2g launch of this "
-                  "workload (sort interval 8, 256 particles per item, 2 CTAs per SM)")
+TRAFFIC_SOURCE = ("not counted in this run: separate ncu --set full captures of one k_g2p2g launch of this "
+                  "workload (256 particles per item, 2 CTAs per SM; sort interval 8 and 32 alike)")
 # warp-instruction issue peak: 152 SMs x 4 schedulers x 2.07 GHz
 ISSUE_PEAK = 152 * 4 * 2.07e9
 # FP32 peak: 152 SMs x 128 lanes x 2 flops per FMA x 2.07 GHz; the algorithmic
