@@ -24,6 +24,7 @@ struct snow_ctx {
   cudaStream_t stream = nullptr;
   size_t budget = 0;
   size_t used = 0;
+  bool defer_sync = false;  // inside a run of allocations that waits for the stream once, at its end
   std::string err;
   bool profiling = false;
   bool graphs = true;  // replay each step as a captured CUDA graph
@@ -171,9 +172,10 @@ snow_status dalloc(snow_ctx* ctx, std::vector<std::pair<void*, size_t>>& owner, 
   bytes = (bytes + 255) & ~(size_t)255;
   if (ctx->budget && ctx->used + bytes > ctx->budget)
     return fail(ctx, SNOW_EBUDGET, "HBM budget exceeded");
-  // stream-ordered, then waited for, so the memory is usable from any stream
+  // stream-ordered, then waited for (here, or once at the end of a run of
+  // allocations: AllocRun), so the memory is usable from any stream
   cudaError_t e = cudaMallocFromPoolAsync(out, bytes, ctx->pool, ctx->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e == cudaSuccess && !ctx->defer_sync) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) {
     cudaGetLastError();
     *out = nullptr;
@@ -184,6 +186,19 @@ snow_status dalloc(snow_ctx* ctx, std::vector<std::pair<void*, size_t>>& owner, 
   owner.emplace_back(*out, bytes);
   return SNOW_OK;
 }
+
+// A run of allocations that waits for the stream once, when it ends (a
+// scene's buffers are a few dozen allocations).
+struct AllocRun {
+  snow_ctx* ctx;
+  bool outer;
+  explicit AllocRun(snow_ctx* c) : ctx(c), outer(!c->defer_sync) { c->defer_sync = true; }
+  ~AllocRun() {
+    if (!outer) return;
+    ctx->defer_sync = false;
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) cudaGetLastError();
+  }
+};
 
 void dfree_all(snow_ctx* ctx, std::vector<std::pair<void*, size_t>>& owner, size_t& owner_bytes) {
   for (auto& a : owner) {
@@ -285,6 +300,7 @@ snow_status push_sd(snow_scene* s) {
 
 // ---- fast-mode buffers ----------------------------------------------------
 snow_status fast_alloc_particles(snow_scene* s, size_t cap) {
+  AllocRun run(s->ctx);
   SceneDev& d = s->sd;
   snow_status st;
   if ((st = salloc(s, cap, &d.xm)) || (st = salloc(s, cap, &d.vv)) || (st = salloc(s, cap, &d.fa)) ||
@@ -314,6 +330,7 @@ snow_status fast_alloc_particles(snow_scene* s, size_t cap) {
 }
 
 snow_status fast_alloc_grid(snow_scene* s) {
+  AllocRun run(s->ctx);
   SceneDev& d = s->sd;
   snow_status st;
   const size_t nb = (size_t)d.nblocks;
@@ -342,6 +359,7 @@ snow_status fast_alloc_grid(snow_scene* s) {
 
 // The output pool (grid-update results of the active blocks).
 snow_status fast_alloc_pool(snow_scene* s, int cap_blocks) {
+  AllocRun run(s->ctx);
   SceneDev& d = s->sd;
   snow_ctx* ctx = s->ctx;
   if (d.gout) dfree_one(ctx, s, d.gout);
@@ -529,6 +547,7 @@ RefArgs& ref_args(snow_scene* s) {
 }
 
 snow_status ref_alloc(snow_scene* s, size_t cap) {
+  AllocRun run(s->ctx);
   RefArgs& a = s->ra;
   snow_status st;
   if ((st = salloc(s, cap, &a.pxm)) || (st = salloc(s, cap, &a.pv)) || (st = salloc(s, 4 * cap, &a.pfe)) ||
