@@ -142,3 +142,28 @@ def test_particles_piled_hundreds_to_a_cell_keep_exact_grid_sums(ctx):
     gmom = (m[:, None] * g.download()["v"].astype(np.float64)).sum(0)
     assert np.abs(gmom - mom).max() <= 1e-4 * np.abs(mom).max()
     g.close()
+
+
+@gpu
+def test_a_long_batched_run_stays_finite(ctx):
+    """Sixteen scenes drawn as the 64-scene batch draws them (10k-100k
+    particles, boxes and spheres thrown at up to 4 m/s into their boxes)
+    stepped 4,000 steps (0.4 s) together: the snow falls, hits the walls,
+    piles up and settles, and no particle's state turns non-finite (the
+    fixed-point sums neither wrap nor lose the momentum transfer); the total
+    kinetic energy ends far below its peak."""
+    from snow_gb300 import api
+    scs = scenes.cfg3_batch(seed=0x5EED0306, n_scenes=16, n_max=100_000)
+    sims = [api.SimScene(ctx, s).upload().init() for s in scs]
+    b = api.Batch(ctx, sims)
+    dts = [s.dt for s in scs]
+    ke = []
+    for _ in range(8):
+        b.step(500, dts)
+        st = [g.stats() for g in sims]
+        assert all(x["nonfinite"] == 0 for x in st)
+        ke.append(sum(x["kinetic_energy"] for x in st))
+    assert all(np.isfinite(ke)) and ke[-1] < 0.5 * max(ke), ke
+    b.close()
+    for g in sims:
+        g.close()
